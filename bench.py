@@ -1,0 +1,409 @@
+"""Benchmark of the coupled LLG + Brownian-dynamics step on GB300.
+
+Workload (one "step" = one Heun time step of the whole system): the single
+large instance of the benchmark suite -- N = 32768 magnetite particles with
+log-normal core diameters (median 20 nm, sigma 0.2), 5 nm shell, volume
+fraction 0.10, static 20 mT field, dt = 1e-12 s, Philox thermal noise,
+Ewald parameters for 1e-5 relative force error (timed autotune over the
+error model), mixed precision.  Synthetic, seeded inputs (log-normal radii,
+random sequential addition, uniform orientations).
+
+Prints one JSON line (see the keys below).  `--impl reference` times the
+reference's CPU algorithm (the C restatement in oracle/, single-threaded per
+replica, all host threads as independent replicas) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = ("single large instance: N=32768 magnetite, log-normal core diameters (median 20 nm, sigma 0.2), "
+            "5 nm shell, volume fraction 0.10, static 20 mT, dt=1e-12 s, T=300 K, viscosity 1e-3 Pa s, "
+            "Philox thermal noise, Ewald at 1e-5 relative force error")
+
+# Algorithmic FLOPs (FMA = 2) per unit of work, counted from the formulas.
+FLOPS_PAIR_FULL = 113.0   # per unordered pair: erfc/exp terms, field on both, force, pressure
+FLOPS_PAIR_FIELD = 58.0   # per unordered pair: field on both particles
+FLOPS_KSF = 11.0          # per (k, particle): phase step (6), weight (1), two accumulations (4)
+FLOPS_KSCAT_FULL = 21.0   # per (k, particle): phase step, field (6), force (9)
+FLOPS_KSCAT_FIELD = 12.0  # per (k, particle): phase step, field
+BYTES_CELLS = 60.0        # per particle (+8 per cell)
+BYTES_HEUN1 = 252.0       # per particle
+BYTES_HEUN2 = 404.0       # per particle
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    p.add_argument("--n", type=int, default=32768)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--autotune", type=int, default=0, help="candidate cutoffs timed (0: the cost-model choice, the same one the reference arm uses)")
+    return p.parse_args()
+
+
+def workload_config(n, seed):
+    from md_sim_wolfschwenger_gb300 import MD_NOISE_PHILOX, MD_PREC_MIXED, Configuration
+    cfg = Configuration.default()
+    cfg.set(SIZE_DIST=1, rMagMean=1e-8, sigmaLog=0.2, dShell=5e-9, volFrac=0.10, magFluxDens=0.02, tMag=1.0,
+            tRelax=0.0, deltaTinit=1e-12, satMag=4.8e5, anisEn=1.1e4, magDamp=0.1, temp=300.0, visOverride=1e-3,
+            numbPartOverride=n, errTolEwald=1e-5, seed=seed, SOLVER=0, ENABLE_MOBILIZATION=1, ENABLE_THERM_FIELD=1,
+            ENABLE_THERM_TORQUE=1, ENABLE_THERM_FORCE=1, ENABLE_COATING_POT=0, INIT_CONFIG_ROT=2,
+            INIT_CONFIG_TRANS=1, precision=MD_PREC_MIXED, noise=MD_NOISE_PHILOX)
+    return cfg
+
+
+def workload_state(n, seed):
+    from md_sim_wolfschwenger_gb300 import init
+    rng = np.random.default_rng(1000 + seed)
+    rMag = init.lognormal_radii(n, 1e-8, 0.2, rng)
+    rHydr = rMag + 5e-9
+    L = init.box_length(rHydr, 0.10)
+    pos = init.rsa_positions(L, rHydr, rng)
+    mm = init.uniform_directions(n, rng)
+    ea = init.uniform_directions(n, rng)
+    return rMag, rHydr, L, pos, mm, ea
+
+
+def oracle_ini(n, seed):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_io
+    return ref_io.ini_dict(volFrac=0.10, magFluxDens=0.02, tMag=1.0, seed=seed)
+
+
+# ------------------------------------------------------------ clocks
+
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# -------------------------------------------------------------- dist
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+    return rank, ws, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(v, ws):
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------- cpu arms
+
+
+def cpu_baseline_port(n, sysd, ewald, seed, threads=1, steps=1):
+    """The oracle's restatement of the reference step (all-pairs list,
+    sequential overlap push, FP64) timed on host cores; `threads` independent
+    replicas run concurrently (ctypes releases the GIL)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    rMag, rHydr, L, pos, mm, ea = sysd
+    alpha, rc, kc = ewald
+    d = O.derive(oracle_ini(n, seed))
+    d["vis"] = 1e-3
+    d["ENABLE_THERM_TORQUE"] = d["ENABLE_THERM_FIELD"] = d["ENABLE_THERM_FORCE"] = True
+    d["magDamp"], d["satMag"], d["anisEn"] = 0.1, 4.8e5, 1.1e4
+    reps = []
+    for t in range(threads):
+        o = O.Oracle(d, rMag, rHydr, L, alpha, rc, kc, vis=1e-3, overlap_mode=0)
+        o.set_state(pos, mm, ea)
+        reps.append(o)
+    times = []
+    for s in range(steps):
+        ths = [threading.Thread(target=r.step, args=(1e-12, 2, None, seed + i)) for i, r in enumerate(reps)]
+        t0 = time.perf_counter()
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        times.append(time.perf_counter() - t0)
+    per = [r.last_seconds() for r in reps]
+    for r in reps:
+        r.close()
+    return times, per
+
+
+def run_reference(args):
+    rank, ws, _ = dist_init()
+    if rank != 0:
+        return
+    n = args.n
+    sysd = workload_state(n, 1)
+    from md_sim_wolfschwenger_gb300 import MD_PREC_MIXED
+    import ctypes as C
+    import md_sim_wolfschwenger_gb300 as m
+    cfg = workload_config(n, 1)
+    a, r, k, ef, et, lb = (C.c_double(), C.c_double(), C.c_int64(), C.c_double(), C.c_double(), C.c_double())
+    P = lambda x: x.ctypes.data_as(C.POINTER(C.c_double))
+    m._lib.check(m.lib().md_ewald_params_host(C.byref(cfg.c), n, P(sysd[0]), P(sysd[1]), -1.0, C.byref(a),
+                                                C.byref(r), C.byref(k), C.byref(ef), C.byref(et), C.byref(lb)))
+    del MD_PREC_MIXED
+    threads = max(1, min(os.cpu_count() or 1, 16))
+    warm, steps = min(args.warmup, 1), max(1, min(args.steps, 3))
+    if warm:
+        cpu_baseline_port(n, sysd, (a.value, r.value, k.value), 7, threads=threads, steps=warm)
+    times, _ = cpu_baseline_port(n, sysd, (a.value, r.value, k.value), 7, threads=threads, steps=steps)
+    total = sum(times)
+    value = threads * n * steps / total
+    sample = (f"{steps} timed step(s) (+{warm} warm-up) of the full N={n} workload on each of {threads} "
+              f"concurrent single-threaded replicas; all-pairs list and FP64 Ewald as the reference")
+    line = {"impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1e3 * total / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "n": n,
+                                                     "ewald": {"alpha_L": a.value * lb.value,
+                                                               "rc_over_L": r.value / lb.value, "kc": k.value}},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------- our arm
+
+
+def run_ours(args):
+    rank, ws, local = dist_init()
+    import torch
+    from md_sim_wolfschwenger_gb300 import (MD_NOISE_PHILOX, MD_PREC_FP64, MD_PREC_MIXED, Simulation,
+                                            calibrate_fp32, select_device)
+    select_device(local)
+    torch.cuda.set_device(local)
+    n = args.n
+    prec = MD_PREC_FP64 if args.precision == "fp64" else MD_PREC_MIXED
+    seed = 1 + rank
+    cfg = workload_config(n, seed)
+    rMag, rHydr, L, pos, mm, ea = sysd = workload_state(n, seed)
+    sim = Simulation(cfg, n, prec, rMag=rMag, rHydr=rHydr)
+    sim.set_state(pos, mm, ea)
+    if args.autotune > 0:
+        alpha, rc, kc, _ = sim.autotune_ewald(args.autotune)
+    else:
+        alpha, rc, kc, _, _ = sim.ewald_params()
+        sim.set_ewald(alpha, rc, kc)
+    _, _, _, errF, errT = sim.ewald_params(rc)
+    sim.set_noise(MD_NOISE_PHILOX, seed)
+    sim.profile(True)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    sim.step(args.warmup, 1e-12)
+    sim.sync()
+    launches_per_step = sim.launches() // max(1, args.warmup)
+    seg_sum = None
+    clocks = ClockSampler(local)
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks.start()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        sim.step(1, 1e-12)
+        seg = sim.profile_read()
+        total_ms += sum(seg.values())
+        seg_sum = seg if seg_sum is None else {k: seg_sum[k] + v for k, v in seg.items()}
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop()
+    total_ms = allmax(total_ms, ws)
+    value = ws * n * args.steps / (total_ms * 1e-3)
+    seg_mean = {k: v / args.steps for k, v in seg_sum.items()}
+    pairs = sim.pairs()
+    nk_real = len(sim.debug_structure_factor())
+
+    # continuous run (graph replays back to back, no flush) for reference
+    sim.profile(False)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ext = torch.cuda.ExternalStream(sim.stream())
+    with torch.cuda.stream(ext):
+        e0.record()
+    sim.step(args.steps, 1e-12)
+    with torch.cuda.stream(ext):
+        e1.record()
+    torch.cuda.synchronize()
+    cont_ms = e0.elapsed_time(e1) / args.steps
+
+    # end to end through the C ABI with pinned host buffers, copies timed
+    host_in = [torch.empty((3, n), dtype=torch.float64).pin_memory().numpy() for _ in range(3)]
+    host_out = [torch.empty((3, n), dtype=torch.float64).pin_memory().numpy() for _ in range(3)]
+    st = sim.get_state(out=host_in)
+    ksteps = max(3, min(args.steps, 10))
+    e2e_s = 0.0
+    for _ in range(ksteps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.set_state(*host_in, reset=False)
+        sim.step(1, 1e-12)
+        sim.get_state(out=host_out)
+        e2e_s += time.perf_counter() - t0
+        for a_, b_ in zip(host_in, host_out):
+            a_[...] = b_
+    e2e_s = allmax(e2e_s, ws)
+    e2e = {"value": ws * n * ksteps / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 3 * 24 * n,
+           "d2h_bytes_per_step": 3 * 24 * n, "steps": ksteps}
+    del st
+
+    # roofline of every segment; the dominant one is reported
+    peak_fp32 = calibrate_fp32()
+    hbm_peak = None
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except Exception:
+        pass
+    work = {"real_full": ("fp32", pairs * FLOPS_PAIR_FULL), "real_field": ("fp32", pairs * FLOPS_PAIR_FIELD),
+            "ksf_full": ("fp32", nk_real * n * FLOPS_KSF), "ksf_field": ("fp32", nk_real * n * FLOPS_KSF),
+            "kscat_full": ("fp32", nk_real * n * FLOPS_KSCAT_FULL),
+            "kscat_field": ("fp32", nk_real * n * FLOPS_KSCAT_FIELD),
+            "cells": ("hbm", n * BYTES_CELLS), "heun1": ("hbm", n * BYTES_HEUN1), "heun2": ("hbm", n * BYTES_HEUN2)}
+    segs = {}
+    for k, ms in seg_mean.items():
+        ent = {"ms": ms}
+        if k in work and ms > 0:
+            kind, amount = work[k]
+            if kind == "fp32":
+                ach = amount / (ms * 1e-3) / 1e12
+                ent.update(bound="fp32", achieved=ach, unit="TFLOP/s", peak=peak_fp32, frac=ach / peak_fp32)
+            else:
+                ach = amount / (ms * 1e-3) / 1e9
+                ent.update(bound="hbm", achieved=ach, unit="GB/s", peak=hbm_peak,
+                           frac=(ach / hbm_peak) if hbm_peak else None)
+        segs[k] = ent
+    dom = max((k for k in segs if k in work), key=lambda k: segs[k]["ms"])
+    traffic = None
+    try:
+        traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(dom)
+    except Exception:
+        pass
+    d = segs[dom]
+    roofline = {"kernel": dom, "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"], "unit": d["unit"],
+                "frac": d["frac"], "traffic": traffic,
+                "peak_source": ("measured FP32 FMA-chain kernel in this process (MEASURED_PEAKS.json has no FP32 "
+                                "figure; this kernel class is FP32/SFU-issue bound, not HBM or tensor)"
+                                if d["bound"] == "fp32" else "MEASURED_PEAKS.json hbm_gbs")}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        times, per = cpu_baseline_port(n, sysd, (alpha, rc, kc), seed, threads=1, steps=1)
+        cpu = {"value": n / per[0], "unit": "particle-steps/s", "cores": 1, "kind": "port",
+               "sample": f"1 step of the same N={n} system and Ewald parameters, single thread (the reference "
+                         f"is single-threaded): all-pairs list, FP64, Philox noise; {per[0]:.1f} s"}
+
+    if rank == 0:
+        line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if prec == MD_PREC_FP64 else "f32",
+                "precision": ("fp64 (plain)" if prec == MD_PREC_FP64 else
+                              "mixed: FP32 pair maths, phases, scatter and integrator; FP64 structure-factor "
+                              "sums across chunks, self/surface terms, positions, reductions"),
+                "data": "synthetic (seeded log-normal radii, random sequential addition, uniform orientations)",
+                "config": {"workload": WORKLOAD, "n": n, "lBox_m": L, "replicas_per_gpu": 1,
+                           "parallelism": f"replicas x{ws}" if ws > 1 else "single instance",
+                           "ewald": {"alpha_L": alpha * L, "rc_over_L": rc / L, "kc": kc,
+                                     "pred_force_err_rel_contact": errF, "pred_torque_err_rel_contact": errT,
+                                     "pairs": pairs, "k_vectors": nk_real},
+                           "l2": "flushed between timed steps (256 MiB write); step time from in-graph CUDA events "
+                                 "on the library's stream"},
+                "e2e": e2e, "roofline": roofline, "segments": segs,
+                "continuous": {"ms_per_step": cont_ms, "value": ws * n / (cont_ms * 1e-3),
+                               "note": "graph replays back to back without L2 flush"},
+                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches_per_step * args.steps}
+        print(json.dumps(line), flush=True)
+    sim.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,258 @@
+/* md_gb300.h -- C ABI of the GB300 implementation of the coupled LLG +
+ * Brownian-dynamics time step for magnetic nanoparticles.
+ *
+ * This is the drop-in boundary for the reference simulator
+ * MD_Sim_Wolfschwenger (C++, single-threaded, FP64).  Every entry point names
+ * the reference interface it replaces (paths relative to that repository).
+ * Plain pointers and sizes only; all arrays are FP64 N x 3 column-major
+ * (x[0..N), y[0..N), z[0..N)), which is the memory layout of the reference's
+ * Eigen ArrayXXd members (src/typedefs.h:37-47), so a caller can pass
+ * `pWorkVar->coordsTrans.pos.data()` directly.
+ *
+ * Every function returns an md_status; md_strerror() describes it and
+ * md_last_error() returns the context's last message.  Nothing here calls
+ * exit(): the reference's `cout` + `exit(-1)` error paths
+ * (src/interaction.cpp:49-50, 235) become MD_ERR_INVALID / MD_ERR_CONFIG.
+ *
+ * Threading: a context owns one CUDA stream on one device; calls on one
+ * context must be serialised by the caller (the reference is single-threaded
+ * and non-reentrant, src/simulation.cpp:12-20).  Different contexts are
+ * independent.
+ */
+#ifndef MD_GB300_H
+#define MD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum md_status {
+  MD_OK = 0,
+  MD_ERR_INVALID = 1,     /* bad argument or state                         */
+  MD_ERR_CUDA = 2,        /* CUDA runtime error (message in md_last_error)  */
+  MD_ERR_NOMEM = 3,       /* device or host allocation failed / over budget */
+  MD_ERR_NONFINITE = 4,   /* NaN/Inf detected in fields, forces or state    */
+  MD_ERR_CONFIG = 5,      /* configuration file missing or malformed        */
+  MD_ERR_UNSUPPORTED = 6, /* feature not available in this build            */
+  MD_ERR_NO_DEVICE = 7    /* no CUDA device visible                          */
+} md_status;
+
+/* Arithmetic of the hot path. */
+enum {
+  MD_PREC_FP64 = 0,  /* everything FP64: the plain GPU path               */
+  MD_PREC_MIXED = 1  /* FP32 pair math, sincos and integrator; FP64
+                        structure-factor sums, self/surface terms,
+                        positions and reductions                           */
+};
+
+/* Thermal noise source (DefThermFluct, src/simulation.cpp:563-603). */
+enum {
+  MD_NOISE_OFF = 0,      /* no thermal torque, field or force                 */
+  MD_NOISE_UPLOADED = 1, /* caller supplies unit normals per step (the
+                            reference's own Rand::normal stream can be fed) */
+  MD_NOISE_PHILOX = 2    /* counter-based Philox4x32-10 on the device        */
+};
+
+/* External field program (DefExtField, src/simulation.cpp:546-556). */
+enum {
+  MD_FIELD_STEP = 0,  /* B = magFluxDens e_z for t < tMag, else 0 (reference) */
+  MD_FIELD_SIN = 1    /* B = fieldAmp sin(2 pi fieldFreq t) e_z (extension)   */
+};
+
+/* Every key of the reference's configuration.ini (src/configuration.ini:1-79,
+ * read by Configuration::Configuration, src/configuration.cpp:6-70) and every
+ * derived constant (src/configuration.cpp:71-84), plus optional extension
+ * keys from an extra [gb300] section.  Integers and flags are int64_t. */
+typedef struct md_config {
+  /* [initial_configuration] [size_distribution] [mobilization] */
+  int64_t INIT_CONFIG_ROT, INIT_CONFIG_TRANS, READ_FROM_FILE, SIZE_DIST, ENABLE_MOBILIZATION;
+  /* [thermal_fluctuations] [interactions] [adaptive_timestepping_solver] */
+  int64_t ENABLE_THERM_FIELD, ENABLE_THERM_TORQUE, ENABLE_THERM_FORCE, seed, ENABLE_COATING_POT, SOLVER;
+  /* [particle_properties] */
+  int64_t npDim;
+  double magDamp, temp, satMag, anisEn;
+  /* [assemble_properties] [steric_repulsion] [vdw_attraction] [electrostat_repulsion] */
+  double rMagMean, dShell, volFrac, densSurfMol, hamaker, z_valency, epsilon_r, gamma_0, conc;
+  /* [time_settings] [external_magnetic_field_t] [solver_settings] */
+  double tMag, tRelax, deltaTinit, magFluxDens, absTol, deltaTmin, deltaTmax;
+  /* [long_range_interactions] [short_range_interactions] [output_settings] */
+  double errTolEwald, errTolSR, npCoords;
+  /* [physical_constants] [faster_calculation] */
+  double my_pi, kB, gyroMr, avogadro, epsilon_0, el, facEwald;
+  /* derived (src/configuration.cpp:39, 64, 71-84) */
+  int64_t numbPart;
+  double mu0, effLenSurfMol, velMmConst, anisConst, sterRepFac, gamma, epsilon, kappa;
+  double electrostatRepFac, irPi, vis, sigma, tEnd;
+  /* [gb300] extension keys; 0 means "reference behaviour" */
+  int64_t numbPartOverride; /* particle count that is not npDim^3            */
+  double visOverride;       /* viscosity instead of the Vogel formula        */
+  double sigmaLog;          /* log-normal sigma of ln(rMag) instead of sigma */
+  int64_t fieldKind;        /* MD_FIELD_STEP or MD_FIELD_SIN                 */
+  double fieldAmp, fieldFreq;
+  int64_t precision;        /* MD_PREC_*                                      */
+  int64_t noise;            /* MD_NOISE_*; default PHILOX                     */
+} md_config;
+
+typedef struct md_ctx md_ctx;
+
+/* ------------------------------------------------------------ status */
+const char* md_strerror(int status);
+/* Copies the context's last error message (or the process-wide one when ctx
+ * is NULL) into buf; returns the status that produced it. */
+int md_last_error(const md_ctx* ctx, char* buf, size_t len);
+/* Library version string and the CUDA architecture it was built for. */
+const char* md_version(void);
+
+/* ------------------------------------------------------ configuration */
+/* Replaces Configuration::getInstance() + its getters
+ * (src/configuration.h:12-180, src/configuration.cpp:6-93).  Unlike the
+ * reference, the path is explicit (the reference reads ../configuration.ini
+ * relative to the working directory, src/configuration.cpp:6) and a parse
+ * error is returned instead of leaving zeroed members. */
+int md_config_load_ini(const char* path, md_config* cfg);
+/* The reference's shipped configuration.ini values (src/configuration.ini). */
+int md_config_default(md_config* cfg);
+/* Recomputes the derived constants (src/configuration.cpp:39, 64, 71-84)
+ * after fields were edited. */
+int md_config_derive(md_config* cfg);
+/* Effective particle count: numbPartOverride if set, else npDim^3. */
+int64_t md_config_numb_part(const md_config* cfg);
+/* sizeof(md_config), for bindings that mirror the struct. */
+size_t md_config_size(void);
+
+/* ------------------------------------------------------------ context */
+/* Makes `device` the calling thread's current CUDA device for this library
+ * (contexts are created on the current device). */
+int md_select_device(int device);
+/* Creates a context for n particles on the current CUDA device
+ * (the storage InitSimulation sizes, src/simulation.cpp:37-113). */
+int md_ctx_create(const md_config* cfg, int64_t n, int precision, md_ctx** out);
+int md_ctx_destroy(md_ctx* ctx);
+/* The context's CUDA stream (cudaStream_t) for callers that order work. */
+int md_ctx_stream(md_ctx* ctx, void** stream);
+/* Device bytes held by this context. */
+int md_ctx_device_bytes(const md_ctx* ctx, int64_t* bytes);
+
+/* Per-particle radii (InitParticleProps, src/simulation.cpp:118-214):
+ * derives volumes, moments, friction coefficients and easy-axis constants,
+ * and the box length L = (sum V_hydr / volFrac)^(1/3) (simulation.cpp:56-57).
+ * rHydr may be NULL: then rHydr = rMag + dShell (simulation.cpp:201). */
+int md_set_particles(md_ctx* ctx, const double* rMag, const double* rHydr);
+int md_get_box(const md_ctx* ctx, double* lBox);
+/* Overrides the box length (e.g. a restart written by another run). */
+int md_set_box(md_ctx* ctx, double lBox);
+
+/* Coordinates (CoordsTrans_S::pos, CoordsRot_S::posMm / posEa), N x 3
+ * column-major FP64.  Upload also re-anchors the diffusion reference
+ * positions like InitSimulation (simulation.cpp:108-109) when reset != 0. */
+int md_state_upload(md_ctx* ctx, const double* pos, const double* mm, const double* ea, int reset);
+int md_state_download(md_ctx* ctx, double* pos, double* mm, double* ea);
+/* Integration time and step counter (RunSimulation's tInt / steps). */
+int md_set_time(md_ctx* ctx, double t, int64_t step);
+int md_get_time(const md_ctx* ctx, double* t, int64_t* step);
+
+/* ------------------------------------------------------------- Ewald */
+/* Ewald error model of CompEwaldParams/FunRealError/FunRezError
+ * (src/interaction.cpp:164-347): for a real-space cutoff rc (metres; if
+ * rc <= 0 the cutoff is chosen by the library's cost model) returns alpha
+ * and the integer k-space cutoff kc that meet errTolEwald.  The particles
+ * must be set.  Predicted relative force/torque errors are returned when
+ * the pointers are non-NULL. */
+int md_ewald_params(md_ctx* ctx, double rc, double* alpha, double* rc_out, int64_t* kc,
+                    double* err_force, double* err_torque);
+/* Host-only form of md_ewald_params (no context, no GPU): the same error
+ * model for n particles with radii rMag (and rHydr, may be NULL); also
+ * returns the box length of InitSimulation (src/simulation.cpp:56). */
+int md_ewald_params_host(const md_config* cfg, int64_t n, const double* rMag, const double* rHydr, double rc,
+                         double* alpha, double* rc_out, int64_t* kc, double* err_force, double* err_torque,
+                         double* lBox);
+/* Sets the Ewald parameters (Params_S alpha, rCutLR, nCutLR) and derives
+ * the constants of InitEwaldConst (src/interaction.cpp:353-374). */
+int md_set_ewald(md_ctx* ctx, double alpha, double rc, int64_t kc);
+/* Times candidate cut-offs on the device and sets the fastest that meets
+ * the error model; the GPU counterpart of the timing sweep of
+ * CompEwaldParams (src/interaction.cpp:185-296). */
+int md_autotune_ewald(md_ctx* ctx, int ncand, double* alpha, double* rc, int64_t* kc,
+                      double* best_ms);
+
+/* ------------------------------------------------------ interactions */
+/* EvalSinCos + CompInteractions (src/interaction.cpp:521-548,
+ * src/simulation.cpp:628-680) on the current state: demagnetising flux
+ * density B (T) and interaction force F (N, without thermal force), the
+ * real-space + short-range pressure sums P3 = {Pxy, Pxz, Pyz} before the
+ * division by the box volume.  Overlapping cores are pushed apart like
+ * CompInteractVecs (src/interaction.cpp:120-129) -- all overlaps resolved
+ * from the same starting positions.  Outputs may be NULL. */
+int md_compute_interactions(md_ctx* ctx, double* B, double* F, double* P3);
+/* CompDemagField (src/simulation.cpp:688-697): B for moment directions mm
+ * (N x 3, need not be unit length) with the geometry of the last
+ * md_compute_interactions. */
+int md_compute_field(md_ctx* ctx, const double* mm, double* B);
+
+/* ---------------------------------------------------------- stepping */
+/* Noise source and seed for md_step. */
+int md_set_noise(md_ctx* ctx, int mode, uint64_t seed);
+/* nsteps iterations of RunSimulation's loop body (src/simulation.cpp:469-518)
+ * with the fixed step dt: DefExtField, DefThermFluct, EvalSinCos,
+ * CompInteractions, IntegrationRot (Heun, SOLVER = 0), IntegrationTrans,
+ * ApplyBoundaryCondArr, EvalTransCoeffs and the mz record.
+ * xi: MD_NOISE_UPLOADED only, nsteps blocks of 9N unit normals, each block
+ * [torque N x 3][field N x 3][force N x 3] column-major (the order of the
+ * three Rand::normal draws of DefThermFluct); NULL otherwise. */
+int md_step(md_ctx* ctx, int64_t nsteps, double dt, const double* xi);
+/* Per-step records {t, mz, MSDx, MSDy, MSDz, Pxy, Pxz, Pyz} (the vectors of
+ * OutputVar_S, src/typedefs.h:129-137, filled by EvalTransCoeffs and
+ * simulation.cpp:514-515) for steps [first, first + count) since the last
+ * md_clear_records; obs is count x 8 row-major. */
+int md_records(md_ctx* ctx, int64_t first, int64_t count, double* obs);
+int md_num_records(const md_ctx* ctx, int64_t* count);
+int md_clear_records(md_ctx* ctx);
+/* Waits for the context's stream. */
+int md_sync(md_ctx* ctx);
+
+/* ----------------------------------------------------- test hooks */
+/* Cell list of the last interaction evaluation: cell_start[ncell + 1],
+ * perm[N] (sorted slot -> particle index); ncell and ncx are returned. */
+int md_debug_cells(md_ctx* ctx, int64_t* ncell, int64_t* ncx, int32_t* cell_start, int32_t* perm);
+/* Structure factor of the last evaluation: nk entries {nx, ny, nz, Sc, Ss}
+ * (as doubles, e(k) not applied).  nk_inout: capacity in, count out. */
+int md_debug_structure_factor(md_ctx* ctx, int64_t* nk_inout, double* out5);
+/* Number of kernel launches issued by the last md_step / md_compute_*. */
+int md_debug_launches(const md_ctx* ctx, int64_t* launches);
+/* In-range particle pairs (each unordered pair once) of the last full
+ * real-space evaluation: the entries CompInteractVecs would list. */
+int md_debug_pairs(md_ctx* ctx, int64_t* pairs);
+
+/* ------------------------------------------------------ profiling */
+/* Kernel segments of one step, in launch order. */
+enum {
+  MD_SEG_CELLS = 0,      /* cell list (a)                          */
+  MD_SEG_REAL_FULL,      /* real space, field + force (b)          */
+  MD_SEG_KSF_FULL,       /* structure factor (c)                   */
+  MD_SEG_KRED_FULL,      /* structure-factor reduction (c)         */
+  MD_SEG_KSCAT_FULL,     /* k-space scatter, field + force (c)     */
+  MD_SEG_HEUN1,          /* integrator stage 1 (d)                 */
+  MD_SEG_REAL_FIELD,     /* real space, field only (b)             */
+  MD_SEG_KSF_FIELD,
+  MD_SEG_KRED_FIELD,
+  MD_SEG_KSCAT_FIELD,
+  MD_SEG_HEUN2,          /* integrator stage 2 (d)                 */
+  MD_SEG_OBS,            /* per-step records                       */
+  MD_NSEG
+};
+/* With enable != 0, every following step records CUDA events between its
+ * kernel segments (inside the replayed graph, on the context's stream). */
+int md_profile(md_ctx* ctx, int enable);
+/* Milliseconds per segment of the last step (ms[MD_NSEG]). */
+int md_profile_read(md_ctx* ctx, double* ms);
+/* Measured FP32 FMA throughput of the current device (TFLOP/s, FMA = 2
+ * FLOPs) from a register-resident FMA-chain kernel on all SMs. */
+int md_calibrate_fp32(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MD_GB300_H */

@@ -1,0 +1,128 @@
+"""ctypes binding of the C ABI in include/md_gb300.h (libmd_gb300.so).
+
+The library is the only compute path: if it is missing or fails to load,
+every call raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+HEADER = os.path.join(os.path.dirname(HERE), "include", "md_gb300.h")
+LIB_PATH = os.path.join(HERE, "_lib", "libmd_gb300.so")
+
+MD_OK = 0
+STATUS = {0: "MD_OK", 1: "MD_ERR_INVALID", 2: "MD_ERR_CUDA", 3: "MD_ERR_NOMEM", 4: "MD_ERR_NONFINITE",
+          5: "MD_ERR_CONFIG", 6: "MD_ERR_UNSUPPORTED", 7: "MD_ERR_NO_DEVICE"}
+MD_PREC_FP64, MD_PREC_MIXED = 0, 1
+MD_NOISE_OFF, MD_NOISE_UPLOADED, MD_NOISE_PHILOX = 0, 1, 2
+MD_FIELD_STEP, MD_FIELD_SIN = 0, 1
+SEGMENTS = ["cells", "real_full", "ksf_full", "kred_full", "kscat_full", "heun1", "real_field", "ksf_field",
+            "kred_field", "kscat_field", "heun2", "obs"]
+
+
+class MdError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def _config_fields():
+    """Fields of md_config, parsed from the C header so the mirror cannot drift."""
+    src = open(HEADER).read()
+    body = src[src.index("typedef struct md_config {"):src.index("} md_config;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = []
+    for m in re.finditer(r"\b(int64_t|double)\s+([^;]+);", body):
+        ty = C.c_int64 if m.group(1) == "int64_t" else C.c_double
+        for name in m.group(2).split(","):
+            fields.append((name.strip(), ty))
+    return fields
+
+
+class MdConfig(C.Structure):
+    _fields_ = _config_fields()
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    """Loads libmd_gb300.so (raises if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OSError(f"{LIB_PATH} not built; run md_sim_wolfschwenger_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    P = C.POINTER(C.c_double)
+    I64 = C.c_int64
+    PI64 = C.POINTER(C.c_int64)
+    V = C.c_void_p
+    sig = {
+        "md_strerror": (C.c_char_p, [C.c_int]),
+        "md_last_error": (C.c_int, [V, C.c_char_p, C.c_size_t]),
+        "md_version": (C.c_char_p, []),
+        "md_config_load_ini": (C.c_int, [C.c_char_p, C.POINTER(MdConfig)]),
+        "md_config_default": (C.c_int, [C.POINTER(MdConfig)]),
+        "md_config_derive": (C.c_int, [C.POINTER(MdConfig)]),
+        "md_config_numb_part": (I64, [C.POINTER(MdConfig)]),
+        "md_config_size": (C.c_size_t, []),
+        "md_select_device": (C.c_int, [C.c_int]),
+        "md_ctx_create": (C.c_int, [C.POINTER(MdConfig), I64, C.c_int, C.POINTER(V)]),
+        "md_ctx_destroy": (C.c_int, [V]),
+        "md_ctx_stream": (C.c_int, [V, C.POINTER(V)]),
+        "md_ctx_device_bytes": (C.c_int, [V, PI64]),
+        "md_set_particles": (C.c_int, [V, P, P]),
+        "md_get_box": (C.c_int, [V, P]),
+        "md_set_box": (C.c_int, [V, C.c_double]),
+        "md_state_upload": (C.c_int, [V, P, P, P, C.c_int]),
+        "md_state_download": (C.c_int, [V, P, P, P]),
+        "md_set_time": (C.c_int, [V, C.c_double, I64]),
+        "md_get_time": (C.c_int, [V, P, PI64]),
+        "md_ewald_params": (C.c_int, [V, C.c_double, P, P, PI64, P, P]),
+        "md_set_ewald": (C.c_int, [V, C.c_double, C.c_double, I64]),
+        "md_ewald_params_host": (C.c_int, [C.POINTER(MdConfig), I64, P, P, C.c_double, P, P, PI64, P, P, P]),
+        "md_autotune_ewald": (C.c_int, [V, C.c_int, P, P, PI64, P]),
+        "md_compute_interactions": (C.c_int, [V, P, P, P]),
+        "md_compute_field": (C.c_int, [V, P, P]),
+        "md_set_noise": (C.c_int, [V, C.c_int, C.c_uint64]),
+        "md_step": (C.c_int, [V, I64, C.c_double, P]),
+        "md_records": (C.c_int, [V, I64, I64, P]),
+        "md_num_records": (C.c_int, [V, PI64]),
+        "md_clear_records": (C.c_int, [V]),
+        "md_sync": (C.c_int, [V]),
+        "md_debug_cells": (C.c_int, [V, PI64, PI64, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+        "md_debug_structure_factor": (C.c_int, [V, PI64, P]),
+        "md_debug_launches": (C.c_int, [V, PI64]),
+        "md_debug_pairs": (C.c_int, [V, PI64]),
+        "md_profile": (C.c_int, [V, C.c_int]),
+        "md_profile_read": (C.c_int, [V, P]),
+        "md_calibrate_fp32": (C.c_int, [P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    if L.md_config_size() != C.sizeof(MdConfig):
+        raise OSError(f"md_config size mismatch: C {L.md_config_size()} vs ctypes {C.sizeof(MdConfig)}")
+    _lib = L
+    return L
+
+
+def exported_symbols():
+    """Every function name declared in include/md_gb300.h."""
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    return sorted(set(re.findall(r"\b(md_[a-z0-9_]+)\s*\(", src)))
+
+
+def check(status, ctx=None):
+    if status != MD_OK:
+        buf = C.create_string_buffer(1024)
+        lib().md_last_error(ctx, buf, len(buf))
+        raise MdError(status, buf.value.decode(errors="replace"))

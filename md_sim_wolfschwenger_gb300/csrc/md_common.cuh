@@ -1,0 +1,213 @@
+// md_common.cuh -- shared definitions of the GB300 kernels.
+//
+// Unit system of the device kernels (both precisions): lengths in units of
+// the box length L, magnetic moments in units of mu_u = max_i |mu_i|.  Then
+// a real-space term like a3 ~ 1/r^7 stays inside FP32 range (it would
+// overflow in SI units), and the results convert to SI with
+//   B_unit = facEwald * mu_u / L^3        [T]
+//   F_unit = facEwald * mu_u^2 / L^4      [N].
+// All Ewald formulas are those of the reference (src/interaction.cpp:353-674)
+// rewritten in these units; the conversion factors are applied once per
+// particle in the integrator.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "md_types.h"
+
+namespace md {
+
+constexpr int kWarp = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+template <typename T> struct V4;
+template <> struct V4<float> { using t = float4; };
+template <> struct V4<double> { using t = double4_32a; };
+template <typename T> struct V2;
+template <> struct V2<float> { using t = float2; };
+template <> struct V2<double> { using t = double2; };
+
+// ------------------------------------------------------------ cell list
+// Sorted particle data (cell order).  Written by the cell-list build and,
+// for the moments, by the integrator between the two Heun stages.
+struct SortedView {
+  float4* xf;     // box coordinates (float) + rMag/L: candidate test
+  int4* xi;       // fixed-point box coordinates (2^32 per L) + particle index
+  double4_32a* xd;  // box coordinates (double) + rMag/L (FP64 path)
+  void* mu;       // T4: moment / mu_u, .w = rMag / L
+  int* cell;      // cell id of the sorted slot
+  int* perm;      // sorted slot -> particle index
+  int* rank;      // particle index -> sorted slot
+  int* cell_start;  // [ncell + 1]
+};
+
+// ------------------------------------------------------- real space
+struct RealParams {
+  int n;
+  CellGrid grid;
+  double alpha, rc;      // box units
+  double rc2, rc2_test;  // exact and (slightly larger) candidate cutoff
+  double c2a;            // 2 alpha / sqrt(pi)
+  double al2, al4;       // alpha^2, alpha^4
+  double cont_eps;       // 1e-10 m / L (contact offset, interaction.cpp:120)
+  // coating potentials (src/interaction.cpp:766-832), box units / F_unit
+  int coat;
+  double rcut_sr2;       // (rCutSR / L)^2
+  double eff_len;        // effLenSurfMol / L
+  double ster, elec, kappa, vdw;  // scaled prefactors
+  const double* rMag_u;  // rMag / L by particle index (coating potentials)
+  SortedView s;
+  void* B;      // [3][n] T, sorted order
+  void* F;      // [3][n] T, sorted order (FULL only)
+  void* ov;     // [3][n] T, overlap displacement, box units (FULL only)
+  double* Ppart;  // [gridDim.x][3] pressure partials (FULL only)
+  unsigned long long* npairs;  // in-range ordered pairs (FULL only, may be null)
+  int* err;       // device error word
+};
+
+// --------------------------------------------------------- k space
+struct KParams {
+  int n;
+  int kc;
+  int nseg, nk;          // segments, padded k count
+  int chunk;             // particles per chunk of the structure-factor grid
+  int nchunk;
+  double two_pi;         // 2 * my_pi (FP64 phases follow the reference's pi)
+  const KSeg* seg;       // [nseg] sorted by len (desc)
+  const int* koff;       // [nseg] k index of the segment's first k
+  const double* ek;      // [nk] 2 exp(-w n^2) / n^2 (0 for padding)
+  double2* Spart;        // [nchunk][nk] partial structure factors
+  double* musum_part;    // [nchunk][3]
+  double* musum;         // [3]
+  void* eS;              // [nk] T2: e(k) * (Sc, Ss)
+  double2* S;            // [nk] full structure factor (debug / FP64)
+  double cflux, cforce;  // 4 pi, 8 pi^2 (box units)
+  SortedView s;
+  void* B;   // [3][n] T sorted
+  void* F;   // [3][n] T sorted (FULL only)
+};
+
+// ----------------------------------------------------- integrator
+struct IntParams {
+  int n;
+  double dt, L;
+  double B_unit, F_unit;     // SI per unit
+  double cself, csurf;       // box units
+  double anisConst, velMmConst, magDamp;
+  int mobil;
+  int noise;                 // MD_NOISE_*
+  uint64_t seed;
+  int field_kind;
+  double magFluxDens, tMag, fieldAmp, fieldFreq;
+  const double* xi;          // uploaded unit normals [9][n] for this step
+  // master state (orig order, FP64 SoA)
+  double *pos, *mm, *ea, *truePos, *posRef;
+  // particle constants (orig order)
+  const double* magMom_u;    // |mu_i| / mu_u
+  const double* rMag_u;      // rMag / L
+  const double* invZt;       // 1 / zeta_trans
+  const double* velEa1;
+  const double* velEa2;
+  const double* sT;          // thermal torque scale (DefThermFluct)
+  const double* sB;          // thermal field scale
+  const double* sF;          // thermal force scale
+  // work arrays (orig order, T)
+  void *k1m, *k1e, *m2, *e2, *th;   // th: [9][n] scaled noise
+  // stage outputs (sorted order, T)
+  const void *Br, *Bk, *Fr, *Fk, *ov;
+  SortedView s;
+  const double* musum;       // [3] sum of mu' of the evaluated stage
+  double* obs_part;          // [gridDim.x][4]: msd x,y,z, mz
+  const double* time;        // device t (double) and step
+  const long long* stepno;
+  int* err;
+};
+
+struct ObsParams {
+  int nblk_int, nblk_real;
+  const double* obs_part;
+  const double* Ppart;
+  double p_scale;            // L * F_unit / (2 * volBox) (pair double count)
+  double inv_n;
+  double dt;
+  double* time;
+  long long* stepno;
+  double* records;           // [cap][8]
+  long long* nrec;
+  long long cap;
+};
+
+// ------------------------------------------------------ device helpers
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): the published
+// multipliers and Weyl increments; counter {i, block, step_lo, step_hi}.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// Nine standard normals of particle i at step s (torque xyz, field xyz,
+// force xyz), Box-Muller on uniforms (x + 0.5) 2^-32.
+template <typename T>
+__device__ __forceinline__ void philox_normals9(uint64_t seed, uint64_t step, uint32_t i, T z[9]) {
+  T w[12];
+#pragma unroll
+  for (uint32_t b = 0; b < 3; b++) {
+    uint4 r = philox4x32_10(make_uint4(i, b, (uint32_t)step, (uint32_t)(step >> 32)), (uint32_t)seed,
+                            (uint32_t)(seed >> 32));
+    uint32_t u[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      if constexpr (std::is_same<T, float>::value) {
+        float u1 = ((float)u[2 * h] + 0.5f) * 2.3283064365386963e-10f;
+        float u2 = ((float)u[2 * h + 1] + 0.5f) * 2.3283064365386963e-10f;
+        float rr = sqrtf(-2.0f * logf(u1)), s, c;
+        sincospif(2.0f * u2, &s, &c);
+        w[4 * b + 2 * h] = rr * c;
+        w[4 * b + 2 * h + 1] = rr * s;
+      } else {
+        double u1 = ((double)u[2 * h] + 0.5) * 2.3283064365386963e-10;
+        double u2 = ((double)u[2 * h + 1] + 0.5) * 2.3283064365386963e-10;
+        double rr = sqrt(-2.0 * log(u1)), s, c;
+        sincospi(2.0 * u2, &s, &c);
+        w[4 * b + 2 * h] = rr * c;
+        w[4 * b + 2 * h + 1] = rr * s;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) z[k] = w[k];
+}
+
+template <typename T>
+__device__ __forceinline__ void cmul(T ar, T ai, T br, T bi, T& cr, T& ci) {
+  cr = ar * br - ai * bi;
+  ci = ar * bi + ai * br;
+}
+
+// Device error word bits.
+enum : int { kErrNonFinite = 1, kErrQueue = 2 };
+
+}  // namespace md

@@ -1,0 +1,1020 @@
+// md_ctx.cu -- the C ABI (include/md_gb300.h): context, device buffers,
+// step orchestration and CUDA-graph replay of one time step.
+//
+// One step on the device (RunSimulation loop body, src/simulation.cpp:469-518):
+//   cells (a) -> real space full (b) -> k space full (c) -> Heun stage 1 (d)
+//   -> real space field (b) -> k space field (c) -> Heun stage 2 (d) -> records
+// The step reads its time and step number from device memory, so the same
+// captured graph is replayed for every step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/md_gb300.h"
+#include "md_common.cuh"
+#include "md_host.h"
+#include "md_kernels.h"
+
+using namespace md;
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_err;
+int g_err_status = 0;
+
+struct DevScalars {
+  double time;
+  long long step;
+  long long nrec;
+  int err;
+  int pad;
+  double musum[3];
+  unsigned long long pairs;
+};
+
+}  // namespace
+
+struct md_ctx {
+  md_config cfg{};
+  int64_t n = 0;
+  int prec = MD_PREC_MIXED;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int err_status = 0;
+  std::vector<void*> allocs;
+  int64_t bytes = 0;
+
+  // host state
+  mdh::Props props;
+  bool have_particles = false, have_state = false, have_ewald = false, have_geometry = false;
+  double L = 0, alpha = 0, rc = 0;
+  int64_t kc = 0;
+  CellGrid grid{1, 1, 0};
+  mdh::KList klist;
+  int nchunk = 1, chunk = 0;
+  int noise = MD_NOISE_PHILOX;
+  uint64_t seed = 1;
+  double cur_dt = -1;
+  bool graph_valid = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t launches = 0, launches_per_step = 0;
+
+  // device: master state & particle constants
+  double *pos = nullptr, *mm = nullptr, *ea = nullptr, *truePos = nullptr, *posRef = nullptr;
+  double *xi = nullptr, *tmpmm = nullptr, *Bout = nullptr, *Fout = nullptr;
+  double *magMom_u = nullptr, *rMag_u = nullptr, *invZt = nullptr, *velEa1 = nullptr, *velEa2 = nullptr;
+  double *sT = nullptr, *sB = nullptr, *sF = nullptr;
+  // cells and sorted views
+  int *cellOf = nullptr, *tmp = nullptr, *perm = nullptr, *rank = nullptr, *scell = nullptr;
+  int *count = nullptr, *cell_start = nullptr;
+  int ncell_cap = 0;
+  float4* xf = nullptr;
+  int4* xi4 = nullptr;
+  double4_32a* xd = nullptr;
+  void* mu = nullptr;
+  // stage outputs (T)
+  void *Br = nullptr, *Fr = nullptr, *ov = nullptr, *Bk = nullptr, *Fk = nullptr, *Br2 = nullptr, *Bk2 = nullptr;
+  void *k1m = nullptr, *k1e = nullptr, *m2 = nullptr, *e2 = nullptr, *th = nullptr;
+  double *Ppart = nullptr, *obs_part = nullptr;
+  DevScalars* sc = nullptr;
+  double* records = nullptr;
+  long long rec_cap = 0;
+  // k space
+  KSeg* kseg = nullptr;
+  int* koff = nullptr;
+  double* ek = nullptr;
+  double2* Spart = nullptr;
+  double* musum_part = nullptr;
+  void* eS = nullptr;
+  double2* Sfull = nullptr;
+  size_t ksize_cap = 0, spart_cap = 0;
+  int musum_cap = 0;
+  // profiling: events between the kernel segments of a step
+  bool prof = false;
+  cudaEvent_t ev[MD_NSEG + 1] = {};
+};
+
+// Records the boundary event `k` when profiling.
+static void mark(md_ctx* c, int k) {
+  if (c->prof) cudaEventRecordWithFlags(c->ev[k], c->stream, cudaEventRecordExternal);
+}
+
+// ------------------------------------------------------------- helpers
+
+static int set_err(md_ctx* c, int status, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) {
+    c->err = buf;
+    c->err_status = status;
+  }
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_err = buf;
+  g_err_status = status;
+  return status;
+}
+
+#define CK(ctx, call)                                                                              \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return set_err(ctx, MD_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                     __FILE__, __LINE__);                                                          \
+  } while (0)
+
+template <typename P>
+static int dalloc(md_ctx* c, P** p, size_t bytes) {
+  void* q = nullptr;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess)
+    return set_err(c, MD_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+  c->allocs.push_back(q);
+  c->bytes += (int64_t)bytes;
+  *p = (P*)q;
+  return MD_OK;
+}
+
+static void dfree(md_ctx* c, void* p) {
+  if (!p) return;
+  auto it = std::find(c->allocs.begin(), c->allocs.end(), p);
+  if (it != c->allocs.end()) c->allocs.erase(it);
+  cudaFree(p);
+}
+
+static bool fp64(const md_ctx* c) { return c->prec == MD_PREC_FP64; }
+static size_t tsz(const md_ctx* c) { return fp64(c) ? 8 : 4; }
+
+static void invalidate_graph(md_ctx* c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->gexec = nullptr;
+  c->graph = nullptr;
+  c->graph_valid = false;
+}
+
+static SortedView sorted_view(md_ctx* c) {
+  SortedView s;
+  s.xf = c->xf;
+  s.xi = c->xi4;
+  s.xd = c->xd;
+  s.mu = c->mu;
+  s.cell = c->scell;
+  s.perm = c->perm;
+  s.rank = c->rank;
+  s.cell_start = c->cell_start;
+  return s;
+}
+
+static double B_unit(const md_ctx* c) { return c->cfg.facEwald * c->props.muMax / std::pow(c->L, 3.0); }
+static double F_unit(const md_ctx* c) { return c->cfg.facEwald * c->props.muMax * c->props.muMax / std::pow(c->L, 4.0); }
+
+static RealParams real_params(md_ctx* c, void* B, void* F, void* ov) {
+  RealParams p{};
+  const md_config& g = c->cfg;
+  const double L = c->L, a = c->alpha * L, rcb = c->rc / L;
+  p.n = (int)c->n;
+  p.grid = c->grid;
+  p.alpha = a;
+  p.rc = rcb;
+  p.rc2 = rcb * rcb;
+  const double rt = rcb * (1.0 + 1e-6) + 2e-7;
+  p.rc2_test = rt * rt;
+  p.c2a = 2.0 * a * g.irPi;
+  p.al2 = a * a;
+  p.al4 = p.al2 * p.al2;
+  p.cont_eps = 1e-10 / L;
+  p.coat = (int)g.ENABLE_COATING_POT;
+  const double Fu = F_unit(c);
+  p.rcut_sr2 = std::pow(c->props.rCutSR / L, 2.0);
+  p.eff_len = g.effLenSurfMol / L;
+  p.ster = g.sterRepFac * L * L / Fu;
+  p.elec = g.electrostatRepFac * L / Fu;
+  p.kappa = g.kappa * L;
+  p.vdw = g.hamaker / (L * Fu);
+  p.rMag_u = c->rMag_u;
+  p.s = sorted_view(c);
+  p.B = B;
+  p.F = F;
+  p.ov = ov;
+  p.Ppart = c->Ppart;
+  p.npairs = F ? &c->sc->pairs : nullptr;
+  p.err = &c->sc->err;
+  return p;
+}
+
+static KParams k_params(md_ctx* c, void* B, void* F) {
+  KParams p{};
+  p.n = (int)c->n;
+  p.kc = (int)c->kc;
+  p.nseg = (int)c->klist.seg.size();
+  p.nk = c->klist.nk;
+  p.chunk = c->chunk;
+  p.nchunk = c->nchunk;
+  p.two_pi = 2.0 * c->cfg.my_pi;
+  p.seg = c->kseg;
+  p.koff = c->koff;
+  p.ek = c->ek;
+  p.Spart = c->Spart;
+  p.musum_part = c->musum_part;
+  p.musum = c->sc->musum;
+  p.eS = c->eS;
+  p.S = c->Sfull;
+  p.cflux = 4.0 * c->cfg.my_pi;
+  p.cforce = 8.0 * c->cfg.my_pi * c->cfg.my_pi;
+  p.s = sorted_view(c);
+  p.B = B;
+  p.F = F;
+  return p;
+}
+
+static IntParams int_params(md_ctx* c, double dt, const void* Br, const void* Bk) {
+  IntParams p{};
+  const md_config& g = c->cfg;
+  const double a = c->alpha * c->L;
+  p.n = (int)c->n;
+  p.dt = dt;
+  p.L = c->L;
+  p.B_unit = B_unit(c);
+  p.F_unit = F_unit(c);
+  p.cself = 4.0 * a * a * a / (3.0 * std::sqrt(g.my_pi));
+  p.csurf = 4.0 * g.my_pi / 3.0;
+  p.anisConst = g.anisConst;
+  p.velMmConst = g.velMmConst;
+  p.magDamp = g.magDamp;
+  p.mobil = (int)g.ENABLE_MOBILIZATION;
+  p.noise = c->noise;
+  p.seed = c->seed;
+  p.field_kind = (int)g.fieldKind;
+  p.magFluxDens = g.magFluxDens;
+  p.tMag = g.tMag;
+  p.fieldAmp = g.fieldAmp;
+  p.fieldFreq = g.fieldFreq;
+  p.xi = c->xi;
+  p.pos = c->pos;
+  p.mm = c->mm;
+  p.ea = c->ea;
+  p.truePos = c->truePos;
+  p.posRef = c->posRef;
+  p.magMom_u = c->magMom_u;
+  p.rMag_u = c->rMag_u;
+  p.invZt = c->invZt;
+  p.velEa1 = c->velEa1;
+  p.velEa2 = c->velEa2;
+  p.sT = c->sT;
+  p.sB = c->sB;
+  p.sF = c->sF;
+  p.k1m = c->k1m;
+  p.k1e = c->k1e;
+  p.m2 = c->m2;
+  p.e2 = c->e2;
+  p.th = c->th;
+  p.Br = Br;
+  p.Bk = Bk;
+  p.Fr = c->Fr;
+  p.Fk = c->Fk;
+  p.ov = c->ov;
+  p.s = sorted_view(c);
+  p.musum = c->sc->musum;
+  p.obs_part = c->obs_part;
+  p.time = &c->sc->time;
+  p.stepno = &c->sc->step;
+  p.err = &c->sc->err;
+  return p;
+}
+
+static int check_ready(md_ctx* c, bool need_state) {
+  if (!c) return set_err(nullptr, MD_ERR_INVALID, "null context");
+  if (!c->have_particles) return set_err(c, MD_ERR_INVALID, "particles not set (md_set_particles)");
+  if (!c->have_ewald) return set_err(c, MD_ERR_INVALID, "Ewald parameters not set (md_set_ewald)");
+  if (need_state && !c->have_state) return set_err(c, MD_ERR_INVALID, "state not uploaded (md_state_upload)");
+  return MD_OK;
+}
+
+// Field + force evaluation on the current master state (no integrator).
+static int issue_interactions(md_ctx* c) {
+  int l = 0;
+  SortedView s = sorted_view(c);
+  mark(c, MD_SEG_CELLS);
+  l += launch_cells(c->stream, (int)c->n, c->pos, c->mm, c->magMom_u, c->rMag_u, c->L, c->grid, c->cellOf, c->count,
+                    c->tmp, s, fp64(c));
+  cudaMemsetAsync(&c->sc->pairs, 0, sizeof(unsigned long long), c->stream);
+  mark(c, MD_SEG_REAL_FULL);
+  l += launch_real(c->stream, real_params(c, c->Br, c->Fr, c->ov), true, fp64(c));
+  mark(c, MD_SEG_KSF_FULL);
+  l += launch_kspace(c->stream, k_params(c, c->Bk, c->Fk), true, fp64(c), c->prof ? &c->ev[MD_SEG_KRED_FULL] : nullptr);
+  c->have_geometry = true;
+  return l;
+}
+
+static int issue_step(md_ctx* c, double dt) {
+  int l = issue_interactions(c);
+  mark(c, MD_SEG_HEUN1);
+  l += launch_heun1(c->stream, int_params(c, dt, c->Br, c->Bk), fp64(c));
+  mark(c, MD_SEG_REAL_FIELD);
+  l += launch_real(c->stream, real_params(c, c->Br2, nullptr, nullptr), false, fp64(c));
+  mark(c, MD_SEG_KSF_FIELD);
+  l += launch_kspace(c->stream, k_params(c, c->Bk2, nullptr), false, fp64(c),
+                     c->prof ? &c->ev[MD_SEG_KRED_FIELD] : nullptr);
+  mark(c, MD_SEG_HEUN2);
+  l += launch_heun2(c->stream, int_params(c, dt, c->Br2, c->Bk2), fp64(c));
+  mark(c, MD_SEG_OBS);
+  ObsParams o{};
+  o.nblk_int = int_blocks((int)c->n);
+  o.nblk_real = real_blocks((int)c->n);
+  o.obs_part = c->obs_part;
+  o.Ppart = c->Ppart;
+  o.p_scale = c->L * F_unit(c) / (2.0 * std::pow(c->L, 3.0));
+  o.inv_n = 1.0 / (double)c->n;
+  o.dt = dt;
+  o.time = &c->sc->time;
+  o.stepno = &c->sc->step;
+  o.records = c->records;
+  o.nrec = &c->sc->nrec;
+  o.cap = c->rec_cap;
+  l += launch_obs(c->stream, o);
+  mark(c, MD_NSEG);
+  return l;
+}
+
+static int read_err_word(md_ctx* c) {
+  int e = 0;
+  CK(c, cudaMemcpyAsync(&e, &c->sc->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (e) {
+    CK(c, cudaMemsetAsync(&c->sc->err, 0, sizeof(int), c->stream));
+    if (e & kErrNonFinite) return set_err(c, MD_ERR_NONFINITE, "non-finite position or orientation after the step");
+  }
+  return MD_OK;
+}
+
+// ============================================================== C ABI
+
+extern "C" {
+
+const char* md_strerror(int s) {
+  switch (s) {
+    case MD_OK: return "ok";
+    case MD_ERR_INVALID: return "invalid argument or state";
+    case MD_ERR_CUDA: return "CUDA runtime error";
+    case MD_ERR_NOMEM: return "out of memory";
+    case MD_ERR_NONFINITE: return "non-finite value in the simulation state";
+    case MD_ERR_CONFIG: return "configuration error";
+    case MD_ERR_UNSUPPORTED: return "unsupported";
+    case MD_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+int md_last_error(const md_ctx* c, char* buf, size_t len) {
+  std::string m;
+  int st;
+  if (c) {
+    m = c->err;
+    st = c->err_status;
+  } else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    m = g_err;
+    st = g_err_status;
+  }
+  if (buf && len) {
+    std::strncpy(buf, m.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return st;
+}
+
+const char* md_version(void) { return "md_gb300 1.0 (sm_103a)"; }
+
+int md_config_default(md_config* cfg) {
+  if (!cfg) return set_err(nullptr, MD_ERR_INVALID, "null config");
+  mdh::config_defaults(cfg);
+  return MD_OK;
+}
+
+int md_config_derive(md_config* cfg) {
+  if (!cfg) return set_err(nullptr, MD_ERR_INVALID, "null config");
+  mdh::config_derive(cfg);
+  return MD_OK;
+}
+
+int md_config_load_ini(const char* path, md_config* cfg) {
+  if (!path || !cfg) return set_err(nullptr, MD_ERR_INVALID, "null argument");
+  std::string e;
+  int st = mdh::config_load_ini(path, cfg, &e);
+  if (st) return set_err(nullptr, st, "%s", e.c_str());
+  return MD_OK;
+}
+
+int64_t md_config_numb_part(const md_config* cfg) { return cfg ? mdh::numb_part(cfg) : 0; }
+
+size_t md_config_size(void) { return sizeof(md_config); }
+
+int md_select_device(int device) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(nullptr, MD_ERR_NO_DEVICE, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+  }
+  return MD_OK;
+}
+
+int md_ctx_create(const md_config* cfg, int64_t n, int precision, md_ctx** out) {
+  if (!cfg || !out || n < 2 || n > (1LL << 30)) return set_err(nullptr, MD_ERR_INVALID, "bad md_ctx_create arguments");
+  if (precision != MD_PREC_FP64 && precision != MD_PREC_MIXED)
+    return set_err(nullptr, MD_ERR_INVALID, "unknown precision %d", precision);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_err(nullptr, MD_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  md_ctx* c = new md_ctx();
+  c->cfg = *cfg;
+  c->n = n;
+  c->prec = precision;
+  c->noise = (int)cfg->noise;
+  c->seed = (uint64_t)cfg->seed;
+  cudaGetDevice(&c->device);
+  int st = MD_OK;
+  auto fail = [&](int s) {
+    md_ctx_destroy(c);
+    return s;
+  };
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(set_err(nullptr, MD_ERR_CUDA, "cudaStreamCreate failed"));
+  const size_t N = (size_t)n, T = tsz(c);
+  double** d3[] = {&c->pos, &c->mm, &c->ea, &c->truePos, &c->posRef, &c->tmpmm, &c->Bout, &c->Fout};
+  for (auto p : d3)
+    if ((st = dalloc(c, p, 24 * N))) return fail(st);
+  if ((st = dalloc(c, &c->xi, 72 * N))) return fail(st);
+  double** d1[] = {&c->magMom_u, &c->rMag_u, &c->invZt, &c->velEa1, &c->velEa2, &c->sT, &c->sB, &c->sF};
+  for (auto p : d1)
+    if ((st = dalloc(c, p, 8 * N))) return fail(st);
+  int** i1[] = {&c->cellOf, &c->tmp, &c->perm, &c->rank, &c->scell};
+  for (auto p : i1)
+    if ((st = dalloc(c, p, 4 * N))) return fail(st);
+  if ((st = dalloc(c, &c->xf, 16 * N))) return fail(st);
+  if (fp64(c)) {
+    if ((st = dalloc(c, &c->xd, 32 * N))) return fail(st);
+  } else {
+    if ((st = dalloc(c, &c->xi4, 16 * N))) return fail(st);
+  }
+  if ((st = dalloc(c, &c->mu, 4 * T * N))) return fail(st);
+  void** t3[] = {&c->Br, &c->Fr, &c->ov, &c->Bk, &c->Fk, &c->Br2, &c->Bk2, &c->k1m, &c->k1e, &c->m2, &c->e2};
+  for (auto p : t3)
+    if ((st = dalloc(c, p, 3 * T * N))) return fail(st);
+  if ((st = dalloc(c, &c->th, 9 * T * N))) return fail(st);
+  if ((st = dalloc(c, &c->Ppart, 24 * (size_t)real_blocks((int)n)))) return fail(st);
+  if ((st = dalloc(c, &c->obs_part, 32 * (size_t)int_blocks((int)n)))) return fail(st);
+  if ((st = dalloc(c, &c->sc, sizeof(DevScalars)))) return fail(st);
+  if (cudaMemsetAsync(c->sc, 0, sizeof(DevScalars), c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->xi, 0, 72 * N, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->Ppart, 0, 24 * (size_t)real_blocks((int)n), c->stream) != cudaSuccess)
+    return fail(set_err(nullptr, MD_ERR_CUDA, "initial memset failed"));
+  *out = c;
+  return MD_OK;
+}
+
+int md_ctx_destroy(md_ctx* c) {
+  if (!c) return MD_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  invalidate_graph(c);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  for (void* p : c->allocs) cudaFree(p);
+  c->allocs.clear();
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return MD_OK;
+}
+
+int md_ctx_stream(md_ctx* c, void** stream) {
+  if (!c || !stream) return set_err(c, MD_ERR_INVALID, "null argument");
+  *stream = (void*)c->stream;
+  return MD_OK;
+}
+
+int md_ctx_device_bytes(const md_ctx* c, int64_t* bytes) {
+  if (!c || !bytes) return MD_ERR_INVALID;
+  *bytes = c->bytes;
+  return MD_OK;
+}
+
+int md_set_particles(md_ctx* c, const double* rMag, const double* rHydr) {
+  if (!c || !rMag) return set_err(c, MD_ERR_INVALID, "null argument");
+  std::string e;
+  mdh::Props p;
+  int st = mdh::make_props(c->cfg, rMag, rHydr, c->n, &p, &e);
+  if (st) return set_err(c, st, "%s", e.c_str());
+  c->props = p;
+  c->L = p.lBox;
+  const size_t N = (size_t)c->n;
+  std::vector<double> mu(N), rm(N), izt(N);
+  for (size_t i = 0; i < N; i++) {
+    mu[i] = p.magMom[i] / p.muMax;
+    rm[i] = p.rMag[i] / c->L;
+    izt[i] = 1.0 / p.zetaTrans[i];
+  }
+  CK(c, cudaMemcpyAsync(c->magMom_u, mu.data(), 8 * N, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->rMag_u, rm.data(), 8 * N, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->invZt, izt.data(), 8 * N, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->velEa1, p.velEa1.data(), 8 * N, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->velEa2, p.velEa2.data(), 8 * N, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->have_particles = true;
+  c->have_ewald = false;
+  c->cur_dt = -1;
+  invalidate_graph(c);
+  return MD_OK;
+}
+
+int md_get_box(const md_ctx* c, double* lBox) {
+  if (!c || !lBox) return MD_ERR_INVALID;
+  *lBox = c->L;
+  return MD_OK;
+}
+
+int md_set_box(md_ctx* c, double lBox) {
+  if (!c || !(lBox > 0) || !c->have_particles) return set_err(c, MD_ERR_INVALID, "bad box or particles not set");
+  c->L = lBox;
+  c->props.lBox = lBox;
+  std::vector<double> rm(c->n);
+  for (int64_t i = 0; i < c->n; i++) rm[i] = c->props.rMag[i] / lBox;
+  CK(c, cudaMemcpy(c->rMag_u, rm.data(), 8 * c->n, cudaMemcpyHostToDevice));
+  c->have_ewald = false;
+  invalidate_graph(c);
+  return MD_OK;
+}
+
+int md_state_upload(md_ctx* c, const double* pos, const double* mm, const double* ea, int reset) {
+  if (!c || !pos || !mm || !ea) return set_err(c, MD_ERR_INVALID, "null argument");
+  const size_t B = 24 * (size_t)c->n;
+  CK(c, cudaMemcpyAsync(c->pos, pos, B, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->mm, mm, B, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->ea, ea, B, cudaMemcpyHostToDevice, c->stream));
+  if (reset || !c->have_state) {
+    CK(c, cudaMemcpyAsync(c->truePos, c->pos, B, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->posRef, c->pos, B, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->have_state = true;
+  c->have_geometry = false;
+  return MD_OK;
+}
+
+int md_state_download(md_ctx* c, double* pos, double* mm, double* ea) {
+  if (!c) return set_err(c, MD_ERR_INVALID, "null context");
+  const size_t B = 24 * (size_t)c->n;
+  if (pos) CK(c, cudaMemcpyAsync(pos, c->pos, B, cudaMemcpyDeviceToHost, c->stream));
+  if (mm) CK(c, cudaMemcpyAsync(mm, c->mm, B, cudaMemcpyDeviceToHost, c->stream));
+  if (ea) CK(c, cudaMemcpyAsync(ea, c->ea, B, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return MD_OK;
+}
+
+int md_set_time(md_ctx* c, double t, int64_t step) {
+  if (!c) return set_err(c, MD_ERR_INVALID, "null context");
+  DevScalars h;
+  CK(c, cudaMemcpy(&h, c->sc, sizeof h, cudaMemcpyDeviceToHost));
+  h.time = t;
+  h.step = step;
+  CK(c, cudaMemcpy(c->sc, &h, sizeof h, cudaMemcpyHostToDevice));
+  return MD_OK;
+}
+
+int md_get_time(const md_ctx* cc, double* t, int64_t* step) {
+  md_ctx* c = const_cast<md_ctx*>(cc);
+  if (!c) return MD_ERR_INVALID;
+  DevScalars h;
+  CK(c, cudaStreamSynchronize(c->stream));
+  CK(c, cudaMemcpy(&h, c->sc, sizeof h, cudaMemcpyDeviceToHost));
+  if (t) *t = h.time;
+  if (step) *step = h.step;
+  return MD_OK;
+}
+
+int md_ewald_params(md_ctx* c, double rc, double* alpha, double* rc_out, int64_t* kc, double* errF, double* errT) {
+  if (!c || !c->have_particles) return set_err(c, MD_ERR_INVALID, "particles not set");
+  mdh::EwaldModel m = mdh::ewald_model(c->cfg, c->props);
+  double a = 0, kraw = 0;
+  int64_t k = 0;
+  if (rc <= 0) {
+    rc = mdh::choose_rc(c->cfg, m, c->n, &a, &k);
+    kraw = (double)k;
+  } else {
+    if (rc > 0.5 * c->L * (1 + 1e-12)) return set_err(c, MD_ERR_INVALID, "rc must not exceed L/2");
+    if (!mdh::ewald_for_rc(c->cfg, m, rc, &a, &kraw))
+      return set_err(c, MD_ERR_INVALID, "alpha for the error tolerance not found");
+    k = (int64_t)std::floor(kraw + 0.5);
+  }
+  if (alpha) *alpha = a;
+  if (rc_out) *rc_out = rc;
+  if (kc) *kc = k;
+  mdh::predicted_errors(c->cfg, m, a, rc, (double)k, errF, errT);
+  return MD_OK;
+}
+
+int md_ewald_params_host(const md_config* cfg, int64_t n, const double* rMag, const double* rHydr, double rc,
+                         double* alpha, double* rc_out, int64_t* kc, double* errF, double* errT, double* lBox) {
+  if (!cfg || !rMag || n < 2) return set_err(nullptr, MD_ERR_INVALID, "bad arguments");
+  std::string e;
+  mdh::Props p;
+  int st = mdh::make_props(*cfg, rMag, rHydr, n, &p, &e);
+  if (st) return set_err(nullptr, st, "%s", e.c_str());
+  mdh::EwaldModel m = mdh::ewald_model(*cfg, p);
+  double a = 0, kraw = 0;
+  int64_t k = 0;
+  if (rc <= 0) {
+    rc = mdh::choose_rc(*cfg, m, n, &a, &k);
+  } else {
+    if (rc > 0.5 * p.lBox * (1 + 1e-12)) return set_err(nullptr, MD_ERR_INVALID, "rc must not exceed L/2");
+    if (!mdh::ewald_for_rc(*cfg, m, rc, &a, &kraw))
+      return set_err(nullptr, MD_ERR_INVALID, "alpha for the error tolerance not found");
+    k = (int64_t)std::floor(kraw + 0.5);
+  }
+  if (alpha) *alpha = a;
+  if (rc_out) *rc_out = rc;
+  if (kc) *kc = k;
+  if (lBox) *lBox = p.lBox;
+  mdh::predicted_errors(*cfg, m, a, rc, (double)k, errF, errT);
+  return MD_OK;
+}
+
+int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
+  if (!c || !c->have_particles) return set_err(c, MD_ERR_INVALID, "particles not set");
+  if (!(alpha > 0) || !(rc > 0) || rc > 0.5 * c->L * (1 + 1e-12) || kc < 1 || kc > 96)
+    return set_err(c, MD_ERR_INVALID, "bad Ewald parameters (alpha>0, 0<rc<=L/2, 1<=kc<=96)");
+  if (kscatter_smem((int)kc, fp64(c)) == 0) return set_err(c, MD_ERR_UNSUPPORTED, "kc too large for shared memory");
+  invalidate_graph(c);
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->alpha = alpha;
+  c->rc = rc;
+  c->kc = kc;
+  const double ab = alpha * c->L;
+  const double w = std::pow(c->cfg.my_pi / ab, 2.0);
+  c->klist = mdh::build_klist((int)kc, w);
+  c->grid = mdh::choose_grid(rc / c->L, c->n, 2);
+  // structure-factor grid: ~4 waves of blocks over the SMs
+  int nsm = 148;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+  const int nsegb = (int)((c->klist.seg.size() + 255) / 256);
+  int nch = std::max(1, (4 * nsm + nsegb - 1) / nsegb);
+  nch = std::min<int64_t>(nch, (c->n + 31) / 32);
+  c->chunk = (int)(((c->n + nch - 1) / nch + 31) / 32 * 32);
+  c->nchunk = (int)((c->n + c->chunk - 1) / c->chunk);
+  // (re)allocate Ewald-sized buffers
+  const int ncell = c->grid.ncell;
+  if (ncell + 1 > c->ncell_cap) {
+    dfree(c, c->count);
+    dfree(c, c->cell_start);
+    c->count = nullptr;
+    c->cell_start = nullptr;
+    int st;
+    if ((st = dalloc(c, &c->count, 4 * (size_t)(ncell + 1)))) return st;
+    if ((st = dalloc(c, &c->cell_start, 4 * (size_t)(ncell + 1)))) return st;
+    c->ncell_cap = ncell + 1;
+  }
+  if (c->grid.ncx == 1) {
+    int h[2] = {0, (int)c->n};
+    CK(c, cudaMemcpy(c->cell_start, h, sizeof h, cudaMemcpyHostToDevice));
+  }
+  const size_t nk = (size_t)c->klist.nk, nseg = c->klist.seg.size();
+  if (nk > c->ksize_cap || nseg > c->ksize_cap) {
+    void* old[] = {c->kseg, c->koff, c->ek, c->eS, c->Sfull};
+    for (void* p : old) dfree(c, p);
+    const size_t cap = std::max(nk, nseg);
+    int st;
+    if ((st = dalloc(c, &c->kseg, sizeof(KSeg) * cap))) return st;
+    if ((st = dalloc(c, &c->koff, sizeof(int) * cap))) return st;
+    if ((st = dalloc(c, &c->ek, sizeof(double) * cap))) return st;
+    if ((st = dalloc(c, &c->eS, 2 * tsz(c) * cap))) return st;
+    if ((st = dalloc(c, &c->Sfull, sizeof(double2) * cap))) return st;
+    c->ksize_cap = cap;
+  }
+  const size_t sp = nk * (size_t)c->nchunk;
+  if (sp > c->spart_cap) {
+    dfree(c, c->Spart);
+    c->Spart = nullptr;
+    int st;
+    if ((st = dalloc(c, &c->Spart, sizeof(double2) * sp))) return st;
+    c->spart_cap = sp;
+  }
+  if (c->nchunk > c->musum_cap) {
+    dfree(c, c->musum_part);
+    c->musum_part = nullptr;
+    int st;
+    if ((st = dalloc(c, &c->musum_part, 24 * (size_t)c->nchunk))) return st;
+    c->musum_cap = c->nchunk;
+  }
+  CK(c, cudaMemcpy(c->kseg, c->klist.seg.data(), sizeof(KSeg) * nseg, cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->koff, c->klist.koff.data(), sizeof(int) * nseg, cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->ek, c->klist.ek.data(), sizeof(double) * nk, cudaMemcpyHostToDevice));
+  c->have_ewald = true;
+  c->have_geometry = false;
+  return MD_OK;
+}
+
+int md_compute_interactions(md_ctx* c, double* B, double* F, double* P3) {
+  int st = check_ready(c, true);
+  if (st) return st;
+  c->launches = issue_interactions(c);
+  IntParams ip = int_params(c, 0.0, c->Br, c->Bk);
+  c->launches += launch_combine(c->stream, ip, c->Bout, c->Fout, 1, fp64(c));
+  CK(c, cudaGetLastError());
+  const size_t Bz = 24 * (size_t)c->n;
+  if (B) CK(c, cudaMemcpyAsync(B, c->Bout, Bz, cudaMemcpyDeviceToHost, c->stream));
+  if (F) CK(c, cudaMemcpyAsync(F, c->Fout, Bz, cudaMemcpyDeviceToHost, c->stream));
+  std::vector<double> pp(3 * (size_t)real_blocks((int)c->n));
+  CK(c, cudaMemcpyAsync(pp.data(), c->Ppart, 8 * pp.size(), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (P3) {
+    double s[3] = {0, 0, 0};
+    for (size_t b = 0; b < pp.size() / 3; b++)
+      for (int q = 0; q < 3; q++) s[q] += pp[3 * b + q];
+    const double sc = c->L * F_unit(c) / 2.0;
+    for (int q = 0; q < 3; q++) P3[q] = s[q] * sc;
+  }
+  return MD_OK;
+}
+
+int md_compute_field(md_ctx* c, const double* mm, double* B) {
+  int st = check_ready(c, true);
+  if (st) return st;
+  if (!mm) return set_err(c, MD_ERR_INVALID, "null moment directions");
+  if (!c->have_geometry) return set_err(c, MD_ERR_INVALID, "call md_compute_interactions first");
+  CK(c, cudaMemcpyAsync(c->tmpmm, mm, 24 * (size_t)c->n, cudaMemcpyHostToDevice, c->stream));
+  SortedView s = sorted_view(c);
+  c->launches = launch_set_mu(c->stream, (int)c->n, c->tmpmm, c->magMom_u, c->rMag_u, s, fp64(c));
+  c->launches += launch_real(c->stream, real_params(c, c->Br2, nullptr, nullptr), false, fp64(c));
+  c->launches += launch_kspace(c->stream, k_params(c, c->Bk2, nullptr), false, fp64(c));
+  IntParams ip = int_params(c, 0.0, c->Br2, c->Bk2);
+  c->launches += launch_combine(c->stream, ip, c->Bout, nullptr, 0, fp64(c));
+  CK(c, cudaGetLastError());
+  if (B) CK(c, cudaMemcpyAsync(B, c->Bout, 24 * (size_t)c->n, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return MD_OK;
+}
+
+int md_set_noise(md_ctx* c, int mode, uint64_t seed) {
+  if (!c || mode < 0 || mode > 2) return set_err(c, MD_ERR_INVALID, "bad noise mode");
+  c->noise = mode;
+  c->seed = seed;
+  invalidate_graph(c);
+  return MD_OK;
+}
+
+static int ensure_records(md_ctx* c, int64_t extra) {
+  long long nrec = 0;
+  CK(c, cudaMemcpy(&nrec, &c->sc->nrec, sizeof nrec, cudaMemcpyDeviceToHost));
+  if (nrec + extra <= c->rec_cap) return MD_OK;
+  long long cap = std::max<long long>(1024, 2 * (nrec + extra));
+  double* nr = nullptr;
+  int st = dalloc(c, &nr, 64 * (size_t)cap);
+  if (st) return st;
+  if (c->records && nrec > 0) CK(c, cudaMemcpy(nr, c->records, 64 * (size_t)nrec, cudaMemcpyDeviceToDevice));
+  dfree(c, c->records);
+  c->records = nr;
+  c->rec_cap = cap;
+  invalidate_graph(c);
+  return MD_OK;
+}
+
+int md_step(md_ctx* c, int64_t nsteps, double dt, const double* xi) {
+  int st = check_ready(c, true);
+  if (st) return st;
+  if (nsteps < 0 || !(dt > 0)) return set_err(c, MD_ERR_INVALID, "bad nsteps or dt");
+  if (c->noise == MD_NOISE_UPLOADED && !xi) return set_err(c, MD_ERR_INVALID, "uploaded noise needs xi");
+  if (nsteps == 0) return MD_OK;
+  if (dt != c->cur_dt) {
+    std::vector<double> a, b, d;
+    mdh::noise_scales(c->cfg, c->props, dt, &a, &b, &d);
+    const size_t N8 = 8 * (size_t)c->n;
+    CK(c, cudaMemcpyAsync(c->sT, a.data(), N8, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->sB, b.data(), N8, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->sF, d.data(), N8, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    c->cur_dt = dt;
+    invalidate_graph(c);
+  }
+  if ((st = ensure_records(c, nsteps))) return st;
+  if (c->noise == MD_NOISE_UPLOADED) {
+    c->launches = 0;
+    for (int64_t s = 0; s < nsteps; s++) {
+      CK(c, cudaMemcpyAsync(c->xi, xi + (size_t)s * 9 * c->n, 72 * (size_t)c->n, cudaMemcpyHostToDevice, c->stream));
+      c->launches += issue_step(c, dt);
+    }
+    CK(c, cudaGetLastError());
+  } else {
+    if (!c->graph_valid) {
+      CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+      c->launches_per_step = issue_step(c, dt);
+      cudaError_t e = cudaStreamEndCapture(c->stream, &c->graph);
+      if (e != cudaSuccess) return set_err(c, MD_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+      CK(c, cudaGraphInstantiate(&c->gexec, c->graph, 0));
+      c->graph_valid = true;
+    }
+    for (int64_t s = 0; s < nsteps; s++) CK(c, cudaGraphLaunch(c->gexec, c->stream));
+    c->launches = c->launches_per_step * nsteps;
+  }
+  c->have_geometry = true;
+  return read_err_word(c);
+}
+
+int md_num_records(const md_ctx* cc, int64_t* count) {
+  md_ctx* c = const_cast<md_ctx*>(cc);
+  if (!c || !count) return MD_ERR_INVALID;
+  long long n = 0;
+  CK(c, cudaStreamSynchronize(c->stream));
+  CK(c, cudaMemcpy(&n, &c->sc->nrec, sizeof n, cudaMemcpyDeviceToHost));
+  *count = n;
+  return MD_OK;
+}
+
+int md_records(md_ctx* c, int64_t first, int64_t count, double* obs) {
+  int64_t n = 0;
+  int st = md_num_records(c, &n);
+  if (st) return st;
+  if (first < 0 || count < 0 || first + count > n || (!obs && count)) return set_err(c, MD_ERR_INVALID, "bad record range");
+  if (count) CK(c, cudaMemcpy(obs, c->records + 8 * first, 64 * (size_t)count, cudaMemcpyDeviceToHost));
+  return MD_OK;
+}
+
+int md_clear_records(md_ctx* c) {
+  if (!c) return MD_ERR_INVALID;
+  CK(c, cudaMemsetAsync(&c->sc->nrec, 0, sizeof(long long), c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return MD_OK;
+}
+
+int md_sync(md_ctx* c) {
+  if (!c) return MD_ERR_INVALID;
+  CK(c, cudaStreamSynchronize(c->stream));
+  return MD_OK;
+}
+
+int md_debug_cells(md_ctx* c, int64_t* ncell, int64_t* ncx, int32_t* cell_start, int32_t* perm) {
+  if (!c || !c->have_geometry) return set_err(c, MD_ERR_INVALID, "no cell list yet");
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (ncell) *ncell = c->grid.ncell;
+  if (ncx) *ncx = c->grid.ncx;
+  if (cell_start) CK(c, cudaMemcpy(cell_start, c->cell_start, 4 * (size_t)(c->grid.ncell + 1), cudaMemcpyDeviceToHost));
+  if (perm) CK(c, cudaMemcpy(perm, c->perm, 4 * (size_t)c->n, cudaMemcpyDeviceToHost));
+  return MD_OK;
+}
+
+int md_debug_structure_factor(md_ctx* c, int64_t* nk_inout, double* out5) {
+  if (!c || !nk_inout || !c->have_geometry) return set_err(c, MD_ERR_INVALID, "no structure factor yet");
+  const int nk = c->klist.nk;
+  std::vector<double2> S(nk);
+  CK(c, cudaStreamSynchronize(c->stream));
+  CK(c, cudaMemcpy(S.data(), c->Sfull, sizeof(double2) * nk, cudaMemcpyDeviceToHost));
+  int64_t cnt = 0;
+  for (int k = 0; k < nk; k++) {
+    if (!c->klist.kreal[k]) continue;
+    if (out5 && cnt < *nk_inout) {
+      double* o = out5 + 5 * cnt;
+      o[0] = c->klist.kx[k];
+      o[1] = c->klist.ky[k];
+      o[2] = c->klist.kz[k];
+      o[3] = S[k].x * c->props.muMax;
+      o[4] = S[k].y * c->props.muMax;
+    }
+    cnt++;
+  }
+  *nk_inout = cnt;
+  return MD_OK;
+}
+
+int md_debug_launches(const md_ctx* c, int64_t* launches) {
+  if (!c || !launches) return MD_ERR_INVALID;
+  *launches = c->launches;
+  return MD_OK;
+}
+
+int md_debug_pairs(md_ctx* c, int64_t* pairs) {
+  if (!c || !pairs) return set_err(c, MD_ERR_INVALID, "null argument");
+  unsigned long long v = 0;
+  CK(c, cudaStreamSynchronize(c->stream));
+  CK(c, cudaMemcpy(&v, &c->sc->pairs, sizeof v, cudaMemcpyDeviceToHost));
+  *pairs = (int64_t)(v / 2);
+  return MD_OK;
+}
+
+int md_profile(md_ctx* c, int enable) {
+  if (!c) return MD_ERR_INVALID;
+  if (enable && !c->ev[0])
+    for (int k = 0; k <= MD_NSEG; k++) CK(c, cudaEventCreate(&c->ev[k]));
+  if ((bool)enable != c->prof) invalidate_graph(c);
+  c->prof = enable != 0;
+  return MD_OK;
+}
+
+int md_profile_read(md_ctx* c, double* ms) {
+  if (!c || !ms || !c->prof) return set_err(c, MD_ERR_INVALID, "profiling not enabled");
+  CK(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < MD_NSEG; k++) {
+    float t = 0;
+    CK(c, cudaEventElapsedTime(&t, c->ev[k], c->ev[k + 1]));
+    ms[k] = t;
+  }
+  return MD_OK;
+}
+
+int md_calibrate_fp32(double* tflops) {
+  if (!tflops) return set_err(nullptr, MD_ERR_INVALID, "null argument");
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return set_err(nullptr, MD_ERR_NO_DEVICE, "no CUDA device");
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int threads = 256, blocks = nsm * 8;
+  float* out = nullptr;
+  cudaStream_t st;
+  cudaEvent_t e0, e1;
+  CK(nullptr, cudaMalloc(&out, sizeof(float) * threads * blocks));
+  CK(nullptr, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  CK(nullptr, cudaEventCreate(&e0));
+  CK(nullptr, cudaEventCreate(&e1));
+  double best = 0;
+  for (int rep = 0; rep < 6; rep++) {
+    cudaEventRecord(e0, st);
+    double flops = 0;
+    for (int q = 0; q < 4; q++) flops += launch_fma_calibration(st, out, blocks, threads);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  cudaFree(out);
+  *tflops = best;
+  return best > 0 ? MD_OK : set_err(nullptr, MD_ERR_CUDA, "calibration failed");
+}
+
+int md_autotune_ewald(md_ctx* c, int ncand, double* alpha_out, double* rc_out, int64_t* kc_out, double* best_ms) {
+  int st = check_ready(c, false);
+  if (!c || !c->have_particles) return set_err(c, MD_ERR_INVALID, "particles not set");
+  if (!c->have_state) return set_err(c, MD_ERR_INVALID, "state not uploaded");
+  (void)st;
+  if (ncand < 1) ncand = 5;
+  mdh::EwaldModel m = mdh::ewald_model(c->cfg, c->props);
+  double a0;
+  int64_t k0;
+  const double rc0 = mdh::choose_rc(c->cfg, m, c->n, &a0, &k0) / c->L;
+  cudaEvent_t e0, e1;
+  CK(c, cudaEventCreate(&e0));
+  CK(c, cudaEventCreate(&e1));
+  double best = 1e300, ba = 0, brc = 0;
+  int64_t bk = 0;
+  for (int q = 0; q < ncand; q++) {
+    const double x = ncand == 1 ? rc0 : std::min(0.5, rc0 * (0.75 + 0.6 * q / (ncand - 1)));
+    double a, kr;
+    if (!mdh::ewald_for_rc(c->cfg, m, x * c->L, &a, &kr)) continue;
+    const int64_t k = (int64_t)std::floor(kr + 0.5);
+    if (k > 64 || md_set_ewald(c, a, x * c->L, k) != MD_OK) continue;
+    float msum = 0;
+    for (int rep = 0; rep < 3; rep++) {
+      CK(c, cudaEventRecord(e0, c->stream));
+      issue_interactions(c);
+      launch_real(c->stream, real_params(c, c->Br2, nullptr, nullptr), false, fp64(c));
+      launch_kspace(c->stream, k_params(c, c->Bk2, nullptr), false, fp64(c));
+      CK(c, cudaEventRecord(e1, c->stream));
+      CK(c, cudaEventSynchronize(e1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) msum += ms;
+    }
+    const double ms = msum / 2;
+    if (ms < best) {
+      best = ms;
+      ba = a;
+      brc = x * c->L;
+      bk = k;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best >= 1e300) return set_err(c, MD_ERR_INVALID, "no candidate cutoff met the error model");
+  if ((st = md_set_ewald(c, ba, brc, bk))) return st;
+  if (alpha_out) *alpha_out = ba;
+  if (rc_out) *rc_out = brc;
+  if (kc_out) *kc_out = bk;
+  if (best_ms) *best_ms = best;
+  return MD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,307 @@
+// md_integrate.cu -- kernel (d): fused stochastic Heun step of the moment
+// (LLG), the easy axis and the translation, with the thermal noise.
+// Restates, per particle:
+//   DefExtField                   src/simulation.cpp:546-556
+//   DefThermFluct                 src/simulation.cpp:563-603
+//   RKCoeffs                      src/simulation.cpp:876-902
+//   IntegrationRot (HEUN_EULER)   src/simulation.cpp:721-749, 866-867
+//   IntegrationTrans              src/simulation.cpp:959-962
+//   ApplyBoundaryCondArr          src/simulation.cpp:610-620
+//   EvalTransCoeffs, mz record    src/postprocessing.cpp:167-187,
+//                                 src/simulation.cpp:514-515
+// Stage 1 (k_heun1) evaluates k1 with the interaction field, forms the
+// predictor (m2, n2) and writes its moments into the sorted view for the
+// second field evaluation.  Stage 2 (k_heun2) evaluates k2, applies the
+// corrector, renormalises, translates with the force of the step start plus
+// the overlap push, wraps, and accumulates MSD and m_z.  The thermal torque,
+// field and force are drawn once per step and frozen across the two stages
+// (the reference draws them once in DefThermFluct).
+//
+// Precision: T = float (mixed) or double.  Positions, the master copies of
+// m and n, the self/surface Ewald terms and all reductions are FP64.
+//
+// Roofline: HBM/L2 bound, tiny; per particle and step ~250 B of algorithmic
+// traffic (state 72 B read + 72 B written, stage outputs, work arrays).
+#include "md_common.cuh"
+#include "md_kernels.h"
+
+namespace md {
+
+constexpr int kIntThreads = 256;
+
+__device__ __forceinline__ double ext_field_z(const IntParams& p, double t) {
+  if (p.field_kind == 1) return p.fieldAmp * sinpi(2.0 * p.fieldFreq * t);
+  return t < p.tMag ? p.magFluxDens : 0.0;
+}
+
+// RKCoeffs: Beff = ext + demag + anisConst (m.n) n + B_th;
+// dn/dt = velEa1 (m.n)(m - (m.n) n) + velEa2 (tau_th x n);
+// dm/dt = -velMmConst (m x Beff + magDamp m x (m x Beff)).
+template <typename T>
+__device__ __forceinline__ void rk(const IntParams& p, const T m[3], const T e[3], const T bd[3], T bz_ext,
+                                   const T bth[3], const T tau[3], T v1, T v2, T km[3], T ke[3]) {
+  const T dot = m[0] * e[0] + m[1] * e[1] + m[2] * e[2];
+  const T ac = (T)p.anisConst;
+  T be[3];
+  be[0] = bd[0] + ac * (e[0] * dot) + bth[0];
+  be[1] = bd[1] + ac * (e[1] * dot) + bth[1];
+  be[2] = (bz_ext + bd[2]) + ac * (e[2] * dot) + bth[2];
+  if (p.mobil) {
+    const T c0 = tau[1] * e[2] - tau[2] * e[1];
+    const T c1 = tau[2] * e[0] - tau[0] * e[2];
+    const T c2 = tau[0] * e[1] - tau[1] * e[0];
+    const T f = v1 * dot;
+    ke[0] = (m[0] - e[0] * dot) * f + c0 * v2;
+    ke[1] = (m[1] - e[1] * dot) * f + c1 * v2;
+    ke[2] = (m[2] - e[2] * dot) * f + c2 * v2;
+  } else {
+    ke[0] = ke[1] = ke[2] = 0;
+  }
+  const T x0 = m[1] * be[2] - m[2] * be[1];
+  const T x1 = m[2] * be[0] - m[0] * be[2];
+  const T x2 = m[0] * be[1] - m[1] * be[0];
+  const T y0 = m[1] * x2 - m[2] * x1;
+  const T y1 = m[2] * x0 - m[0] * x2;
+  const T y2 = m[0] * x1 - m[1] * x0;
+  const T vm = (T)p.velMmConst, md = (T)p.magDamp;
+  km[0] = -vm * (x0 + md * y0);
+  km[1] = -vm * (x1 + md * y1);
+  km[2] = -vm * (x2 + md * y2);
+}
+
+// Demagnetising field of particle i (sorted slot r) in SI.
+template <typename T>
+__device__ __forceinline__ void demag_si(const IntParams& p, int r, T b[3]) {
+  using T4 = typename V4<T>::t;
+  const int n = p.n;
+  const T* Br = (const T*)p.Br;
+  const T* Bk = (const T*)p.Bk;
+  const T4 mu = ((const T4*)p.s.mu)[r];
+  const double mu3[3] = {(double)mu.x, (double)mu.y, (double)mu.z};
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const double selfsurf = p.cself * mu3[a] - p.csurf * p.musum[a];
+    b[a] = (T)((((double)Br[a * n + r] + (double)Bk[a * n + r]) + selfsurf) * p.B_unit);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kIntThreads) k_heun1(IntParams p) {
+  using T4 = typename V4<T>::t;
+  const int i = blockIdx.x * kIntThreads + threadIdx.x;
+  const int n = p.n;
+  if (i >= n) return;
+  const int r = p.s.rank[i];
+  T m[3], e[3], bd[3], z[9];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    m[a] = (T)p.mm[a * n + i];
+    e[a] = (T)p.ea[a * n + i];
+  }
+  demag_si<T>(p, r, bd);
+  if (p.noise == 2) {
+    philox_normals9<T>(p.seed, (uint64_t)*p.stepno, (uint32_t)i, z);
+  } else if (p.noise == 1) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) z[q] = (T)p.xi[(q / 3) * 3 * n + (q % 3) * n + i];
+  } else {
+#pragma unroll
+    for (int q = 0; q < 9; q++) z[q] = 0;
+  }
+  const T sT = (T)p.sT[i], sB = (T)p.sB[i], sF = (T)p.sF[i];
+  T tau[3], bth[3];
+  T* th = (T*)p.th;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    tau[a] = sT * z[a];
+    bth[a] = sB * z[3 + a];
+    th[a * n + i] = tau[a];
+    th[(3 + a) * n + i] = bth[a];
+    th[(6 + a) * n + i] = sF * z[6 + a];
+  }
+  const T bz = (T)ext_field_z(p, *p.time);
+  T km[3], ke[3];
+  rk<T>(p, m, e, bd, bz, bth, tau, (T)p.velEa1[i], (T)p.velEa2[i], km, ke);
+  const T dt = (T)p.dt;
+  T* k1m = (T*)p.k1m;
+  T* k1e = (T*)p.k1e;
+  T* m2 = (T*)p.m2;
+  T* e2 = (T*)p.e2;
+  T mm2[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    k1m[a * n + i] = km[a];
+    k1e[a * n + i] = ke[a];
+    e2[a * n + i] = e[a] + dt * ke[a];
+    mm2[a] = m[a] + dt * km[a];
+    m2[a * n + i] = mm2[a];
+  }
+  const T mu = (T)p.magMom_u[i];
+  T4 v;
+  v.x = mm2[0] * mu;
+  v.y = mm2[1] * mu;
+  v.z = mm2[2] * mu;
+  v.w = (T)p.rMag_u[i];
+  ((T4*)p.s.mu)[r] = v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kIntThreads) k_heun2(IntParams p) {
+  const int i = blockIdx.x * kIntThreads + threadIdx.x;
+  const int n = p.n;
+  double acc[4] = {0, 0, 0, 0};
+  if (i < n) {
+    const int r = p.s.rank[i];
+    const T* th = (const T*)p.th;
+    T m[3], e[3], m2[3], e2[3], bd[3], tau[3], bth[3], k1m[3], k1e[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      m[a] = (T)p.mm[a * n + i];
+      e[a] = (T)p.ea[a * n + i];
+      m2[a] = ((const T*)p.m2)[a * n + i];
+      e2[a] = ((const T*)p.e2)[a * n + i];
+      k1m[a] = ((const T*)p.k1m)[a * n + i];
+      k1e[a] = ((const T*)p.k1e)[a * n + i];
+      tau[a] = th[a * n + i];
+      bth[a] = th[(3 + a) * n + i];
+    }
+    demag_si<T>(p, r, bd);
+    const T bz = (T)ext_field_z(p, *p.time);
+    T km[3], ke[3];
+    rk<T>(p, m2, e2, bd, bz, bth, tau, (T)p.velEa1[i], (T)p.velEa2[i], km, ke);
+    const T dt = (T)p.dt, h = (T)0.5;
+    T mn[3], en[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      en[a] = e[a] + dt * (h * k1e[a] + h * ke[a]);
+      mn[a] = m[a] + dt * (h * k1m[a] + h * km[a]);
+    }
+    const T nm = sqrt(mn[0] * mn[0] + mn[1] * mn[1] + mn[2] * mn[2]);
+    const T ne = sqrt(en[0] * en[0] + en[1] * en[1] + en[2] * en[2]);
+    const T* Fr = (const T*)p.Fr;
+    const T* Fk = (const T*)p.Fk;
+    const T* ov = (const T*)p.ov;
+    const double L = p.L, half = 0.5 * L, dtd = p.dt;
+    const T izt = (T)p.invZt[i];
+    bool bad = false;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const T mf = mn[a] / nm, ef = en[a] / ne;
+      p.mm[a * n + i] = (double)mf;
+      p.ea[a * n + i] = (double)ef;
+      const T f = (T)(((double)Fr[a * n + r] + (double)Fk[a * n + r]) * p.F_unit) + th[(6 + a) * n + i];
+      double x = p.pos[a * n + i] + (double)ov[a * n + r] * L + dtd * (double)(f * izt);
+      x -= L * (double)(x > half);
+      x += L * (double)(x < -half);
+      p.pos[a * n + i] = x;
+      double tp = p.truePos[a * n + i];
+      tp = x + round((tp - x) / L) * L;
+      p.truePos[a * n + i] = tp;
+      const double d = tp - p.posRef[a * n + i];
+      acc[a] = d * d;
+      bad |= !isfinite(x) || !isfinite((double)mf) || !isfinite((double)ef);
+    }
+    acc[3] = p.mm[2 * n + i];
+    if (bad) atomicOr(p.err, kErrNonFinite);
+  }
+  __shared__ double red[4][kIntThreads / 32];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const double v = warp_sum(acc[q]);
+    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double s = 0;
+    for (int w = 0; w < kIntThreads / 32; w++) s += red[threadIdx.x][w];
+    p.obs_part[4 * blockIdx.x + threadIdx.x] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_obs(ObsParams p) {
+  __shared__ double red[7][8];
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < p.nblk_int; b += blockDim.x)
+    for (int q = 0; q < 4; q++) acc[q] += p.obs_part[4 * b + q];
+  for (int b = threadIdx.x; b < p.nblk_real; b += blockDim.x)
+    for (int q = 0; q < 3; q++) acc[4 + q] += p.Ppart[3 * b + q];
+  for (int q = 0; q < 7; q++) {
+    const double v = warp_sum(acc[q]);
+    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s[7];
+    for (int q = 0; q < 7; q++) {
+      s[q] = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) s[q] += red[q][w];
+    }
+    const long long k = *p.nrec;
+    if (k < p.cap) {
+      double* o = p.records + 8 * k;
+      o[0] = *p.time;
+      o[1] = s[3] * p.inv_n;
+      o[2] = s[0] * p.inv_n;
+      o[3] = s[1] * p.inv_n;
+      o[4] = s[2] * p.inv_n;
+      o[5] = s[4] * p.p_scale;
+      o[6] = s[5] * p.p_scale;
+      o[7] = s[6] * p.p_scale;
+      *p.nrec = k + 1;
+    }
+    *p.time += p.dt;
+    *p.stepno += 1;
+  }
+}
+
+// B and F in SI, particle order; optional overlap push of the positions
+// (CompInteractVecs moves the positions, src/interaction.cpp:126-127).
+template <typename T>
+__global__ void k_combine(IntParams p, double* Bout, double* Fout, int apply_overlap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = p.n;
+  if (i >= n) return;
+  const int r = p.s.rank[i];
+  T b[3];
+  demag_si<T>(p, r, b);
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    if (Bout) Bout[a * n + i] = (double)b[a];
+    if (Fout)
+      Fout[a * n + i] = ((double)((const T*)p.Fr)[a * n + r] + (double)((const T*)p.Fk)[a * n + r]) * p.F_unit;
+    if (apply_overlap) p.pos[a * n + i] += (double)((const T*)p.ov)[a * n + r] * p.L;
+  }
+}
+
+int int_blocks(int n) { return (n + kIntThreads - 1) / kIntThreads; }
+
+int launch_heun1(cudaStream_t st, const IntParams& p, bool fp64) {
+  if (fp64)
+    k_heun1<double><<<int_blocks(p.n), kIntThreads, 0, st>>>(p);
+  else
+    k_heun1<float><<<int_blocks(p.n), kIntThreads, 0, st>>>(p);
+  return 1;
+}
+
+int launch_heun2(cudaStream_t st, const IntParams& p, bool fp64) {
+  if (fp64)
+    k_heun2<double><<<int_blocks(p.n), kIntThreads, 0, st>>>(p);
+  else
+    k_heun2<float><<<int_blocks(p.n), kIntThreads, 0, st>>>(p);
+  return 1;
+}
+
+int launch_obs(cudaStream_t st, const ObsParams& p) {
+  k_obs<<<1, 256, 0, st>>>(p);
+  return 1;
+}
+
+int launch_combine(cudaStream_t st, const IntParams& p, double* Bout, double* Fout, int apply_overlap, bool fp64) {
+  if (fp64)
+    k_combine<double><<<(p.n + 255) / 256, 256, 0, st>>>(p, Bout, Fout, apply_overlap);
+  else
+    k_combine<float><<<(p.n + 255) / 256, 256, 0, st>>>(p, Bout, Fout, apply_overlap);
+  return 1;
+}
+
+}  // namespace md
