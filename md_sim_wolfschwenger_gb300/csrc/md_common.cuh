@@ -76,9 +76,13 @@ struct KParams {
   int chunk;             // particles per chunk of the structure-factor grid
   int nchunk;
   double two_pi;         // 2 * my_pi (FP64 phases follow the reference's pi)
-  const KSeg* seg;       // [nseg] sorted by len (desc)
-  const int* koff;       // [nseg] k index of the segment's first k
-  const double* ek;      // [nk] 2 exp(-w n^2) / n^2 (0 for padding)
+  const KSeg* seg;       // [nseg] sorted by len (desc): structure-factor threads
+  const int* koff;       // [nseg] k index of the segment's first k (sorted order)
+  const double* ek;      // [nk] 2 exp(-w n^2) / n^2 (0 for padding), sorted order
+  const KSeg* rseg;      // [nseg] the same segments in row order (nz, ny ascending)
+  const int* rowpos;     // [nk] sorted k index -> row-order k index
+  const int2* chunks;    // [nchk + 1] (first row segment, first row-order k)
+  int nchk;              // chunks of <= kKChunk row-order k's (scatter staging)
   double2* Spart;        // [nchunk][nk] partial structure factors
   double* musum_part;    // [nchunk][3]
   double* musum;         // [3]
@@ -120,16 +124,16 @@ struct IntParams {
   const void *Br, *Bk, *Fr, *Fk, *ov;
   SortedView s;
   const double* musum;       // [3] sum of mu' of the evaluated stage
-  double* obs_part;          // [gridDim.x][4]: msd x,y,z, mz
+  const double* Ppart;       // [n][3] per-particle pressure sums of the full real-space pass
+  double* obs_part;          // [gridDim.x][7]: msd x,y,z, mz, Pxy, Pxz, Pyz
   const double* time;        // device t (double) and step
   const long long* stepno;
   int* err;
 };
 
 struct ObsParams {
-  int nblk_int, nblk_real;
+  int nblk_int;
   const double* obs_part;
-  const double* Ppart;
   double p_scale;            // L * F_unit / (2 * volBox) (pair double count)
   double inv_n;
   double dt;

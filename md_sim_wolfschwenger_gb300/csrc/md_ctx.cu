@@ -93,6 +93,9 @@ struct md_ctx {
   KSeg* kseg = nullptr;
   int* koff = nullptr;
   double* ek = nullptr;
+  KSeg* rseg = nullptr;
+  int* rowpos = nullptr;
+  int2* chunks = nullptr;
   double2* Spart = nullptr;
   double* musum_part = nullptr;
   void* eS = nullptr;
@@ -228,6 +231,10 @@ static KParams k_params(md_ctx* c, void* B, void* F) {
   p.seg = c->kseg;
   p.koff = c->koff;
   p.ek = c->ek;
+  p.rseg = c->rseg;
+  p.rowpos = c->rowpos;
+  p.chunks = c->chunks;
+  p.nchk = c->klist.nchk;
   p.Spart = c->Spart;
   p.musum_part = c->musum_part;
   p.musum = c->sc->musum;
@@ -290,6 +297,7 @@ static IntParams int_params(md_ctx* c, double dt, const void* Br, const void* Bk
   p.s = sorted_view(c);
   p.musum = c->sc->musum;
   p.obs_part = c->obs_part;
+  p.Ppart = c->Ppart;
   p.time = &c->sc->time;
   p.stepno = &c->sc->step;
   p.err = &c->sc->err;
@@ -334,9 +342,7 @@ static int issue_step(md_ctx* c, double dt) {
   mark(c, MD_SEG_OBS);
   ObsParams o{};
   o.nblk_int = int_blocks((int)c->n);
-  o.nblk_real = real_blocks((int)c->n);
   o.obs_part = c->obs_part;
-  o.Ppart = c->Ppart;
   o.p_scale = c->L * F_unit(c) / (2.0 * std::pow(c->L, 3.0));
   o.inv_n = 1.0 / (double)c->n;
   o.dt = dt;
@@ -477,12 +483,12 @@ int md_ctx_create(const md_config* cfg, int64_t n, int precision, md_ctx** out) 
   for (auto p : t3)
     if ((st = dalloc(c, p, 3 * T * N))) return fail(st);
   if ((st = dalloc(c, &c->th, 9 * T * N))) return fail(st);
-  if ((st = dalloc(c, &c->Ppart, 24 * (size_t)real_blocks((int)n)))) return fail(st);
-  if ((st = dalloc(c, &c->obs_part, 32 * (size_t)int_blocks((int)n)))) return fail(st);
+  if ((st = dalloc(c, &c->Ppart, 24 * N))) return fail(st);
+  if ((st = dalloc(c, &c->obs_part, 56 * (size_t)int_blocks((int)n)))) return fail(st);
   if ((st = dalloc(c, &c->sc, sizeof(DevScalars)))) return fail(st);
   if (cudaMemsetAsync(c->sc, 0, sizeof(DevScalars), c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->xi, 0, 72 * N, c->stream) != cudaSuccess ||
-      cudaMemsetAsync(c->Ppart, 0, 24 * (size_t)real_blocks((int)n), c->stream) != cudaSuccess)
+      cudaMemsetAsync(c->Ppart, 0, 24 * N, c->stream) != cudaSuccess)
     return fail(set_err(nullptr, MD_ERR_CUDA, "initial memset failed"));
   *out = c;
   return MD_OK;
@@ -672,6 +678,7 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
   const int nsegb = (int)((c->klist.seg.size() + 255) / 256);
   int nch = std::max(1, (4 * nsm + nsegb - 1) / nsegb);
+  nch = std::max<int64_t>(nch, (c->n + 511) / 512);  // FP32 sums over <= 512 particles
   nch = std::min<int64_t>(nch, (c->n + 31) / 32);
   c->chunk = (int)(((c->n + nch - 1) / nch + 31) / 32 * 32);
   c->nchunk = (int)((c->n + c->chunk - 1) / c->chunk);
@@ -692,16 +699,19 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
     CK(c, cudaMemcpy(c->cell_start, h, sizeof h, cudaMemcpyHostToDevice));
   }
   const size_t nk = (size_t)c->klist.nk, nseg = c->klist.seg.size();
-  if (nk > c->ksize_cap || nseg > c->ksize_cap) {
-    void* old[] = {c->kseg, c->koff, c->ek, c->eS, c->Sfull};
+  if (nk + 2 > c->ksize_cap || nseg + 2 > c->ksize_cap) {
+    void* old[] = {c->kseg, c->koff, c->ek, c->eS, c->Sfull, c->rseg, c->rowpos, c->chunks};
     for (void* p : old) dfree(c, p);
-    const size_t cap = std::max(nk, nseg);
+    const size_t cap = std::max(nk, nseg) + 2;
     int st;
     if ((st = dalloc(c, &c->kseg, sizeof(KSeg) * cap))) return st;
     if ((st = dalloc(c, &c->koff, sizeof(int) * cap))) return st;
     if ((st = dalloc(c, &c->ek, sizeof(double) * cap))) return st;
     if ((st = dalloc(c, &c->eS, 2 * tsz(c) * cap))) return st;
     if ((st = dalloc(c, &c->Sfull, sizeof(double2) * cap))) return st;
+    if ((st = dalloc(c, &c->rseg, sizeof(KSeg) * cap))) return st;
+    if ((st = dalloc(c, &c->rowpos, sizeof(int) * cap))) return st;
+    if ((st = dalloc(c, &c->chunks, sizeof(int2) * cap))) return st;
     c->ksize_cap = cap;
   }
   const size_t sp = nk * (size_t)c->nchunk;
@@ -722,6 +732,9 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
   CK(c, cudaMemcpy(c->kseg, c->klist.seg.data(), sizeof(KSeg) * nseg, cudaMemcpyHostToDevice));
   CK(c, cudaMemcpy(c->koff, c->klist.koff.data(), sizeof(int) * nseg, cudaMemcpyHostToDevice));
   CK(c, cudaMemcpy(c->ek, c->klist.ek.data(), sizeof(double) * nk, cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->rseg, c->klist.rseg.data(), sizeof(KSeg) * nseg, cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->rowpos, c->klist.rowpos.data(), sizeof(int) * nk, cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->chunks, c->klist.chunks.data(), sizeof(int) * c->klist.chunks.size(), cudaMemcpyHostToDevice));
   c->have_ewald = true;
   c->have_geometry = false;
   return MD_OK;
@@ -737,7 +750,7 @@ int md_compute_interactions(md_ctx* c, double* B, double* F, double* P3) {
   const size_t Bz = 24 * (size_t)c->n;
   if (B) CK(c, cudaMemcpyAsync(B, c->Bout, Bz, cudaMemcpyDeviceToHost, c->stream));
   if (F) CK(c, cudaMemcpyAsync(F, c->Fout, Bz, cudaMemcpyDeviceToHost, c->stream));
-  std::vector<double> pp(3 * (size_t)real_blocks((int)c->n));
+  std::vector<double> pp(3 * (size_t)c->n);
   CK(c, cudaMemcpyAsync(pp.data(), c->Ppart, 8 * pp.size(), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   if (P3) {

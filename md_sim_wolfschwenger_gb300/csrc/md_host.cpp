@@ -511,11 +511,32 @@ KList build_klist(int kc, double w) {
   std::vector<int> order(segs.size());
   for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return segs[a].len > segs[b].len; });
+  // row order (generation order): k offsets and chunks of <= kKChunk k's
+  std::vector<int> rkoff(segs.size());
+  int roff = 0;
+  L.rseg = segs;
+  L.chunks.clear();
+  int chunk_k = 0;
+  for (size_t s = 0; s < segs.size(); s++) {
+    if (s == 0 || chunk_k + segs[s].len > md::kKChunk) {
+      L.chunks.push_back((int)s);
+      L.chunks.push_back(roff);
+      chunk_k = 0;
+    }
+    rkoff[s] = roff;
+    roff += segs[s].len;
+    chunk_k += segs[s].len;
+  }
+  L.nchk = (int)L.chunks.size() / 2;
+  L.chunks.push_back((int)segs.size());
+  L.chunks.push_back(roff);
+  L.rowpos.clear();
   int off = 0;
   for (int idx : order) {
     const md::KSeg& sg = segs[idx];
     L.seg.push_back(sg);
     L.koff.push_back(off);
+    for (int t = 0; t < sg.len; t++) L.rowpos.push_back(rkoff[idx] + t);
     for (int t = 0; t < sg.len; t++) {
       int nx = sg.nx0 + t;
       bool real = t < reals[idx];

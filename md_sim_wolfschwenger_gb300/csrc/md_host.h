@@ -54,9 +54,13 @@ double model_cost(double rc_box, int64_t kc, int64_t n);
 
 // ------------------------------------------------------ k-vector list
 struct KList {
-  std::vector<md::KSeg> seg;
+  std::vector<md::KSeg> seg;   // length-sorted (structure factor)
   std::vector<int> koff;
   std::vector<double> ek;
+  std::vector<md::KSeg> rseg;  // row order (scatter)
+  std::vector<int> rowpos;     // sorted k -> row-order k
+  std::vector<int> chunks;     // pairs (first row segment, first row k), nchk + 1 pairs
+  int nchk = 0;
   std::vector<int> kx, ky, kz;  // per padded k (padding k's are marked by kreal = 0)
   std::vector<char> kreal;
   int nk = 0, nk_real = 0;

@@ -149,8 +149,12 @@ template <typename T>
 __global__ void __launch_bounds__(kIntThreads) k_heun2(IntParams p) {
   const int i = blockIdx.x * kIntThreads + threadIdx.x;
   const int n = p.n;
-  double acc[4] = {0, 0, 0, 0};
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   if (i < n) {
+    // pressure partials of the real-space pass (any order sums the same pairs)
+    acc[4] = p.Ppart[3 * i];
+    acc[5] = p.Ppart[3 * i + 1];
+    acc[6] = p.Ppart[3 * i + 2];
     const int r = p.s.rank[i];
     const T* th = (const T*)p.th;
     T m[3], e[3], m2[3], e2[3], bd[3], tau[3], bth[3], k1m[3], k1e[3];
@@ -204,17 +208,17 @@ __global__ void __launch_bounds__(kIntThreads) k_heun2(IntParams p) {
     acc[3] = p.mm[2 * n + i];
     if (bad) atomicOr(p.err, kErrNonFinite);
   }
-  __shared__ double red[4][kIntThreads / 32];
+  __shared__ double red[7][kIntThreads / 32];
 #pragma unroll
-  for (int q = 0; q < 4; q++) {
+  for (int q = 0; q < 7; q++) {
     const double v = warp_sum(acc[q]);
     if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v;
   }
   __syncthreads();
-  if (threadIdx.x < 4) {
+  if (threadIdx.x < 7) {
     double s = 0;
     for (int w = 0; w < kIntThreads / 32; w++) s += red[threadIdx.x][w];
-    p.obs_part[4 * blockIdx.x + threadIdx.x] = s;
+    p.obs_part[7 * blockIdx.x + threadIdx.x] = s;
   }
 }
 
@@ -222,9 +226,7 @@ __global__ void __launch_bounds__(256) k_obs(ObsParams p) {
   __shared__ double red[7][8];
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < p.nblk_int; b += blockDim.x)
-    for (int q = 0; q < 4; q++) acc[q] += p.obs_part[4 * b + q];
-  for (int b = threadIdx.x; b < p.nblk_real; b += blockDim.x)
-    for (int q = 0; q < 3; q++) acc[4 + q] += p.Ppart[3 * b + q];
+    for (int q = 0; q < 7; q++) acc[q] += p.obs_part[7 * b + q];
   for (int q = 0; q < 7; q++) {
     const double v = warp_sum(acc[q]);
     if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v;

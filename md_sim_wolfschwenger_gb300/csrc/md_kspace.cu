@@ -11,30 +11,55 @@
 //
 // k vectors are stored as row segments (fixed ny, nz; up to 16 consecutive
 // nx, padded to a multiple of 4 with e = 0).  Within a segment the phase is
-// advanced by one complex multiply per k; each segment starts from per-
-// particle tables X(n) = exp(2 pi i n x / L), n = 0..kc, that are evaluated
-// directly (every 4th entry and n < 4) or as one product of two direct
-// entries.  On the mixed path the table phases are reduced exactly in 32-bit
-// fixed point before sincospif.
+// advanced by one complex multiply per k, starting from a directly evaluated
+// phase (at most 16 recurrence steps).  Direct phases: on the mixed path the
+// argument n x / L is reduced exactly in 32-bit fixed point before
+// sincospif; the FP64 path uses sincos(2 my_pi n x / L) like the reference.
 //
-// Structure factor (k_sk): threads = segments, particles staged through
-// shared-memory tiles of 32; FP32 sums per tile, compensated (Kahan) FP32
-// across tiles, FP64 across particle chunks (k_sk_reduce).
-// Scatter (k_kscatter): threads = particles, per-thread tables in shared
-// memory; per segment FP32, blocks of 8 segments added with Kahan (mixed).
+// Structure factor (k_sk): threads = segments (sorted by length so warps are
+// uniform), particles staged through shared-memory tiles of 64 with their
+// per-axis phase tables; FP32 sums over a chunk of <= 512 particles, FP64
+// across chunks (k_sk_reduce), which also applies e(n) and writes e*S in row
+// order for the scatter.
+// Scatter (k_kscatter): threads = particles; the block walks the k rows in
+// order, staging e*S and the segments chunk by chunk in shared memory; the
+// x phase comes from a per-thread table, y and z phases per row (direct
+// every 8th row, otherwise one multiply).  FP32 per segment, blocks of 8
+// segments added with Kahan compensation (mixed path).
 //
-// Roofline: FP32 issue bound.  Algorithmic FLOPs per (k, particle): 14 for
-// the structure factor, 12 for the field scatter, 22 for field + force.
+// Roofline: FP32 issue bound.  Algorithmic FLOPs per (k, particle): 11 for
+// the structure factor, 12 for the field scatter, 21 for field + force.
 #include "md_common.cuh"
 #include "md_kernels.h"
 
 namespace md {
 
 constexpr int kSkThreads = 256;
-constexpr int kSkTile = 32;
+constexpr int kSkTile = 64;
 constexpr int kSegMax = 16;
 
-// Table of exp(2 pi i n x) for n = 0..kc at out[n * stride].
+// exp(2 pi i n x) evaluated directly.
+template <typename T>
+__device__ __forceinline__ typename V2<T>::t phase_direct(int nn, unsigned sfix, double xb, double two_pi) {
+  using T2 = typename V2<T>::t;
+  T2 v;
+  if constexpr (std::is_same<T, float>::value) {
+    const int ph = (int)((unsigned)nn * sfix);  // exact reduction mod one box length
+    float s, c;
+    sincospif(2.0f * ((float)ph * 2.3283064365386963e-10f), &s, &c);
+    v.x = c;
+    v.y = s;
+  } else {
+    double s, c;
+    sincos(two_pi * (double)nn * xb, &s, &c);
+    v.x = c;
+    v.y = s;
+  }
+  return v;
+}
+
+// Table of exp(2 pi i n x) for n = 0..kc at out[n * stride]: direct for
+// n < 4 and multiples of 4, otherwise the product of two direct entries.
 template <typename T>
 __device__ __forceinline__ void fill_table(typename V2<T>::t* out, int stride, int kc, unsigned sfix, double xb,
                                            double two_pi) {
@@ -42,22 +67,10 @@ __device__ __forceinline__ void fill_table(typename V2<T>::t* out, int stride, i
   for (int nn = 0; nn <= kc; nn++) {
     T2 v;
     if (nn < 4 || (nn & 3) == 0) {
-      if constexpr (std::is_same<T, float>::value) {
-        int ph = (int)((unsigned)nn * sfix);  // exact reduction mod 1 box
-        float s, c;
-        sincospif(2.0f * ((float)ph * 2.3283064365386963e-10f), &s, &c);
-        v = make_float2(c, s);
-      } else {
-        double s, c;
-        sincos(two_pi * (double)nn * xb, &s, &c);
-        v = make_double2(c, s);
-      }
+      v = phase_direct<T>(nn, sfix, xb, two_pi);
     } else {
-      T2 a = out[(nn & ~3) * stride], b = out[(nn & 3) * stride];
-      T cr, ci;
-      cmul<T>(a.x, a.y, b.x, b.y, cr, ci);
-      v.x = cr;
-      v.y = ci;
+      const T2 a = out[(nn & ~3) * stride], b = out[(nn & 3) * stride];
+      cmul<T>(a.x, a.y, b.x, b.y, v.x, v.y);
     }
     out[nn * stride] = v;
   }
@@ -66,24 +79,26 @@ __device__ __forceinline__ void fill_table(typename V2<T>::t* out, int stride, i
 template <typename T>
 __device__ __forceinline__ void particle_coord(const SortedView& s, int k, int ax, unsigned& sfix, double& xb) {
   if constexpr (std::is_same<T, float>::value) {
-    int4 q = s.xi[k];
+    const int4 q = s.xi[k];
     sfix = (unsigned)(ax == 0 ? q.x : (ax == 1 ? q.y : q.z));
     xb = 0.0;
   } else {
-    double4_32a q = s.xd[k];
+    const double4_32a q = s.xd[k];
     xb = ax == 0 ? q.x : (ax == 1 ? q.y : q.z);
     sfix = 0;
   }
 }
 
+// ------------------------------------------------------ structure factor
+
 template <typename T>
-__global__ void __launch_bounds__(kSkThreads) k_sk(KParams p) {
+__global__ void __launch_bounds__(kSkThreads, 2) k_sk(KParams p) {
   using T2 = typename V2<T>::t;
   using T4 = typename V4<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int K1 = p.kc + 1;
-  T2* tab = (T2*)smem_raw;
-  T4* mus = (T4*)(tab + kSkTile * 3 * K1);
+  T2* tab = (T2*)smem_raw;                   // [kSkTile][3][K1]
+  T4* mus = (T4*)(tab + kSkTile * 3 * K1);   // [kSkTile]
   const int tid = threadIdx.x;
   const int sidx = blockIdx.x * kSkThreads + tid;
   const int chunk = blockIdx.y;
@@ -94,9 +109,9 @@ __global__ void __launch_bounds__(kSkThreads) k_sk(KParams p) {
   const int len = sg.len;
   const int ax0 = sg.nx0 < 0 ? -sg.nx0 : sg.nx0, ay = sg.ny < 0 ? -sg.ny : sg.ny;
   const T nx0f = (T)sg.nx0, nyf = (T)sg.ny, nzf = (T)sg.nz;
-  T sc[kSegMax], ss[kSegMax], cc[kSegMax], cs[kSegMax];
+  T sc[kSegMax], ss[kSegMax];
 #pragma unroll
-  for (int c = 0; c < kSegMax; c++) sc[c] = ss[c] = cc[c] = cs[c] = 0;
+  for (int c = 0; c < kSegMax; c++) sc[c] = ss[c] = 0;
 
   for (int t0 = p0; t0 < p1; t0 += kSkTile) {
     const int tn = min(kSkTile, p1 - t0);
@@ -111,12 +126,10 @@ __global__ void __launch_bounds__(kSkThreads) k_sk(KParams p) {
     for (int pp = tid; pp < tn; pp += kSkThreads) mus[pp] = ((const T4*)p.s.mu)[t0 + pp];
     __syncthreads();
     if (!has) continue;
-    T ac[kSegMax], as[kSegMax];
-#pragma unroll
-    for (int c = 0; c < kSegMax; c++) ac[c] = as[c] = 0;
     for (int pp = 0; pp < tn; pp++) {
       const T2* tb = tab + pp * 3 * K1;
-      T2 X = tb[ax0], Y = tb[K1 + ay], Z = tb[2 * K1 + sg.nz], E = tb[1];
+      T2 X = tb[ax0], Y = tb[K1 + ay];
+      const T2 Z = tb[2 * K1 + sg.nz], E = tb[1];
       if (sg.nx0 < 0) X.y = -X.y;
       if (sg.ny < 0) Y.y = -Y.y;
       T yr, yi, pr, pi;
@@ -129,8 +142,8 @@ __global__ void __launch_bounds__(kSkThreads) k_sk(KParams p) {
         if (c >= len) break;
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-          ac[c + u] += w * pr;
-          as[c + u] += w * pi;
+          sc[c + u] += w * pr;
+          ss[c + u] += w * pi;
           const T npr = pr * E.x - pi * E.y;
           pi = pr * E.y + pi * E.x;
           pr = npr;
@@ -138,28 +151,12 @@ __global__ void __launch_bounds__(kSkThreads) k_sk(KParams p) {
         }
       }
     }
-#pragma unroll
-    for (int c = 0; c < kSegMax; c++) {
-      if constexpr (std::is_same<T, float>::value) {
-        float y = ac[c] - cc[c], t = sc[c] + y;
-        cc[c] = (t - sc[c]) - y;
-        sc[c] = t;
-        y = as[c] - cs[c];
-        t = ss[c] + y;
-        cs[c] = (t - ss[c]) - y;
-        ss[c] = t;
-      } else {
-        sc[c] += ac[c];
-        ss[c] += as[c];
-      }
-    }
   }
   if (has) {
-    const int ko = p.koff[sidx];
-    double2* out = p.Spart + (size_t)chunk * p.nk + ko;
+    double2* out = p.Spart + (size_t)chunk * p.nk + p.koff[sidx];
 #pragma unroll
     for (int c = 0; c < kSegMax; c++)
-      if (c < len) out[c] = make_double2((double)sc[c] - (double)cc[c], (double)ss[c] - (double)cs[c]);
+      if (c < len) out[c] = make_double2((double)sc[c], (double)ss[c]);
   }
   if (blockIdx.x == 0) {
     // sum of moments of this chunk (surface term), FP64
@@ -204,12 +201,25 @@ __global__ void k_sk_reduce(KParams p) {
     T2 o;
     o.x = (T)(e * a);
     o.y = (T)(e * b);
-    ((T2*)p.eS)[kk] = o;
+    ((T2*)p.eS)[p.rowpos[kk]] = o;
   }
   if (blockIdx.x == 0 && threadIdx.x < 3) {
     double s = 0;
     for (int c = 0; c < p.nchunk; c++) s += p.musum_part[3 * c + threadIdx.x];
     p.musum[threadIdx.x] = s;
+  }
+}
+
+// ---------------------------------------------------------------- scatter
+
+template <typename T>
+__device__ __forceinline__ void kahan_add(T& s, T& c, T v) {
+  if constexpr (std::is_same<T, float>::value) {
+    const float y = v - c, t = s + y;
+    c = (t - s) - y;
+    s = t;
+  } else {
+    s += v;
   }
 }
 
@@ -219,44 +229,72 @@ __global__ void __launch_bounds__(NT) k_kscatter(KParams p) {
   using T4 = typename V4<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int K1 = p.kc + 1;
-  T2* tab = (T2*)smem_raw;  // [3 * K1][NT]
+  T2* tab = (T2*)smem_raw;                 // x phase table [K1][NT]
+  T2* es_s = tab + K1 * NT;                // e*S of the chunk [kKChunk]
+  KSeg* seg_s = (KSeg*)(es_s + kKChunk);   // segments of the chunk [kKChunk / 4]
   const int tid = threadIdx.x;
   const int k = blockIdx.x * NT + tid;
   const bool active = k < p.n;
   const int kk = active ? k : p.n - 1;
-  for (int ax = 0; ax < 3; ax++) {
-    unsigned sf;
-    double xb;
-    particle_coord<T>(p.s, kk, ax, sf, xb);
-    fill_table<T>(tab + ax * K1 * NT + tid, NT, p.kc, sf, xb, p.two_pi);
-  }
+  unsigned sx, sy, sz;
+  double xbx, xby, xbz;
+  particle_coord<T>(p.s, kk, 0, sx, xbx);
+  particle_coord<T>(p.s, kk, 1, sy, xby);
+  particle_coord<T>(p.s, kk, 2, sz, xbz);
+  fill_table<T>(tab + tid, NT, p.kc, sx, xbx, p.two_pi);
   const T4 mu = ((const T4*)p.s.mu)[kk];
-  const T2* eS = (const T2*)p.eS;
   const T2 E = tab[NT + tid];
+  const T2 EY = phase_direct<T>(1, sy, xby, p.two_pi);
   T b[3] = {0, 0, 0}, f[3] = {0, 0, 0}, cb[3] = {0, 0, 0}, cf[3] = {0, 0, 0};
-  for (int s0 = 0; s0 < p.nseg; s0 += 8) {
-    T bb[3] = {0, 0, 0}, fb[3] = {0, 0, 0};
-    const int s1 = min(p.nseg, s0 + 8);
-    for (int s = s0; s < s1; s++) {
-      const KSeg sg = p.seg[s];
-      const int ko = p.koff[s];
-      const int ax0 = sg.nx0 < 0 ? -sg.nx0 : sg.nx0, ay = sg.ny < 0 ? -sg.ny : sg.ny;
-      T2 X = tab[ax0 * NT + tid], Y = tab[(K1 + ay) * NT + tid], Z = tab[(2 * K1 + sg.nz) * NT + tid];
+  T bb[3] = {0, 0, 0}, fb[3] = {0, 0, 0};
+  int cur_ny = 1 << 30, cur_nz = 1 << 30, anchor = 0, nflush = 0;
+  T2 Y = {0, 0}, Z = {0, 0};
+  T yzr = 0, yzi = 0;
+  for (int c = 0; c < p.nchk; c++) {
+    const int2 c0 = p.chunks[c], c1 = p.chunks[c + 1];
+    const int nsg = c1.x - c0.x, nkc = c1.y - c0.y;
+    __syncthreads();
+    for (int i = tid; i < nkc; i += NT) es_s[i] = ((const T2*)p.eS)[c0.y + i];
+    for (int i = tid; i < nsg; i += NT) seg_s[i] = p.rseg[c0.x + i];
+    __syncthreads();
+    int ko = 0;
+    for (int s = 0; s < nsg; s++) {
+      const KSeg sg = seg_s[s];
+      if (sg.nz != cur_nz) {
+        Z = phase_direct<T>(sg.nz, sz, xbz, p.two_pi);
+        Y = phase_direct<T>(sg.ny, sy, xby, p.two_pi);
+        cur_nz = sg.nz;
+        cur_ny = anchor = sg.ny;
+        cmul<T>(Y.x, Y.y, Z.x, Z.y, yzr, yzi);
+      } else if (sg.ny != cur_ny) {
+        if (sg.ny - anchor >= 8) {
+          Y = phase_direct<T>(sg.ny, sy, xby, p.two_pi);
+          anchor = sg.ny;
+        } else {
+          T nr, ni;
+          cmul<T>(Y.x, Y.y, EY.x, EY.y, nr, ni);
+          Y.x = nr;
+          Y.y = ni;
+        }
+        cur_ny = sg.ny;
+        cmul<T>(Y.x, Y.y, Z.x, Z.y, yzr, yzi);
+      }
+      const int ax0 = sg.nx0 < 0 ? -sg.nx0 : sg.nx0;
+      T2 X = tab[ax0 * NT + tid];
       if (sg.nx0 < 0) X.y = -X.y;
-      if (sg.ny < 0) Y.y = -Y.y;
-      T yr, yi, pr, pi;
-      cmul<T>(Y.x, Y.y, Z.x, Z.y, yr, yi);
-      cmul<T>(X.x, X.y, yr, yi, pr, pi);
+      T pr, pi;
+      cmul<T>(X.x, X.y, yzr, yzi, pr, pi);
       T nxf = (T)sg.nx0;
       T w = 0;
       if constexpr (FULL) w = nxf * mu.x + (T)sg.ny * mu.y + (T)sg.nz * mu.z;
       T gx = 0, gs = 0, hx = 0, hs = 0;
+      const T2* es_seg = es_s + ko;
 #pragma unroll
-      for (int c = 0; c < kSegMax; c += 4) {
-        if (c >= sg.len) break;
+      for (int q = 0; q < kSegMax; q += 4) {
+        if (q >= sg.len) break;
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-          const T2 es = eS[ko + c + u];
+          const T2 es = es_seg[q + u];
           const T g = es.x * pr + es.y * pi;
           gx += g * nxf;
           gs += g;
@@ -272,6 +310,7 @@ __global__ void __launch_bounds__(NT) k_kscatter(KParams p) {
           nxf += (T)1;
         }
       }
+      ko += sg.len;
       bb[0] += gx;
       bb[1] += gs * (T)sg.ny;
       bb[2] += gs * (T)sg.nz;
@@ -280,35 +319,35 @@ __global__ void __launch_bounds__(NT) k_kscatter(KParams p) {
         fb[1] += hs * (T)sg.ny;
         fb[2] += hs * (T)sg.nz;
       }
-    }
+      if (++nflush == 8) {
+        nflush = 0;
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-      if constexpr (std::is_same<T, float>::value) {
-        float y = bb[a] - cb[a], t = b[a] + y;
-        cb[a] = (t - b[a]) - y;
-        b[a] = t;
-        if constexpr (FULL) {
-          y = fb[a] - cf[a];
-          t = f[a] + y;
-          cf[a] = (t - f[a]) - y;
-          f[a] = t;
+        for (int a = 0; a < 3; a++) {
+          kahan_add<T>(b[a], cb[a], bb[a]);
+          bb[a] = 0;
+          if constexpr (FULL) {
+            kahan_add<T>(f[a], cf[a], fb[a]);
+            fb[a] = 0;
+          }
         }
-      } else {
-        b[a] += bb[a];
-        if constexpr (FULL) f[a] += fb[a];
       }
     }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    kahan_add<T>(b[a], cb[a], bb[a]);
+    if constexpr (FULL) kahan_add<T>(f[a], cf[a], fb[a]);
   }
   if (active) {
     T* B = (T*)p.B;
     const int n = p.n;
     const T cfl = (T)p.cflux, cfo = (T)p.cforce;
 #pragma unroll
-    for (int a = 0; a < 3; a++) B[a * n + k] = -cfl * b[a];
+    for (int a = 0; a < 3; a++) B[a * n + k] = -cfl * (b[a] - cb[a]);
     if constexpr (FULL) {
       T* F = (T*)p.F;
 #pragma unroll
-      for (int a = 0; a < 3; a++) F[a * n + k] = cfo * f[a];
+      for (int a = 0; a < 3; a++) F[a * n + k] = cfo * (f[a] - cf[a]);
     }
   }
 }
@@ -321,13 +360,15 @@ size_t ksf_smem(int kc, bool fp64) {
 static int scatter_threads(int kc, bool fp64) {
   const size_t e = fp64 ? 16 : 8;
   for (int nt : {128, 64, 32})
-    if ((size_t)3 * (kc + 1) * nt * e <= 200 * 1024) return nt;
+    if ((size_t)(kc + 1) * nt * e + (size_t)kKChunk * e + (size_t)kKChunk / 4 * sizeof(KSeg) <= 200 * 1024)
+      return nt;
   return 0;
 }
 
 size_t kscatter_smem(int kc, bool fp64) {
   const int nt = scatter_threads(kc, fp64);
-  return nt ? (size_t)3 * (kc + 1) * nt * (fp64 ? 16 : 8) : 0;
+  const size_t e = fp64 ? 16 : 8;
+  return nt ? (size_t)(kc + 1) * nt * e + (size_t)kKChunk * e + (size_t)kKChunk / 4 * sizeof(KSeg) : 0;
 }
 
 template <typename T, int NT>

@@ -16,4 +16,7 @@ struct KSeg {
   int nx0, ny, nz, len;
 };
 
+// k vectors per shared-memory chunk of the k-space scatter.
+constexpr int kKChunk = 1024;
+
 }  // namespace md
