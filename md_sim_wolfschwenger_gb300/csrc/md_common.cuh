@@ -88,6 +88,7 @@ struct KParams {
   double* musum;         // [3]
   void* eS;              // [nk] T2: e(k) * (Sc, Ss)
   double2* S;            // [nk] full structure factor (debug / FP64)
+  void* tab;             // [n][3][kc + 1] T2 phase tables of the sorted particles
   double cflux, cforce;  // 4 pi, 8 pi^2 (box units)
   SortedView s;
   void* B;   // [3][n] T sorted

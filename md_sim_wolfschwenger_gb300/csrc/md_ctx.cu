@@ -100,6 +100,8 @@ struct md_ctx {
   double* musum_part = nullptr;
   void* eS = nullptr;
   double2* Sfull = nullptr;
+  void* ptab = nullptr;  // phase tables [3][kc+1][n]
+  size_t ptab_cap = 0;
   size_t ksize_cap = 0, spart_cap = 0;
   int musum_cap = 0;
   // profiling: events between the kernel segments of a step
@@ -240,6 +242,7 @@ static KParams k_params(md_ctx* c, void* B, void* F) {
   p.musum = c->sc->musum;
   p.eS = c->eS;
   p.S = c->Sfull;
+  p.tab = c->ptab;
   p.cflux = 4.0 * c->cfg.my_pi;
   p.cforce = 8.0 * c->cfg.my_pi * c->cfg.my_pi;
   p.s = sorted_view(c);
@@ -320,6 +323,7 @@ static int issue_interactions(md_ctx* c) {
   l += launch_cells(c->stream, (int)c->n, c->pos, c->mm, c->magMom_u, c->rMag_u, c->L, c->grid, c->cellOf, c->count,
                     c->tmp, s, fp64(c));
   cudaMemsetAsync(&c->sc->pairs, 0, sizeof(unsigned long long), c->stream);
+  l += launch_phase_tables(c->stream, k_params(c, nullptr, nullptr), fp64(c));
   mark(c, MD_SEG_REAL_FULL);
   l += launch_real(c->stream, real_params(c, c->Br, c->Fr, c->ov), true, fp64(c));
   mark(c, MD_SEG_KSF_FULL);
@@ -721,6 +725,14 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
     int st;
     if ((st = dalloc(c, &c->Spart, sizeof(double2) * sp))) return st;
     c->spart_cap = sp;
+  }
+  const size_t pt = (size_t)3 * (c->kc + 1) * c->n * 2 * tsz(c);
+  if (pt > c->ptab_cap) {
+    dfree(c, c->ptab);
+    c->ptab = nullptr;
+    int st;
+    if ((st = dalloc(c, &c->ptab, pt))) return st;
+    c->ptab_cap = pt;
   }
   if (c->nchunk > c->musum_cap) {
     dfree(c, c->musum_part);

@@ -19,6 +19,9 @@ int launch_real(cudaStream_t st, const RealParams& p, bool full, bool fp64);
 // ev (optional): two events recorded after the structure factor and after
 // the reduction.
 int launch_kspace(cudaStream_t st, const KParams& p, bool full, bool fp64, cudaEvent_t* ev = nullptr);
+// Per-particle phase tables (once per step; positions are frozen across the
+// two Heun stages).
+int launch_phase_tables(cudaStream_t st, const KParams& p, bool fp64);
 // FP32 FMA-chain calibration: returns FLOPs issued by one launch.
 double launch_fma_calibration(cudaStream_t st, float* out, int blocks, int threads);
 size_t kscatter_smem(int kc, bool fp64);

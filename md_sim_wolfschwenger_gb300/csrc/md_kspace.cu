@@ -9,23 +9,26 @@
 // this code sums half of the plane (ny > 0, or ny = 0 and nx > 0) with the
 // full e(n).  The self and surface terms are added in the integrator.
 //
-// k vectors are stored as row segments (fixed ny, nz; up to 16 consecutive
-// nx, padded to a multiple of 4 with e = 0).  Within a segment the phase is
-// advanced by one complex multiply per k, starting from a directly evaluated
-// phase (at most 16 recurrence steps).  Direct phases: on the mixed path the
-// argument n x / L is reduced exactly in 32-bit fixed point before
-// sincospif; the FP64 path uses sincos(2 my_pi n x / L) like the reference.
+// Phase tables (k_phase_tables, once per step -- positions are frozen across
+// the two Heun stages): X(n) = exp(2 pi i n x / L) per particle and axis,
+// n = 0..kc, evaluated directly for n < 4 and multiples of 4, otherwise as one
+// product of two direct entries.  Direct phases: on the mixed path n x / L is
+// reduced exactly in 32-bit fixed point before sincospif; the FP64 path uses
+// sincos(2 my_pi n x / L) like the reference.  Layout [3][kc+1][n].
+//
+// k vectors are row segments (fixed ny, nz; up to 16 consecutive nx, padded
+// to a multiple of 4 with e = 0).  Within a segment the phase is advanced by
+// one complex multiply per k from a table entry (<= 15 recurrence steps).
 //
 // Structure factor (k_sk): threads = segments (sorted by length so warps are
-// uniform), particles staged through shared-memory tiles of 64 with their
-// per-axis phase tables; FP32 sums over a chunk of <= 512 particles, FP64
-// across chunks (k_sk_reduce), which also applies e(n) and writes e*S in row
-// order for the scatter.
-// Scatter (k_kscatter): threads = particles; the block walks the k rows in
-// order, staging e*S and the segments chunk by chunk in shared memory; the
-// x phase comes from a per-thread table, y and z phases per row (direct
-// every 8th row, otherwise one multiply).  FP32 per segment, blocks of 8
-// segments added with Kahan compensation (mixed path).
+// uniform), particles staged through shared-memory tiles of 64; FP32 sums over
+// a chunk of <= 512 particles, FP64 across chunks (k_sk_reduce), which also
+// applies e(n) and writes e*S in row order for the scatter.
+// Scatter (k_kscatter): threads = (particle, partition); the k rows are split
+// into chunks staged in shared memory and dealt round-robin to 4 partitions
+// of threads that share the particle's tables; FP32 per segment, blocks of 8
+// segments added with Kahan compensation (mixed path); the partitions are
+// summed in a fixed order.
 //
 // Roofline: FP32 issue bound.  Algorithmic FLOPs per (k, particle): 11 for
 // the structure factor, 12 for the field scatter, 21 for field + force.
@@ -58,24 +61,6 @@ __device__ __forceinline__ typename V2<T>::t phase_direct(int nn, unsigned sfix,
   return v;
 }
 
-// Table of exp(2 pi i n x) for n = 0..kc at out[n * stride]: direct for
-// n < 4 and multiples of 4, otherwise the product of two direct entries.
-template <typename T>
-__device__ __forceinline__ void fill_table(typename V2<T>::t* out, int stride, int kc, unsigned sfix, double xb,
-                                           double two_pi) {
-  using T2 = typename V2<T>::t;
-  for (int nn = 0; nn <= kc; nn++) {
-    T2 v;
-    if (nn < 4 || (nn & 3) == 0) {
-      v = phase_direct<T>(nn, sfix, xb, two_pi);
-    } else {
-      const T2 a = out[(nn & ~3) * stride], b = out[(nn & 3) * stride];
-      cmul<T>(a.x, a.y, b.x, b.y, v.x, v.y);
-    }
-    out[nn * stride] = v;
-  }
-}
-
 template <typename T>
 __device__ __forceinline__ void particle_coord(const SortedView& s, int k, int ax, unsigned& sfix, double& xb) {
   if constexpr (std::is_same<T, float>::value) {
@@ -89,16 +74,50 @@ __device__ __forceinline__ void particle_coord(const SortedView& s, int k, int a
   }
 }
 
+// ------------------------------------------------------------ phase tables
+
+template <typename T>
+__global__ void k_phase_tables(KParams p) {
+  using T2 = typename V2<T>::t;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * p.n) return;
+  const int ax = t / p.n, k = t - ax * p.n;
+  unsigned sf;
+  double xb;
+  particle_coord<T>(p.s, k, ax, sf, xb);
+  T2* tab = (T2*)p.tab;
+  const int K1 = p.kc + 1;
+  const size_t stride = (size_t)p.n;
+  T2* out = tab + (size_t)ax * K1 * stride + k;
+  T2 d[4];
+  for (int nn = 0; nn <= p.kc; nn++) {
+    T2 v;
+    if (nn < 4) {
+      v = phase_direct<T>(nn, sf, xb, p.two_pi);
+      d[nn] = v;
+    } else if ((nn & 3) == 0) {
+      v = phase_direct<T>(nn, sf, xb, p.two_pi);
+      d[0] = v;  // anchor of this block of 4
+    } else {
+      const T2 a = d[0];
+      const T2 b = (nn & 3) == 1 ? d[1] : ((nn & 3) == 2 ? d[2] : d[3]);
+      cmul<T>(a.x, a.y, b.x, b.y, v.x, v.y);
+    }
+    out[(size_t)nn * stride] = v;
+  }
+}
+
 // ------------------------------------------------------ structure factor
 
 template <typename T>
-__global__ void __launch_bounds__(kSkThreads, 2) k_sk(KParams p) {
+__global__ void __launch_bounds__(kSkThreads, 3) k_sk(KParams p) {
   using T2 = typename V2<T>::t;
   using T4 = typename V4<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int K1 = p.kc + 1;
+  const int K1 = p.kc + 1, E3 = 3 * K1;
   T2* tab = (T2*)smem_raw;                   // [kSkTile][3][K1]
-  T4* mus = (T4*)(tab + kSkTile * 3 * K1);   // [kSkTile]
+  T4* mus = (T4*)(tab + kSkTile * E3);       // [kSkTile]
+  const T2* gtab = (const T2*)p.tab;
   const int tid = threadIdx.x;
   const int sidx = blockIdx.x * kSkThreads + tid;
   const int chunk = blockIdx.y;
@@ -116,18 +135,15 @@ __global__ void __launch_bounds__(kSkThreads, 2) k_sk(KParams p) {
   for (int t0 = p0; t0 < p1; t0 += kSkTile) {
     const int tn = min(kSkTile, p1 - t0);
     __syncthreads();
-    for (int job = tid; job < tn * 3; job += kSkThreads) {
-      const int pp = job / 3, ax = job - 3 * pp;
-      unsigned sf;
-      double xb;
-      particle_coord<T>(p.s, t0 + pp, ax, sf, xb);
-      fill_table<T>(tab + (pp * 3 + ax) * K1, 1, p.kc, sf, xb, p.two_pi);
+    for (int i = tid; i < tn * E3; i += kSkThreads) {
+      const int e = i / tn, pp = i - e * tn;
+      tab[pp * E3 + e] = gtab[(size_t)e * p.n + t0 + pp];
     }
     for (int pp = tid; pp < tn; pp += kSkThreads) mus[pp] = ((const T4*)p.s.mu)[t0 + pp];
     __syncthreads();
     if (!has) continue;
     for (int pp = 0; pp < tn; pp++) {
-      const T2* tb = tab + pp * 3 * K1;
+      const T2* tb = tab + pp * E3;
       T2 X = tb[ax0], Y = tb[K1 + ay];
       const T2 Z = tb[2 * K1 + sg.nz], E = tb[1];
       if (sg.nx0 < 0) X.y = -X.y;
@@ -185,16 +201,26 @@ __global__ void __launch_bounds__(kSkThreads, 2) k_sk(KParams p) {
   }
 }
 
+// Sum of the chunk partials: block = 32 k's x 8 chunk groups, fixed order.
 template <typename T>
-__global__ void k_sk_reduce(KParams p) {
+__global__ void __launch_bounds__(256) k_sk_reduce(KParams p) {
   using T2 = typename V2<T>::t;
-  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
-  if (kk < p.nk) {
-    double a = 0, b = 0;
-    for (int c = 0; c < p.nchunk; c++) {
+  __shared__ double2 red[8][32];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int kk = blockIdx.x * 32 + tx;
+  double a = 0, b = 0;
+  if (kk < p.nk)
+    for (int c = ty; c < p.nchunk; c += 8) {
       const double2 v = p.Spart[(size_t)c * p.nk + kk];
       a += v.x;
       b += v.y;
+    }
+  red[ty][tx] = make_double2(a, b);
+  __syncthreads();
+  if (ty == 0 && kk < p.nk) {
+    for (int g = 1; g < 8; g++) {
+      a += red[g][tx].x;
+      b += red[g][tx].y;
     }
     p.S[kk] = make_double2(a, b);
     const double e = p.ek[kk];
@@ -223,64 +249,64 @@ __device__ __forceinline__ void kahan_add(T& s, T& c, T v) {
   }
 }
 
-template <typename T, int NT, bool FULL>
-__global__ void __launch_bounds__(NT) k_kscatter(KParams p) {
+template <typename T, int NP, bool FULL>
+__global__ void __launch_bounds__(NP * kScatterParts) k_kscatter(KParams p) {
   using T2 = typename V2<T>::t;
   using T4 = typename V4<T>::t;
+  constexpr int NT = NP * kScatterParts;
+  constexpr int kSegChunk = kKChunk / 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int K1 = p.kc + 1;
-  T2* tab = (T2*)smem_raw;                 // x phase table [K1][NT]
-  T2* es_s = tab + K1 * NT;                // e*S of the chunk [kKChunk]
-  KSeg* seg_s = (KSeg*)(es_s + kKChunk);   // segments of the chunk [kKChunk / 4]
+  const int K1 = p.kc + 1, E3 = 3 * K1;
+  T2* tab = (T2*)smem_raw;                       // [3 * K1][NP]
+  T2* es_all = tab + E3 * NP;                    // [parts][kKChunk]
+  KSeg* seg_all = (KSeg*)(es_all + kScatterParts * kKChunk);  // [parts][kSegChunk]
+  T* red = (T*)es_all;                           // [parts][6][NP], after the loop
   const int tid = threadIdx.x;
-  const int k = blockIdx.x * NT + tid;
+  const int part = tid / NP, lp = tid - part * NP;
+  const int base = blockIdx.x * NP;
+  const int k = base + lp;
   const bool active = k < p.n;
   const int kk = active ? k : p.n - 1;
-  unsigned sx, sy, sz;
-  double xbx, xby, xbz;
-  particle_coord<T>(p.s, kk, 0, sx, xbx);
-  particle_coord<T>(p.s, kk, 1, sy, xby);
-  particle_coord<T>(p.s, kk, 2, sz, xbz);
-  fill_table<T>(tab + tid, NT, p.kc, sx, xbx, p.two_pi);
+  const T2* gtab = (const T2*)p.tab;
+  for (int i = tid; i < E3 * NP; i += NT) {
+    const int e = i / NP, q = i - e * NP;
+    tab[i] = gtab[(size_t)e * p.n + min(base + q, p.n - 1)];
+  }
   const T4 mu = ((const T4*)p.s.mu)[kk];
-  const T2 E = tab[NT + tid];
-  const T2 EY = phase_direct<T>(1, sy, xby, p.two_pi);
+  T2* es_s = es_all + part * kKChunk;
+  KSeg* seg_s = seg_all + part * kSegChunk;
+  __syncthreads();
+  const T2 E = tab[1 * NP + lp];
   T b[3] = {0, 0, 0}, f[3] = {0, 0, 0}, cb[3] = {0, 0, 0}, cf[3] = {0, 0, 0};
   T bb[3] = {0, 0, 0}, fb[3] = {0, 0, 0};
-  int cur_ny = 1 << 30, cur_nz = 1 << 30, anchor = 0, nflush = 0;
-  T2 Y = {0, 0}, Z = {0, 0};
+  int cur_ny = 1 << 30, cur_nz = 1 << 30, nflush = 0;
   T yzr = 0, yzi = 0;
-  for (int c = 0; c < p.nchk; c++) {
-    const int2 c0 = p.chunks[c], c1 = p.chunks[c + 1];
-    const int nsg = c1.x - c0.x, nkc = c1.y - c0.y;
+  const int rounds = (p.nchk + kScatterParts - 1) / kScatterParts;
+  for (int r = 0; r < rounds; r++) {
+    const int c = r * kScatterParts + part;
+    const bool mine = c < p.nchk;
+    int nsg = 0;
     __syncthreads();
-    for (int i = tid; i < nkc; i += NT) es_s[i] = ((const T2*)p.eS)[c0.y + i];
-    for (int i = tid; i < nsg; i += NT) seg_s[i] = p.rseg[c0.x + i];
+    if (mine) {
+      const int2 c0 = p.chunks[c], c1 = p.chunks[c + 1];
+      nsg = c1.x - c0.x;
+      const int nkc = c1.y - c0.y;
+      for (int i = lp; i < nkc; i += NP) es_s[i] = ((const T2*)p.eS)[c0.y + i];
+      for (int i = lp; i < nsg; i += NP) seg_s[i] = p.rseg[c0.x + i];
+    }
     __syncthreads();
     int ko = 0;
     for (int s = 0; s < nsg; s++) {
       const KSeg sg = seg_s[s];
-      if (sg.nz != cur_nz) {
-        Z = phase_direct<T>(sg.nz, sz, xbz, p.two_pi);
-        Y = phase_direct<T>(sg.ny, sy, xby, p.two_pi);
-        cur_nz = sg.nz;
-        cur_ny = anchor = sg.ny;
+      if (sg.nz != cur_nz || sg.ny != cur_ny) {
+        T2 Y = tab[(K1 + (sg.ny < 0 ? -sg.ny : sg.ny)) * NP + lp];
+        const T2 Z = tab[(2 * K1 + sg.nz) * NP + lp];
+        if (sg.ny < 0) Y.y = -Y.y;
         cmul<T>(Y.x, Y.y, Z.x, Z.y, yzr, yzi);
-      } else if (sg.ny != cur_ny) {
-        if (sg.ny - anchor >= 8) {
-          Y = phase_direct<T>(sg.ny, sy, xby, p.two_pi);
-          anchor = sg.ny;
-        } else {
-          T nr, ni;
-          cmul<T>(Y.x, Y.y, EY.x, EY.y, nr, ni);
-          Y.x = nr;
-          Y.y = ni;
-        }
         cur_ny = sg.ny;
-        cmul<T>(Y.x, Y.y, Z.x, Z.y, yzr, yzi);
+        cur_nz = sg.nz;
       }
-      const int ax0 = sg.nx0 < 0 ? -sg.nx0 : sg.nx0;
-      T2 X = tab[ax0 * NT + tid];
+      T2 X = tab[(sg.nx0 < 0 ? -sg.nx0 : sg.nx0) * NP + lp];
       if (sg.nx0 < 0) X.y = -X.y;
       T pr, pi;
       cmul<T>(X.x, X.y, yzr, yzi, pr, pi);
@@ -338,16 +364,31 @@ __global__ void __launch_bounds__(NT) k_kscatter(KParams p) {
     kahan_add<T>(b[a], cb[a], bb[a]);
     if constexpr (FULL) kahan_add<T>(f[a], cf[a], fb[a]);
   }
-  if (active) {
+  __syncthreads();  // staging buffers are reused for the partition reduction
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    red[(part * 6 + a) * NP + lp] = b[a] - cb[a];
+    if constexpr (FULL) red[(part * 6 + 3 + a) * NP + lp] = f[a] - cf[a];
+  }
+  __syncthreads();
+  if (part == 0 && active) {
     T* B = (T*)p.B;
     const int n = p.n;
     const T cfl = (T)p.cflux, cfo = (T)p.cforce;
 #pragma unroll
-    for (int a = 0; a < 3; a++) B[a * n + k] = -cfl * (b[a] - cb[a]);
+    for (int a = 0; a < 3; a++) {
+      T s = 0;
+      for (int q = 0; q < kScatterParts; q++) s += red[(q * 6 + a) * NP + lp];
+      B[a * n + k] = -cfl * s;
+    }
     if constexpr (FULL) {
       T* F = (T*)p.F;
 #pragma unroll
-      for (int a = 0; a < 3; a++) F[a * n + k] = cfo * (f[a] - cf[a]);
+      for (int a = 0; a < 3; a++) {
+        T s = 0;
+        for (int q = 0; q < kScatterParts; q++) s += red[(q * 6 + 3 + a) * NP + lp];
+        F[a * n + k] = cfo * s;
+      }
     }
   }
 }
@@ -357,29 +398,32 @@ size_t ksf_smem(int kc, bool fp64) {
   return (size_t)kSkTile * 3 * (kc + 1) * e + (size_t)kSkTile * (fp64 ? 32 : 16);
 }
 
-static int scatter_threads(int kc, bool fp64) {
+static size_t scatter_bytes(int kc, bool fp64, int np) {
   const size_t e = fp64 ? 16 : 8;
-  for (int nt : {128, 64, 32})
-    if ((size_t)(kc + 1) * nt * e + (size_t)kKChunk * e + (size_t)kKChunk / 4 * sizeof(KSeg) <= 200 * 1024)
-      return nt;
+  return (size_t)3 * (kc + 1) * np * e + (size_t)kScatterParts * kKChunk * e +
+         (size_t)kScatterParts * (kKChunk / 4) * sizeof(KSeg);
+}
+
+static int scatter_particles(int kc, bool fp64) {
+  for (int np : {64, 32})
+    if (scatter_bytes(kc, fp64, np) <= 200 * 1024) return np;
   return 0;
 }
 
 size_t kscatter_smem(int kc, bool fp64) {
-  const int nt = scatter_threads(kc, fp64);
-  const size_t e = fp64 ? 16 : 8;
-  return nt ? (size_t)(kc + 1) * nt * e + (size_t)kKChunk * e + (size_t)kKChunk / 4 * sizeof(KSeg) : 0;
+  const int np = scatter_particles(kc, fp64);
+  return np ? scatter_bytes(kc, fp64, np) : 0;
 }
 
-template <typename T, int NT>
+template <typename T, int NP>
 static void scatter_launch(cudaStream_t st, const KParams& p, bool full, size_t smem) {
-  dim3 grid((p.n + NT - 1) / NT);
+  dim3 grid((p.n + NP - 1) / NP);
   if (full) {
-    cudaFuncSetAttribute(k_kscatter<T, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_kscatter<T, NT, true><<<grid, NT, smem, st>>>(p);
+    cudaFuncSetAttribute(k_kscatter<T, NP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_kscatter<T, NP, true><<<grid, NP * kScatterParts, smem, st>>>(p);
   } else {
-    cudaFuncSetAttribute(k_kscatter<T, NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_kscatter<T, NT, false><<<grid, NT, smem, st>>>(p);
+    cudaFuncSetAttribute(k_kscatter<T, NP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_kscatter<T, NP, false><<<grid, NP * kScatterParts, smem, st>>>(p);
   }
 }
 
@@ -391,13 +435,10 @@ static int kspace_t(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* e
   dim3 g1((p.nseg + kSkThreads - 1) / kSkThreads, p.nchunk);
   k_sk<T><<<g1, kSkThreads, sm1, st>>>(p);
   if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
-  k_sk_reduce<T><<<(p.nk + 255) / 256, 256, 0, st>>>(p);
+  k_sk_reduce<T><<<(p.nk + 31) / 32, 256, 0, st>>>(p);
   if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
-  const int nt = scatter_threads(p.kc, fp64);
   const size_t sm2 = kscatter_smem(p.kc, fp64);
-  if (nt == 128)
-    scatter_launch<T, 128>(st, p, full, sm2);
-  else if (nt == 64)
+  if (scatter_particles(p.kc, fp64) == 64)
     scatter_launch<T, 64>(st, p, full, sm2);
   else
     scatter_launch<T, 32>(st, p, full, sm2);
@@ -406,6 +447,15 @@ static int kspace_t(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* e
 
 int launch_kspace(cudaStream_t st, const KParams& p, bool full, bool fp64, cudaEvent_t* ev) {
   return fp64 ? kspace_t<double>(st, p, full, ev) : kspace_t<float>(st, p, full, ev);
+}
+
+int launch_phase_tables(cudaStream_t st, const KParams& p, bool fp64) {
+  const int nt = 3 * p.n;
+  if (fp64)
+    k_phase_tables<double><<<(nt + 255) / 256, 256, 0, st>>>(p);
+  else
+    k_phase_tables<float><<<(nt + 255) / 256, 256, 0, st>>>(p);
+  return 1;
 }
 
 // FP32 throughput calibration: 8 independent FMA chains per thread, 4096

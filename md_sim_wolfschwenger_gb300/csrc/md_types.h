@@ -17,6 +17,9 @@ struct KSeg {
 };
 
 // k vectors per shared-memory chunk of the k-space scatter.
-constexpr int kKChunk = 1024;
+constexpr int kKChunk = 512;
+// Thread partitions of the k-space scatter: each particle's k range is split
+// over this many threads (by chunk), reduced in a fixed order.
+constexpr int kScatterParts = 4;
 
 }  // namespace md
