@@ -252,6 +252,31 @@ int md_profile_read(md_ctx* ctx, double* ms);
  * FLOPs) from a register-resident FMA-chain kernel on all SMs. */
 int md_calibrate_fp32(double* tflops);
 
+/* ------------------------------------------- structure factor, no allocation */
+/* This entry point has no counterpart in the reference.  It exists for
+ * callers that cannot call cudaMalloc -- a host framework that owns all
+ * device memory through its own pool, a real-time loop that must not allocate
+ * after start-up, a process under a fixed device-memory budget.  It computes
+ * the Ewald structure factor S(n) = sum_j (n . mu_j) exp(2 pi i n . r_j / L)
+ * (FP64) with caller-owned device buffers and no allocation of its own: its
+ * scratch is one file-scope device array of md_noalloc_scratch_bytes()
+ * (about 2.6 MB) that every GPU loading the library holds until exit.
+ *   pos, mom: device pointers, N x 3 column-major FP64 (positions in m,
+ *             moment vectors in A m^2);  out5: device pointer with room for
+ *             nk x 5 doubles {nx, ny, nz, Sc, Ss}, the k vectors of the
+ *             reference's loops (nz = 0..kc, ny and nx = -kc..kc,
+ *             0 < |n|^2 <= kc^2, in that loop order); nk_out (host) gets nk.
+ *   stream:   cudaStream_t (NULL: the default stream); the call is
+ *             asynchronous on it.
+ * kc above MD_NOALLOC_MAX_KC is rejected with MD_ERR_INVALID.  The first
+ * call on a device looks up the array's device address (make it before any
+ * stream capture).  All calls share the array and it keeps the last call's
+ * contents, so calls whose work overlaps on the GPU race: serialise them. */
+#define MD_NOALLOC_MAX_KC 16
+size_t md_noalloc_scratch_bytes(void);
+int md_structure_factor_noalloc(const double* pos, const double* mom, int64_t n, double lBox, int64_t kc,
+                                double my_pi, double* out5, int64_t* nk_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -104,6 +104,8 @@ def lib():
         "md_profile": (C.c_int, [V, C.c_int]),
         "md_profile_read": (C.c_int, [V, P]),
         "md_calibrate_fp32": (C.c_int, [P]),
+        "md_noalloc_scratch_bytes": (C.c_size_t, []),
+        "md_structure_factor_noalloc": (C.c_int, [V, V, I64, C.c_double, I64, C.c_double, V, PI64, V]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
