@@ -29,9 +29,22 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = ("single large instance: N=32768 magnetite, log-normal core diameters (median 20 nm, sigma 0.2), "
-            "5 nm shell, volume fraction 0.10, static 20 mT, dt=1e-12 s, T=300 K, viscosity 1e-3 Pa s, "
-            "Philox thermal noise, Ewald at 1e-5 relative force error")
+COMMON = ("magnetite (Ms 4.8e5 A/m, K 1.1e4 J/m^3, damping 0.1), 5 nm shell, T=300 K, viscosity 1e-3 Pa s, "
+          "dt=1e-12 s, Philox thermal noise, Ewald at 1e-5 relative force error")
+WORKLOADS = {
+    # the headline: the single large instance of the benchmark suite
+    "large": dict(n=32768, median=1e-8, sigma=0.2, phi=0.10, B0=0.02,
+                  desc="single large instance: N=32768, log-normal core diameters (median 20 nm, sigma 0.2), "
+                       "volume fraction 0.10, static 20 mT, " + COMMON),
+    # the reference's own CPU-runnable case (monodisperse, N=512)
+    "small": dict(n=512, median=1e-8, sigma=0.0, phi=0.05, B0=0.01,
+                  desc="plain case: N=512 monodisperse 20/30 nm, volume fraction 0.05, static 10 mT, " + COMMON),
+    # stress instance
+    "stress": dict(n=131072, median=1.25e-8, sigma=0.25, phi=0.20, B0=0.03,
+                   desc="stress instance: N=131072, log-normal core diameters (median 25 nm, sigma 0.25), "
+                        "volume fraction 0.20, static 30 mT, " + COMMON),
+}
+W = dict(WORKLOADS["large"])
 
 # Algorithmic FLOPs (FMA = 2) per unit of work, counted from the formulas.
 FLOPS_PAIR_FULL = 113.0   # per unordered pair: erfc/exp terms, field on both, force, pressure
@@ -51,7 +64,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
-    p.add_argument("--n", type=int, default=32768)
+    p.add_argument("--workload", choices=sorted(WORKLOADS), default="large")
+    p.add_argument("--n", type=int, default=0, help="override the workload's particle count")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--autotune", type=int, default=0, help="candidate cutoffs timed (0: the cost-model choice, the same one the reference arm uses)")
     return p.parse_args()
@@ -60,7 +74,8 @@ def parse():
 def workload_config(n, seed):
     from md_sim_wolfschwenger_gb300 import MD_NOISE_PHILOX, MD_PREC_MIXED, Configuration
     cfg = Configuration.default()
-    cfg.set(SIZE_DIST=1, rMagMean=1e-8, sigmaLog=0.2, dShell=5e-9, volFrac=0.10, magFluxDens=0.02, tMag=1.0,
+    cfg.set(SIZE_DIST=1 if W["sigma"] > 0 else 0, rMagMean=W["median"], sigmaLog=W["sigma"], dShell=5e-9,
+            volFrac=W["phi"], magFluxDens=W["B0"], tMag=1.0,
             tRelax=0.0, deltaTinit=1e-12, satMag=4.8e5, anisEn=1.1e4, magDamp=0.1, temp=300.0, visOverride=1e-3,
             numbPartOverride=n, errTolEwald=1e-5, seed=seed, SOLVER=0, ENABLE_MOBILIZATION=1, ENABLE_THERM_FIELD=1,
             ENABLE_THERM_TORQUE=1, ENABLE_THERM_FORCE=1, ENABLE_COATING_POT=0, INIT_CONFIG_ROT=2,
@@ -71,9 +86,9 @@ def workload_config(n, seed):
 def workload_state(n, seed):
     from md_sim_wolfschwenger_gb300 import init
     rng = np.random.default_rng(1000 + seed)
-    rMag = init.lognormal_radii(n, 1e-8, 0.2, rng)
+    rMag = init.lognormal_radii(n, W["median"], W["sigma"], rng)
     rHydr = rMag + 5e-9
-    L = init.box_length(rHydr, 0.10)
+    L = init.box_length(rHydr, W["phi"])
     pos = init.rsa_positions(L, rHydr, rng)
     mm = init.uniform_directions(n, rng)
     ea = init.uniform_directions(n, rng)
@@ -83,7 +98,7 @@ def workload_state(n, seed):
 def oracle_ini(n, seed):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import ref_io
-    return ref_io.ini_dict(volFrac=0.10, magFluxDens=0.02, tMag=1.0, seed=seed)
+    return ref_io.ini_dict(volFrac=W["phi"], magFluxDens=W["B0"], tMag=1.0, seed=seed)
 
 
 # ------------------------------------------------------------ clocks
@@ -235,7 +250,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
             "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1e3 * total / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "n": n,
+            "data": "synthetic (seeded)", "config": {"workload": W["desc"], "n": n,
                                                      "ewald": {"alpha_L": a.value * lb.value,
                                                                "rc_over_L": r.value / lb.value, "kc": k.value}},
             "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
@@ -382,7 +397,7 @@ def run_ours(args):
                               "mixed: FP32 pair maths, phases, scatter and integrator; FP64 structure-factor "
                               "sums across chunks, self/surface terms, positions, reductions"),
                 "data": "synthetic (seeded log-normal radii, random sequential addition, uniform orientations)",
-                "config": {"workload": WORKLOAD, "n": n, "lBox_m": L, "replicas_per_gpu": 1,
+                "config": {"workload": W["desc"], "n": n, "lBox_m": L, "replicas_per_gpu": 1,
                            "parallelism": f"replicas x{ws}" if ws > 1 else "single instance",
                            "ewald": {"alpha_L": alpha * L, "rc_over_L": rc / L, "kc": kc,
                                      "pred_force_err_rel_contact": errF, "pred_torque_err_rel_contact": errT,
@@ -399,6 +414,11 @@ def run_ours(args):
 
 def main():
     args = parse()
+    W.clear()
+    W.update(WORKLOADS[args.workload])
+    if args.n > 0:
+        W["n"] = args.n
+    args.n = W["n"]
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -24,16 +24,23 @@ def box_length(rHydr, volFrac, my_pi=3.14159265359):
     return math.pow(float(vh.sum()) / volFrac, 1.0 / 3.0)
 
 
-def rsa_positions(L, rHydr, rng, max_tries=100000):
-    """(3, N) positions, non-overlapping hydrodynamic spheres."""
+def rsa_positions(L, rHydr, rng, max_tries=100000, largest_first=None):
+    """(3, N) positions, non-overlapping hydrodynamic spheres.  Particles are
+    placed in index order like the reference; with largest_first (default:
+    when the radii are not all equal) they are placed in order of decreasing
+    radius, which keeps dense polydisperse systems from jamming on the last
+    large particles.  Each particle keeps its own index either way."""
     rH = np.asarray(rHydr, dtype=np.float64)
     n = rH.size
+    if largest_first is None:
+        largest_first = bool(rH.max() > rH.min())
+    order = np.argsort(-rH, kind="stable") if largest_first else np.arange(n)
     cs = 2.0 * rH.max()
     nc = max(1, int(L // cs))
     cs = L / nc
     cells = {}
     pos = np.zeros((n, 3))
-    for i in range(n):
+    for i in order:
         for _ in range(max_tries):
             x = rng.uniform(-1.0, 1.0, 3) * (L / 2.0 - rH[i])
             c = np.minimum(((x + L / 2) / cs).astype(int), nc - 1)
