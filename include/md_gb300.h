@@ -225,6 +225,13 @@ int md_debug_launches(const md_ctx* ctx, int64_t* launches);
 /* In-range particle pairs (each unordered pair once) of the last full
  * real-space evaluation: the entries CompInteractVecs would list. */
 int md_debug_pairs(md_ctx* ctx, int64_t* pairs);
+/* Skin of the real-space neighbour list as a fraction of rc (default 0.02):
+ * the list holds pairs within rc (1 + skin) and is rebuilt on the device when
+ * a particle has moved more than skin rc / 2 since the last build. */
+int md_set_neighbor_skin(md_ctx* ctx, double skin_frac);
+/* Test hook: caps the neighbour-list capacity (entries); a list that does not
+ * fit makes the real-space kernels scan the cells directly for that step. */
+int md_debug_neighbor_capacity(md_ctx* ctx, int64_t cap, int64_t* used);
 
 /* ------------------------------------------------------ profiling */
 /* Kernel segments of one step, in launch order. */

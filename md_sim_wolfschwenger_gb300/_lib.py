@@ -101,6 +101,8 @@ def lib():
         "md_debug_structure_factor": (C.c_int, [V, PI64, P]),
         "md_debug_launches": (C.c_int, [V, PI64]),
         "md_debug_pairs": (C.c_int, [V, PI64]),
+        "md_set_neighbor_skin": (C.c_int, [V, C.c_double]),
+        "md_debug_neighbor_capacity": (C.c_int, [V, I64, PI64]),
         "md_profile": (C.c_int, [V, C.c_int]),
         "md_profile_read": (C.c_int, [V, P]),
         "md_calibrate_fp32": (C.c_int, [P]),

@@ -44,6 +44,15 @@ struct SortedView {
   int* cell_start;  // [ncell + 1]
 };
 
+// Per-step control words in device memory (written by the step's own kernels,
+// so one captured graph serves every step).
+struct StepFlags {
+  int rebuild;        // this step rebuilds the cell list and neighbour list
+  int overflow;       // the neighbour list did not fit: real space scans cells
+  int force;          // host request: rebuild on the next step
+  unsigned maxdisp;   // float bits of the largest displacement since the build (box units)
+};
+
 // ------------------------------------------------------- real space
 struct RealParams {
   int n;
@@ -63,9 +72,17 @@ struct RealParams {
   void* B;      // [3][n] T, sorted order
   void* F;      // [3][n] T, sorted order (FULL only)
   void* ov;     // [3][n] T, overlap displacement, box units (FULL only)
-  double* Ppart;  // [gridDim.x][3] pressure partials (FULL only)
+  double* Ppart;  // [n][3] per-particle pressure sums (FULL only)
   unsigned long long* npairs;  // in-range ordered pairs (FULL only, may be null)
   int* err;       // device error word
+  // Verlet neighbour list (sorted indices) with a skin: rebuilt when a
+  // particle has moved more than skin/2 since the last build.
+  double rl2;                 // (rc + skin)^2, box units
+  int* nbr;                   // [cap] neighbour indices
+  int* nbr_cnt;               // [n]
+  int* nbr_off;               // [n + 1]
+  long long nbr_cap;
+  const StepFlags* flags;     // rebuild / overflow
 };
 
 // --------------------------------------------------------- k space
@@ -130,6 +147,8 @@ struct IntParams {
   const double* time;        // device t (double) and step
   const long long* stepno;
   int* err;
+  const double* xbuild;      // [3][n] positions at the last neighbour-list build
+  StepFlags* flags;          // maxdisp is raised here
 };
 
 struct ObsParams {

@@ -38,6 +38,7 @@ struct DevScalars {
   int pad;
   double musum[3];
   unsigned long long pairs;
+  StepFlags flags;
 };
 
 }  // namespace
@@ -104,6 +105,12 @@ struct md_ctx {
   size_t ptab_cap = 0;
   size_t ksize_cap = 0, spart_cap = 0;
   int musum_cap = 0;
+  // Verlet list (sorted indices) within rc + skin
+  int *nbr = nullptr, *nbr_cnt = nullptr, *nbr_off = nullptr;
+  long long nbr_cap = 0;
+  double* xbuild = nullptr;
+  double skin_frac = 0.02;  // skin = skin_frac * rc
+  bool list_valid = false;  // a build for the current particles, grid and skin exists
   // profiling: events between the kernel segments of a step
   bool prof = false;
   cudaEvent_t ev[MD_NSEG + 1] = {};
@@ -218,6 +225,13 @@ static RealParams real_params(md_ctx* c, void* B, void* F, void* ov) {
   p.Ppart = c->Ppart;
   p.npairs = F ? &c->sc->pairs : nullptr;
   p.err = &c->sc->err;
+  const double rl = rcb * (1.0 + c->skin_frac);
+  p.rl2 = rl * rl;
+  p.nbr = c->nbr;
+  p.nbr_cnt = c->nbr_cnt;
+  p.nbr_off = c->nbr_off;
+  p.nbr_cap = c->nbr_cap;
+  p.flags = &c->sc->flags;
   return p;
 }
 
@@ -301,6 +315,8 @@ static IntParams int_params(md_ctx* c, double dt, const void* Br, const void* Bk
   p.musum = c->sc->musum;
   p.obs_part = c->obs_part;
   p.Ppart = c->Ppart;
+  p.xbuild = c->xbuild;
+  p.flags = &c->sc->flags;
   p.time = &c->sc->time;
   p.stepno = &c->sc->step;
   p.err = &c->sc->err;
@@ -320,15 +336,19 @@ static int issue_interactions(md_ctx* c) {
   int l = 0;
   SortedView s = sorted_view(c);
   mark(c, MD_SEG_CELLS);
+  const double half_skin = 0.5 * c->skin_frac * c->rc / c->L;
+  l += launch_step_begin(c->stream, &c->sc->flags, half_skin);
   l += launch_cells(c->stream, (int)c->n, c->pos, c->mm, c->magMom_u, c->rMag_u, c->L, c->grid, c->cellOf, c->count,
-                    c->tmp, s, fp64(c));
+                    c->tmp, s, fp64(c), c->xbuild, &c->sc->flags);
   cudaMemsetAsync(&c->sc->pairs, 0, sizeof(unsigned long long), c->stream);
+  l += launch_nbr(c->stream, real_params(c, nullptr, nullptr, nullptr), &c->sc->flags, fp64(c));
   l += launch_phase_tables(c->stream, k_params(c, nullptr, nullptr), fp64(c));
   mark(c, MD_SEG_REAL_FULL);
   l += launch_real(c->stream, real_params(c, c->Br, c->Fr, c->ov), true, fp64(c));
   mark(c, MD_SEG_KSF_FULL);
   l += launch_kspace(c->stream, k_params(c, c->Bk, c->Fk), true, fp64(c), c->prof ? &c->ev[MD_SEG_KRED_FULL] : nullptr);
   c->have_geometry = true;
+  c->list_valid = true;
   return l;
 }
 
@@ -360,6 +380,44 @@ static int issue_step(md_ctx* c, double dt) {
   return l;
 }
 
+// Asks the device to rebuild the cell order and the neighbour list at the
+// start of the next evaluation.
+static int force_rebuild(md_ctx* c) {
+  static const int one = 1;
+  CK(c, cudaMemcpyAsync(&c->sc->flags.force, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  return MD_OK;
+}
+
+static int alloc_nbr(md_ctx* c, long long cap) {
+  cap = std::min<long long>(cap, 0x7ffffffeLL);
+  if (cap <= c->nbr_cap) return MD_OK;
+  dfree(c, c->nbr);
+  c->nbr = nullptr;
+  c->nbr_cap = 0;
+  int st = dalloc(c, &c->nbr, 4 * (size_t)cap);
+  if (st) return st;
+  c->nbr_cap = cap;
+  invalidate_graph(c);
+  return MD_OK;
+}
+
+// After work on the stream: a neighbour list that did not fit was replaced by
+// the direct cell scan (results are correct); grow it for the next steps.
+static int check_overflow(md_ctx* c) {
+  StepFlags f;
+  CK(c, cudaMemcpyAsync(&f, &c->sc->flags, sizeof f, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (!f.overflow) return MD_OK;
+  int total = 0;
+  CK(c, cudaMemcpy(&total, c->nbr_off + c->n, sizeof(int), cudaMemcpyDeviceToHost));
+  const long long need = (total > 0 && total < 0x7fffffff) ? (long long)(total * 1.25) + 16LL * c->n : 2 * c->nbr_cap;
+  int st = alloc_nbr(c, need);
+  if (st) return st;
+  static const int zero = 0;
+  CK(c, cudaMemcpyAsync(&c->sc->flags.overflow, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  return force_rebuild(c);
+}
+
 static int read_err_word(md_ctx* c) {
   int e = 0;
   CK(c, cudaMemcpyAsync(&e, &c->sc->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -368,7 +426,7 @@ static int read_err_word(md_ctx* c) {
     CK(c, cudaMemsetAsync(&c->sc->err, 0, sizeof(int), c->stream));
     if (e & kErrNonFinite) return set_err(c, MD_ERR_NONFINITE, "non-finite position or orientation after the step");
   }
-  return MD_OK;
+  return check_overflow(c);
 }
 
 // ============================================================== C ABI
@@ -487,6 +545,9 @@ int md_ctx_create(const md_config* cfg, int64_t n, int precision, md_ctx** out) 
   for (auto p : t3)
     if ((st = dalloc(c, p, 3 * T * N))) return fail(st);
   if ((st = dalloc(c, &c->th, 9 * T * N))) return fail(st);
+  if ((st = dalloc(c, &c->nbr_cnt, 4 * N))) return fail(st);
+  if ((st = dalloc(c, &c->nbr_off, 4 * (N + 1)))) return fail(st);
+  if ((st = dalloc(c, &c->xbuild, 24 * N))) return fail(st);
   if ((st = dalloc(c, &c->Ppart, 24 * N))) return fail(st);
   if ((st = dalloc(c, &c->obs_part, 56 * (size_t)int_blocks((int)n)))) return fail(st);
   if ((st = dalloc(c, &c->sc, sizeof(DevScalars)))) return fail(st);
@@ -546,6 +607,7 @@ int md_set_particles(md_ctx* c, const double* rMag, const double* rHydr) {
   CK(c, cudaStreamSynchronize(c->stream));
   c->have_particles = true;
   c->have_ewald = false;
+  c->list_valid = false;
   c->cur_dt = -1;
   invalidate_graph(c);
   return MD_OK;
@@ -565,6 +627,7 @@ int md_set_box(md_ctx* c, double lBox) {
   for (int64_t i = 0; i < c->n; i++) rm[i] = c->props.rMag[i] / lBox;
   CK(c, cudaMemcpy(c->rMag_u, rm.data(), 8 * c->n, cudaMemcpyHostToDevice));
   c->have_ewald = false;
+  c->list_valid = false;
   invalidate_graph(c);
   return MD_OK;
 }
@@ -578,6 +641,12 @@ int md_state_upload(md_ctx* c, const double* pos, const double* mm, const double
   if (reset || !c->have_state) {
     CK(c, cudaMemcpyAsync(c->truePos, c->pos, B, cudaMemcpyDeviceToDevice, c->stream));
     CK(c, cudaMemcpyAsync(c->posRef, c->pos, B, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  if (c->list_valid) {
+    // same particles: rebuild on the next step only if they moved beyond the skin
+    launch_disp_check(c->stream, (int)c->n, c->pos, c->xbuild, c->L, &c->sc->flags);
+  } else if (int st = force_rebuild(c)) {
+    return st;
   }
   CK(c, cudaStreamSynchronize(c->stream));
   c->have_state = true;
@@ -673,6 +742,7 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
   c->alpha = alpha;
   c->rc = rc;
   c->kc = kc;
+  c->list_valid = false;
   const double ab = alpha * c->L;
   const double w = std::pow(c->cfg.my_pi / ab, 2.0);
   c->klist = mdh::build_klist((int)kc, w);
@@ -747,6 +817,15 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
   CK(c, cudaMemcpy(c->rseg, c->klist.rseg.data(), sizeof(KSeg) * nseg, cudaMemcpyHostToDevice));
   CK(c, cudaMemcpy(c->rowpos, c->klist.rowpos.data(), sizeof(int) * nk, cudaMemcpyHostToDevice));
   CK(c, cudaMemcpy(c->chunks, c->klist.chunks.data(), sizeof(int) * c->klist.chunks.size(), cudaMemcpyHostToDevice));
+  {
+    // neighbour-list capacity: uniform-density estimate + margin (grown on overflow)
+    const double rlb = rc / c->L * (1.0 + c->skin_frac);
+    double est = (double)c->n * (double)c->n * 4.0 / 3.0 * 3.141592653589793 * rlb * rlb * rlb;
+    est = std::min(est, (double)c->n * (double)(c->n - 1));
+    int st = alloc_nbr(c, (long long)(1.3 * est) + 64LL * c->n);
+    if (st) return st;
+  }
+  if (int st = force_rebuild(c)) return st;
   c->have_ewald = true;
   c->have_geometry = false;
   return MD_OK;
@@ -755,6 +834,7 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
 int md_compute_interactions(md_ctx* c, double* B, double* F, double* P3) {
   int st = check_ready(c, true);
   if (st) return st;
+  if ((st = force_rebuild(c))) return st;
   c->launches = issue_interactions(c);
   IntParams ip = int_params(c, 0.0, c->Br, c->Bk);
   c->launches += launch_combine(c->stream, ip, c->Bout, c->Fout, 1, fp64(c));
@@ -765,6 +845,7 @@ int md_compute_interactions(md_ctx* c, double* B, double* F, double* P3) {
   std::vector<double> pp(3 * (size_t)c->n);
   CK(c, cudaMemcpyAsync(pp.data(), c->Ppart, 8 * pp.size(), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
+  if ((st = check_overflow(c))) return st;
   if (P3) {
     double s[3] = {0, 0, 0};
     for (size_t b = 0; b < pp.size() / 3; b++)
@@ -935,6 +1016,38 @@ int md_debug_pairs(md_ctx* c, int64_t* pairs) {
   CK(c, cudaStreamSynchronize(c->stream));
   CK(c, cudaMemcpy(&v, &c->sc->pairs, sizeof v, cudaMemcpyDeviceToHost));
   *pairs = (int64_t)(v / 2);
+  return MD_OK;
+}
+
+int md_set_neighbor_skin(md_ctx* c, double skin_frac) {
+  if (!c || !(skin_frac >= 0) || skin_frac > 1) return set_err(c, MD_ERR_INVALID, "skin fraction must be in [0, 1]");
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->skin_frac = skin_frac;
+  c->list_valid = false;
+  invalidate_graph(c);
+  if (c->have_ewald) {
+    const double rlb = c->rc / c->L * (1.0 + c->skin_frac);
+    double est = (double)c->n * (double)c->n * 4.0 / 3.0 * 3.141592653589793 * rlb * rlb * rlb;
+    est = std::min(est, (double)c->n * (double)(c->n - 1));
+    if (int st = alloc_nbr(c, (long long)(1.3 * est) + 64LL * c->n)) return st;
+  }
+  return force_rebuild(c);
+}
+
+int md_debug_neighbor_capacity(md_ctx* c, int64_t cap, int64_t* used) {
+  if (!c) return MD_ERR_INVALID;
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (used) {
+    int total = 0;
+    CK(c, cudaMemcpy(&total, c->nbr_off + c->n, sizeof(int), cudaMemcpyDeviceToHost));
+    *used = total;
+  }
+  if (cap > 0) {
+    // shrink only the usable capacity; the allocation stays
+    c->nbr_cap = std::min<long long>(cap, c->nbr_cap);
+    invalidate_graph(c);
+    return force_rebuild(c);
+  }
   return MD_OK;
 }
 

@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(kIntThreads) k_heun2(IntParams p) {
   const int i = blockIdx.x * kIntThreads + threadIdx.x;
   const int n = p.n;
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  double disp2 = 0;  // squared displacement since the last neighbour-list build
   if (i < n) {
     // pressure partials of the real-space pass (any order sums the same pairs)
     acc[4] = p.Ppart[3 * i];
@@ -198,6 +199,11 @@ __global__ void __launch_bounds__(kIntThreads) k_heun2(IntParams p) {
       x -= L * (double)(x > half);
       x += L * (double)(x < -half);
       p.pos[a * n + i] = x;
+      if (p.xbuild) {
+        double db = x - p.xbuild[a * n + i];
+        db -= L * round(db / L);
+        disp2 += db * db;
+      }
       double tp = p.truePos[a * n + i];
       tp = x + round((tp - x) / L) * L;
       p.truePos[a * n + i] = tp;
@@ -207,6 +213,12 @@ __global__ void __launch_bounds__(kIntThreads) k_heun2(IntParams p) {
     }
     acc[3] = p.mm[2 * n + i];
     if (bad) atomicOr(p.err, kErrNonFinite);
+  }
+  if (p.flags) {
+    float d = (float)(sqrt(disp2) / p.L);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_xor_sync(kFull, d, o));
+    if ((threadIdx.x & 31) == 0 && d > 0.f) atomicMax(&p.flags->maxdisp, __float_as_uint(d));
   }
   __shared__ double red[7][kIntThreads / 32];
 #pragma unroll

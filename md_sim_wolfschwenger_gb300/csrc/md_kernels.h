@@ -5,9 +5,17 @@
 
 namespace md {
 
+// Step start: decides whether this step rebuilds the cell order and the
+// neighbour list (host request, or a particle moved more than half_skin).
+int launch_step_begin(cudaStream_t st, StepFlags* flags, double half_skin);
+// Raises the displacement since the last build after new positions arrived.
+int launch_disp_check(cudaStream_t st, int n, const double* pos, const double* xbuild, double L, StepFlags* flags);
+// Cell order (skipped unless the step rebuilds) and the sorted views.
 int launch_cells(cudaStream_t st, int n, const double* pos, const double* mm, const double* magMom_u,
                  const double* rMag_u, double L, const CellGrid& g, int* cellOf, int* count, int* tmp,
-                 const SortedView& s, bool fp64);
+                 const SortedView& s, bool fp64, double* xbuild, const StepFlags* flags);
+// Neighbour list within rc + skin (count, scan, fill; skipped unless rebuilding).
+int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64);
 int launch_set_mu(cudaStream_t st, int n, const double* mm, const double* magMom_u, const double* rMag_u,
                   const SortedView& s, bool fp64);
 

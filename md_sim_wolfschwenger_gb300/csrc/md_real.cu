@@ -9,14 +9,24 @@
 //                                       src/interaction.cpp:766-832,
 //                                       src/simulation.cpp:648-676
 //
-// Mapping: one warp per (cell-sorted) particle i.  The warp walks the rows of
-// its cell stencil; lane r first computes row r's cell range, culled to the
-// cells that intersect the cutoff sphere around i.  Lanes then test 32
-// candidates at a time (the next 32 are prefetched), and the in-range ones
-// are compacted with a ballot into a per-warp queue in shared memory that
-// holds the pair vector.  The pair maths (erfc, exp, ~90 flops) runs only on
-// full 32-pair batches, so every lane does useful work.  Per-lane sums are
-// reduced with warp shuffles; each warp writes its own pressure partial.
+// Neighbour search.  The reference lists every pair with r < rc each step
+// (all N(N-1)/2 pairs, CompInteractVecs).  Here a Verlet list with a skin
+// holds, for each cell-sorted particle, the particles within rc + skin at the
+// last build; it is rebuilt (on the device, inside the step) when some
+// particle has moved more than skin/2 since then, so every pair that is now
+// within rc is in the list.  Each evaluation tests the exact distance
+// against rc like the reference.  Build: one warp per particle walks the rows
+// of its cell stencil; lane r computes row r's cell range, culled to the
+// cells that intersect the search sphere; lanes test 32 candidates at a time
+// (next 32 prefetched) and a ballot compacts the hits (count pass, prefix
+// sum, fill pass).  If the list does not fit its capacity the evaluation
+// falls back to that scan directly, with in-range pairs compacted into a
+// per-warp shared-memory queue (correct, slower); the host then grows the
+// list.
+//
+// Evaluation: one warp per particle; lanes take list entries 32 at a time,
+// gather the neighbour's coordinates and moment, and run the pair maths
+// (erfc, exp, ~90 flops).  Per-lane sums are reduced with warp shuffles.
 //
 // Geometry (mixed path): 32-bit fixed-point coordinates (2^32 per box
 // length); their wrapping difference is the exact minimum image, converted
@@ -72,18 +82,14 @@ template <typename T, bool FULL, bool COAT>
 __device__ __forceinline__ void pair_terms(const RealParams& p, T dx, T dy, T dz, T r2, const typename V4<T>::t& mi,
                                            const typename V4<T>::t& mj, int oi, int oj, Acc<T>& a) {
   a.np++;
-  T ir0, ux, uy, uz, r, ire;
-  if constexpr (std::is_same<T, float>::value) {
+  T ir0;
+  if constexpr (std::is_same<T, float>::value)
     ir0 = rsqrtf(r2);
-  } else {
+  else
     ir0 = rsqrt(r2);
-  }
   const T r0 = r2 * ir0;
-  ux = dx * ir0;
-  uy = dy * ir0;
-  uz = dz * ir0;
-  r = r0;
-  ire = ir0;
+  const T ux = dx * ir0, uy = dy * ir0, uz = dz * ir0;
+  T r = r0, ire = ir0;
   const T dcont = mi.w + mj.w + (T)p.cont_eps;
   if (r < dcont) {
     if constexpr (FULL) {
@@ -161,77 +167,54 @@ __device__ __forceinline__ void pair_terms(const RealParams& p, T dx, T dy, T dz
   }
 }
 
-template <typename T, bool FULL, bool COAT>
-__global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
-  using T4 = typename V4<T>::t;
-  constexpr bool F32 = std::is_same<T, float>::value;
-  __shared__ float4 q[kRealWarps][64];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int k = blockIdx.x * kRealWarps + wib;
-  if (k >= p.n) return;  // whole warp; no block-level synchronisation below
-  Acc<T> a;
-  const T4 mi = ((const T4*)p.s.mu)[k];
-  int4 si = make_int4(0, 0, 0, 0);
-  double4_32a di = make_double4_32a(0, 0, 0, 0);
-  float xix, xiy, xiz;
+// Own coordinates of sorted particle k.
+template <typename T>
+struct Self {
+  int4 si;
+  double4_32a di;
+  float x, y, z;
   int oi;
-  if constexpr (F32) {
-    si = p.s.xi[k];
+};
+
+template <typename T, bool COAT>
+__device__ __forceinline__ Self<T> load_self(const RealParams& p, int k) {
+  Self<T> s;
+  s.si = make_int4(0, 0, 0, 0);
+  s.di = make_double4_32a(0, 0, 0, 0);
+  if constexpr (std::is_same<T, float>::value) {
+    s.si = p.s.xi[k];
     const float sc = 2.3283064365386963e-10f;
-    xix = (float)si.x * sc;
-    xiy = (float)si.y * sc;
-    xiz = (float)si.z * sc;
-    oi = si.w;
+    s.x = (float)s.si.x * sc;
+    s.y = (float)s.si.y * sc;
+    s.z = (float)s.si.z * sc;
+    s.oi = s.si.w;
   } else {
-    di = p.s.xd[k];
+    s.di = p.s.xd[k];
     const float4 f = p.s.xf[k];
-    xix = f.x;
-    xiy = f.y;
-    xiz = f.z;
-    oi = COAT ? p.s.perm[k] : 0;
+    s.x = f.x;
+    s.y = f.y;
+    s.z = f.z;
+    s.oi = COAT ? p.s.perm[k] : 0;
   }
+  return s;
+}
+
+// Walks the cell-stencil rows of particle k and calls visit(in, j, dx, dy, dz)
+// for every batch of 32 candidates (warp-synchronous; `in` marks candidates
+// within the search radius; dx.. is the pair vector on the mixed path).
+template <typename T, typename V>
+__device__ __forceinline__ void scan_rows(const RealParams& p, int k, int lane, const Self<T>& me, double r2box,
+                                          V&& visit) {
+  constexpr bool F32 = std::is_same<T, float>::value;
   const int ncx = p.grid.ncx, m = p.grid.reach, side = 2 * m + 1, R = side * side;
   const int cell = p.s.cell[k];
   const int cx = cell % ncx, cy = (cell / ncx) % ncx, cz = cell / (ncx * ncx);
   const float inv = 1.0f / (float)ncx;
-  const float rct2 = (float)p.rc2_test;
-  // fixed-point cutoff: r^2 in units of (L / 2^32)^2
-  const float rc2_fix = (float)(p.rc2 * 18446744073709551616.0);
+  const double rr = sqrt(r2box);
+  const float rt = (float)(rr * (1.0 + 1e-6) + 2e-7);
+  const float rct2 = rt * rt;                                          // culling / FP64 pre-test
+  const float r2fix = (float)(r2box * 18446744073709551616.0);         // (r / (L 2^-32))^2
   const int* cs = p.s.cell_start;
-  int head = 0, tail = 0;
-
-  auto flush = [&](int cnt) {
-    __syncwarp();
-    float4 e = lane < cnt ? q[wib][(head + lane) & 63] : make_float4(0, 0, 0, 0);
-    __syncwarp();
-    head += cnt;
-    if (lane < cnt) {
-      const int j = __float_as_int(e.w);
-      const T4 mj = ((const T4*)p.s.mu)[j];
-      int oj = 0;
-      if constexpr (COAT) oj = F32 ? p.s.xi[j].w : p.s.perm[j];
-      if constexpr (F32) {
-        pair_terms<T, FULL, COAT>(p, e.x, e.y, e.z, e.x * e.x + e.y * e.y + e.z * e.z, mi, mj, oi, oj, a);
-      } else {
-        const double4_32a dj = p.s.xd[j];
-        double dx = dj.x - di.x, dy = dj.y - di.y, dz = dj.z - di.z;
-        dx -= (double)(dx > 0.5);
-        dx += (double)(dx < -0.5);
-        dy -= (double)(dy > 0.5);
-        dy += (double)(dy < -0.5);
-        dz -= (double)(dz > 0.5);
-        dz += (double)(dz < -0.5);
-        const double r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < p.rc2) pair_terms<T, FULL, COAT>(p, dx, dy, dz, r2, mi, mj, oi, oj, a);
-      }
-    }
-  };
-  auto enqueue = [&](bool in, float4 v) {
-    const unsigned mask = __ballot_sync(kFull, in);
-    if (in) q[wib][(tail + __popc(mask & lanemask_lt())) & 63] = v;
-    tail += __popc(mask);
-    if (tail - head >= 32) flush(32);
-  };
   auto scan = [&](int s, int e) {
     if (s >= e) return;
     if constexpr (F32) {
@@ -241,9 +224,9 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
         const int j = j0 + lane;
         const int4 sj = nxt;
         if (j0 + 32 + lane < e) nxt = p.s.xi[j0 + 32 + lane];
-        const float dx = (float)(sj.x - si.x), dy = (float)(sj.y - si.y), dz = (float)(sj.z - si.z);
-        const bool in = j < e && j != k && dx * dx + dy * dy + dz * dz < rc2_fix;
-        enqueue(in, make_float4(dx * sc, dy * sc, dz * sc, __int_as_float(j)));
+        const float dx = (float)(sj.x - me.si.x), dy = (float)(sj.y - me.si.y), dz = (float)(sj.z - me.si.z);
+        const bool in = j < e && j != k && dx * dx + dy * dy + dz * dz < r2fix;
+        visit(in, j, dx * sc, dy * sc, dz * sc);
       }
     } else {
       float4 nxt = s + lane < e ? p.s.xf[s + lane] : make_float4(0, 0, 0, 0);
@@ -251,16 +234,15 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
         const int j = j0 + lane;
         const float4 xj = nxt;
         if (j0 + 32 + lane < e) nxt = p.s.xf[j0 + 32 + lane];
-        float dx = xj.x - xix, dy = xj.y - xiy, dz = xj.z - xiz;
+        float dx = xj.x - me.x, dy = xj.y - me.y, dz = xj.z - me.z;
         dx -= rintf(dx);
         dy -= rintf(dy);
         dz -= rintf(dz);
         const bool in = j < e && j != k && dx * dx + dy * dy + dz * dz < rct2;
-        enqueue(in, make_float4(0, 0, 0, __int_as_float(j)));
+        visit(in, j, 0.f, 0.f, 0.f);
       }
     }
   };
-
   for (int rb = 0; rb < R; rb += 32) {
     const int r = rb + lane;
     int a0 = 0, b0 = 0, a1 = 0, b1 = 0;
@@ -271,14 +253,14 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
       bool ok = true;
       if (ncx > 1) {
         const float ylo = uy * inv - 0.5f, yhi = ylo + inv, zlo = uz * inv - 0.5f, zhi = zlo + inv;
-        const float ey = fmaxf(0.f, fmaxf(ylo - xiy, xiy - yhi));
-        const float ez = fmaxf(0.f, fmaxf(zlo - xiz, xiz - zhi));
+        const float ey = fmaxf(0.f, fmaxf(ylo - me.y, me.y - yhi));
+        const float ez = fmaxf(0.f, fmaxf(zlo - me.z, me.z - zhi));
         const float d2 = ey * ey + ez * ez;
         ok = d2 < rct2;
         if (ok) {
           const float w = sqrtf(rct2 - d2);
-          xlo = max(xlo, (int)floorf((xix - w + 0.5f) * ncx));
-          xhi = min(xhi, (int)floorf((xix + w + 0.5f) * ncx));
+          xlo = max(xlo, (int)floorf((me.x - w + 0.5f) * ncx));
+          xhi = min(xhi, (int)floorf((me.x + w + 0.5f) * ncx));
         }
       }
       if (ok && xlo <= xhi) {
@@ -301,14 +283,169 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
       }
     }
     const int nr = min(32, R - rb);
-    for (int rr = 0; rr < nr; rr++) {
-      const int s0 = __shfl_sync(kFull, a0, rr), e0 = __shfl_sync(kFull, b0, rr);
-      const int s1 = __shfl_sync(kFull, a1, rr), e1 = __shfl_sync(kFull, b1, rr);
+    for (int q = 0; q < nr; q++) {
+      const int s0 = __shfl_sync(kFull, a0, q), e0 = __shfl_sync(kFull, b0, q);
+      const int s1 = __shfl_sync(kFull, a1, q), e1 = __shfl_sync(kFull, b1, q);
       scan(s0, e0);
       scan(s1, e1);
     }
   }
-  if (tail - head > 0) flush(tail - head);
+}
+
+// ------------------------------------------------------- neighbour list
+
+// Count (FILL = false) or write (FILL = true) the neighbours within rc + skin.
+template <typename T, bool FILL>
+__global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build(RealParams p) {
+  if (!p.flags->rebuild) return;
+  if (FILL && p.flags->overflow) return;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * kRealWarps + wib;
+  if (k >= p.n) return;
+  const Self<T> me = load_self<T, false>(p, k);
+  int cnt = 0;
+  int* out = FILL ? p.nbr + p.nbr_off[k] : nullptr;
+  scan_rows<T>(p, k, lane, me, p.rl2, [&](bool in, int j, float, float, float) {
+    const unsigned mask = __ballot_sync(kFull, in);
+    if (FILL && in) out[cnt + __popc(mask & lanemask_lt())] = j;
+    cnt += __popc(mask);
+  });
+  if (!FILL && lane == 0) p.nbr_cnt[k] = cnt;
+}
+
+// Exclusive scan of the counts (one block); flags overflow.
+__global__ void __launch_bounds__(1024) k_nbr_scan(RealParams p, StepFlags* flags) {
+  if (!flags->rebuild) return;
+  __shared__ long long wsum[32];
+  const int t = threadIdx.x, nt = blockDim.x, n = p.n;
+  const int per = (n + nt - 1) / nt;
+  const int b = t * per, e = min(n, b + per);
+  long long local = 0;
+  for (int i = b; i < e; i++) local += p.nbr_cnt[i];
+  const int lane = t & 31, w = t >> 5;
+  long long incl = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    const long long v = lane < (nt >> 5) ? wsum[lane] : 0;
+    long long inc2 = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long u = __shfl_up_sync(kFull, inc2, o);
+      if (lane >= o) inc2 += u;
+    }
+    wsum[lane] = inc2 - v;
+  }
+  __syncthreads();
+  long long run = wsum[w] + incl - local;
+  for (int i = b; i < e; i++) {
+    p.nbr_off[i] = (int)min(run, (long long)0x7fffffff);
+    run += p.nbr_cnt[i];
+  }
+  if (t == nt - 1) {
+    p.nbr_off[n] = (int)min(run, (long long)0x7fffffff);
+    flags->overflow = run > p.nbr_cap ? 1 : 0;
+  }
+}
+
+// ------------------------------------------------------------ evaluation
+
+template <typename T, bool FULL, bool COAT>
+__global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
+  using T4 = typename V4<T>::t;
+  constexpr bool F32 = std::is_same<T, float>::value;
+  __shared__ float4 q[kRealWarps][64];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * kRealWarps + wib;
+  if (k >= p.n) return;  // whole warp; no block-level synchronisation below
+  Acc<T> a;
+  const T4 mi = ((const T4*)p.s.mu)[k];
+  const Self<T> me = load_self<T, COAT>(p, k);
+  const float rc2_fix = (float)(p.rc2 * 18446744073709551616.0);
+
+  // pair terms with the neighbour's loaded coordinates and moment (mixed path)
+  auto eval_loaded = [&](const int4& sj, const T4& mj) {
+    if constexpr (F32) {
+      const float dxf = (float)(sj.x - me.si.x), dyf = (float)(sj.y - me.si.y), dzf = (float)(sj.z - me.si.z);
+      if (dxf * dxf + dyf * dyf + dzf * dzf < rc2_fix) {
+        const float sc = 2.3283064365386963e-10f;
+        const float dx = dxf * sc, dy = dyf * sc, dz = dzf * sc;
+        pair_terms<T, FULL, COAT>(p, dx, dy, dz, dx * dx + dy * dy + dz * dz, mi, mj, me.oi, COAT ? sj.w : 0, a);
+      }
+    }
+  };
+  // pair vector from i to sorted particle j, and the in-range test
+  auto eval = [&](int j) {
+    const T4 mj = ((const T4*)p.s.mu)[j];
+    if constexpr (F32) {
+      const int4 sj = p.s.xi[j];
+      const float dxf = (float)(sj.x - me.si.x), dyf = (float)(sj.y - me.si.y), dzf = (float)(sj.z - me.si.z);
+      if (dxf * dxf + dyf * dyf + dzf * dzf < rc2_fix) {
+        const float sc = 2.3283064365386963e-10f;
+        const float dx = dxf * sc, dy = dyf * sc, dz = dzf * sc;
+        pair_terms<T, FULL, COAT>(p, dx, dy, dz, dx * dx + dy * dy + dz * dz, mi, mj, me.oi, COAT ? sj.w : 0, a);
+      }
+    } else {
+      const double4_32a dj = p.s.xd[j];
+      double dx = dj.x - me.di.x, dy = dj.y - me.di.y, dz = dj.z - me.di.z;
+      dx -= (double)(dx > 0.5);
+      dx += (double)(dx < -0.5);
+      dy -= (double)(dy > 0.5);
+      dy += (double)(dy < -0.5);
+      dz -= (double)(dz > 0.5);
+      dz += (double)(dz < -0.5);
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 < p.rc2) pair_terms<T, FULL, COAT>(p, dx, dy, dz, r2, mi, mj, me.oi, COAT ? p.s.perm[j] : 0, a);
+    }
+  };
+
+  if (!p.flags->overflow) {
+    // Verlet list of this particle
+    const int* lst = p.nbr + p.nbr_off[k];
+    const int cnt = p.nbr_off[k + 1] - p.nbr_off[k];
+    if constexpr (F32) {
+      // two batches of 32 entries per iteration: all gathers issued first
+      for (int t0 = 0; t0 < cnt; t0 += 64) {
+        const int ta = t0 + lane, tb = t0 + 32 + lane;
+        const bool va = ta < cnt, vb = tb < cnt;
+        const int ja = va ? lst[ta] : k, jb = vb ? lst[tb] : k;
+        const int4 sa = p.s.xi[ja], sb = p.s.xi[jb];
+        const T4 ma = ((const T4*)p.s.mu)[ja], mb = ((const T4*)p.s.mu)[jb];
+        if (va) eval_loaded(sa, ma);
+        if (vb) eval_loaded(sb, mb);
+      }
+    } else {
+      int jn = lane < cnt ? lst[lane] : 0;
+      for (int t0 = 0; t0 < cnt; t0 += 32) {
+        const int j = jn;
+        const bool valid = t0 + lane < cnt;
+        if (t0 + 32 + lane < cnt) jn = lst[t0 + 32 + lane];
+        if (valid) eval(j);
+      }
+    }
+  } else {
+    // fallback: scan the cells; in-range candidates through the warp queue
+    int head = 0, tail = 0;
+    auto flush = [&](int cnt) {
+      __syncwarp();
+      const float4 e = lane < cnt ? q[wib][(head + lane) & 63] : make_float4(0, 0, 0, 0);
+      __syncwarp();
+      head += cnt;
+      if (lane < cnt) eval(__float_as_int(e.w));
+    };
+    scan_rows<T>(p, k, lane, me, p.rc2, [&](bool in, int j, float, float, float) {
+      const unsigned mask = __ballot_sync(kFull, in);
+      if (in) q[wib][(tail + __popc(mask & lanemask_lt())) & 63] = make_float4(0, 0, 0, __int_as_float(j));
+      tail += __popc(mask);
+      if (tail - head >= 32) flush(32);
+    });
+    if (tail - head > 0) flush(tail - head);
+  }
 
   a.b0 = warp_sum(a.b0);
   a.b1 = warp_sum(a.b1);
@@ -349,6 +486,20 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
 }
 
 int real_blocks(int n) { return (n + kRealWarps - 1) / kRealWarps; }
+
+int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64) {
+  dim3 grid(real_blocks(p.n)), block(kRealWarps * 32);
+  if (fp64)
+    k_nbr_build<double, false><<<grid, block, 0, st>>>(p);
+  else
+    k_nbr_build<float, false><<<grid, block, 0, st>>>(p);
+  k_nbr_scan<<<1, 1024, 0, st>>>(p, flags);
+  if (fp64)
+    k_nbr_build<double, true><<<grid, block, 0, st>>>(p);
+  else
+    k_nbr_build<float, true><<<grid, block, 0, st>>>(p);
+  return 3;
+}
 
 int launch_real(cudaStream_t st, const RealParams& p, bool full, bool fp64) {
   dim3 grid(real_blocks(p.n)), block(kRealWarps * 32);

@@ -255,6 +255,16 @@ class Simulation:
         self._ck(self.L.md_debug_pairs(self.h, C.byref(v)))
         return v.value
 
+    def set_neighbor_skin(self, skin_frac):
+        """Skin of the real-space neighbour list as a fraction of rc."""
+        self._ck(self.L.md_set_neighbor_skin(self.h, float(skin_frac)))
+
+    def neighbor_capacity(self, cap=0):
+        """Entries of the last neighbour list; cap > 0 caps the capacity (test hook)."""
+        used = C.c_int64()
+        self._ck(self.L.md_debug_neighbor_capacity(self.h, int(cap), C.byref(used)))
+        return used.value
+
     def profile(self, enable=True):
         self._ck(self.L.md_profile(self.h, int(enable)))
 
