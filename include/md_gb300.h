@@ -259,6 +259,119 @@ int md_profile_read(md_ctx* ctx, double* ms);
  * FLOPs) from a register-resident FMA-chain kernel on all SMs. */
 int md_calibrate_fp32(double* tflops);
 
+/* ------------------------------------------------------ initial systems */
+/* InitParticleProps size draws and InitCoordsFromSketch
+ * (src/simulation.cpp:118-351) for n particles: radii rMag, rHydr (n), pos,
+ * mm, ea (n x 3 column-major FP64) and the box length (src/simulation.cpp:56).
+ *   sizes:     SIZE_DIST 0: rMagMean; 1: log-normal with the reference's
+ *              (mu, sigmaLog) from rMagMean and sigma, or ln r ~ N(ln rMagMean,
+ *              sigmaLog) when the [gb300] sigmaLog key is set;
+ *   positions: INIT_CONFIG_TRANS 1: random sequential addition of
+ *              non-overlapping hydrodynamic spheres in [-(L/2 - r_h), L/2 - r_h]^3
+ *              (cell grid, O(n); polydisperse sizes are placed largest first);
+ *              2: cubic grid (n must be a cube);
+ *   rotations: INIT_CONFIG_ROT 1, 2, 3 as the reference; 4 (extension): mm
+ *              and ea independent and uniform on the sphere.
+ * rHydr may be NULL.  Random numbers: a seeded xoshiro256** stream, not the
+ * reference's Mersenne-Twister stream. */
+int md_init_system(const md_config* cfg, int64_t n, uint64_t seed, double* rMag, double* rHydr, double* pos,
+                   double* mm, double* ea, double* lBox);
+
+/* Ewald cutoff tuned per (N, volume fraction) bucket: the first system of a
+ * bucket runs md_autotune_ewald (timed field evaluations over candidate
+ * cutoffs, each with alpha and kc from the error model); later systems of the
+ * bucket reuse the winning rc / L.  *hit = 1 when the cache answered.  The
+ * cache is process-wide; md_tune_cache_save/load keep it in a text file. */
+int md_autotune_ewald_cached(md_ctx* ctx, double volFrac, double* alpha, double* rc, int64_t* kc, int* hit);
+int md_tune_cache_save(const char* path);
+int md_tune_cache_load(const char* path);
+int md_tune_cache_clear(void);
+
+/* ------------------------------------------------------ packed systems */
+/* Independent systems (replicas of uneven N: field sweeps, seed ensembles,
+ * served requests) advanced together: every kernel of the step is launched
+ * once for all systems of the batch (one grid over all their blocks, one
+ * captured CUDA graph per step), and each system's results equal those of
+ * md_step on it alone, bit for bit.  Systems keep their own contexts (the
+ * caller owns them); the batch holds at most `capacity` of them.
+ * Requirements: MD_PREC_MIXED, noise MD_NOISE_OFF or MD_NOISE_PHILOX, state
+ * uploaded and Ewald parameters set.  While a round is in flight
+ * (md_batch_launch .. md_batch_wait) the contexts in the batch must not be
+ * used. */
+typedef struct md_batch md_batch;
+int md_batch_create(int64_t capacity, md_batch** out);
+int md_batch_destroy(md_batch* batch);
+/* Adds ctx to run nsteps steps of size dt; *id identifies it in the batch. */
+int md_batch_add(md_batch* batch, md_ctx* ctx, int64_t nsteps, double dt, int64_t* id);
+int md_batch_remove(md_batch* batch, int64_t id);
+/* Launches min(max_steps, fewest steps left of any system) steps of every
+ * system (asynchronous; *steps gets that count) ... */
+int md_batch_launch(md_batch* batch, int64_t max_steps, int64_t* steps);
+/* ... and waits for them: MD_ERR_NONFINITE if some system's state became
+ * non-finite (md_batch_remaining tells which). */
+int md_batch_wait(md_batch* batch);
+/* launch + wait. */
+int md_batch_run(md_batch* batch, int64_t max_steps, int64_t* steps);
+/* Steps still to run and the status of the last round of system id. */
+int md_batch_remaining(const md_batch* batch, int64_t id, int64_t* left, int* status);
+/* Systems, particles, kernel launches per packed step, GPU time of the last
+ * round (ms, CUDA events on the batch's stream). */
+int md_batch_info(const md_batch* batch, int64_t* systems, int64_t* particles, int64_t* launches_per_step,
+                  double* last_round_ms);
+
+/* ------------------------------------------------------------ serving */
+/* One simulation request of a served stream. */
+typedef struct md_request {
+  int64_t n;          /* particles                                           */
+  double volFrac;     /* volume fraction of hydrodynamic spheres             */
+  int64_t steps;      /* Heun steps                                          */
+  double dt;          /* step (s)                                            */
+  int64_t fieldKind;  /* MD_FIELD_STEP: fieldAmp along z for all t;
+                         MD_FIELD_SIN: fieldAmp sin(2 pi fieldFreq t) along z */
+  double fieldAmp;    /* T                                                   */
+  double fieldFreq;   /* Hz                                                  */
+  uint64_t seed;      /* initial system and Philox noise                     */
+  double arrival;     /* s after the start of md_serve_run                  */
+} md_request;
+
+typedef struct md_request_result {
+  int status;         /* MD_OK or the error that ended the request           */
+  double admitted;    /* s after the start: state on the device              */
+  double finished;    /* s after the start: last step done                   */
+  double latency;     /* finished - arrival                                  */
+  double mz;          /* mean m_z after the last step                        */
+  double checksum;    /* sum of pos / L + mm + ea over all particles (final) */
+  int64_t steps_done;
+  int64_t device_bytes;
+} md_request_result;
+
+typedef struct md_serve_opts {
+  double hbm_budget;     /* device bytes the admitted systems may hold        */
+  int64_t max_systems;   /* systems packed at once                            */
+  int64_t round_steps;   /* steps per packed round (admission granularity)    */
+  int realtime;          /* 1: admit a request no earlier than its arrival    */
+  int autotune;          /* 1: Ewald cutoff from md_autotune_ewald_cached     */
+} md_serve_opts;
+
+typedef struct md_serve_stats {
+  double wall;            /* s from start to the last completion              */
+  double particle_steps;  /* sum over requests of n * steps                   */
+  double gpu_ms;          /* GPU time of all packed rounds (CUDA events)      */
+  double admit_ms;        /* host time spent admitting (init, upload, setup)  */
+  int64_t rounds, repacks, peak_systems;
+  double peak_bytes;
+} md_serve_stats;
+
+/* Continuous batching over a request stream: requests are admitted in
+ * arrival order as device memory (hbm_budget) and batch slots free up; each
+ * admitted request becomes a system (md_init_system with base's keys and the
+ * request's n, volFrac, field and seed; Ewald parameters for
+ * base.errTolEwald) that joins the packed batch at the next round, while the
+ * current round runs on the GPU.  Finished systems leave the batch and free
+ * their memory.  results[i] belongs to reqs[i]. */
+int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, const md_serve_opts* opts,
+                 md_request_result* results, md_serve_stats* stats);
+
 /* ------------------------------------------- structure factor, no allocation */
 /* This entry point has no counterpart in the reference.  It exists for
  * callers that cannot call cudaMalloc -- a host framework that owns all

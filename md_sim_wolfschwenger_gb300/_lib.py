@@ -49,6 +49,29 @@ class MdConfig(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class MdRequest(C.Structure):
+    _fields_ = [("n", C.c_int64), ("volFrac", C.c_double), ("steps", C.c_int64), ("dt", C.c_double),
+                ("fieldKind", C.c_int64), ("fieldAmp", C.c_double), ("fieldFreq", C.c_double),
+                ("seed", C.c_uint64), ("arrival", C.c_double)]
+
+
+class MdRequestResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("admitted", C.c_double), ("finished", C.c_double), ("latency", C.c_double),
+                ("mz", C.c_double), ("checksum", C.c_double), ("steps_done", C.c_int64),
+                ("device_bytes", C.c_int64)]
+
+
+class MdServeOpts(C.Structure):
+    _fields_ = [("hbm_budget", C.c_double), ("max_systems", C.c_int64), ("round_steps", C.c_int64),
+                ("realtime", C.c_int), ("autotune", C.c_int)]
+
+
+class MdServeStats(C.Structure):
+    _fields_ = [("wall", C.c_double), ("particle_steps", C.c_double), ("gpu_ms", C.c_double),
+                ("admit_ms", C.c_double), ("rounds", C.c_int64), ("repacks", C.c_int64),
+                ("peak_systems", C.c_int64), ("peak_bytes", C.c_double)]
+
+
 _lib = None
 
 
@@ -106,6 +129,22 @@ def lib():
         "md_profile": (C.c_int, [V, C.c_int]),
         "md_profile_read": (C.c_int, [V, P]),
         "md_calibrate_fp32": (C.c_int, [P]),
+        "md_init_system": (C.c_int, [C.POINTER(MdConfig), I64, C.c_uint64, P, P, P, P, P, P]),
+        "md_autotune_ewald_cached": (C.c_int, [V, C.c_double, P, P, PI64, C.POINTER(C.c_int)]),
+        "md_tune_cache_save": (C.c_int, [C.c_char_p]),
+        "md_tune_cache_load": (C.c_int, [C.c_char_p]),
+        "md_tune_cache_clear": (C.c_int, []),
+        "md_batch_create": (C.c_int, [I64, C.POINTER(V)]),
+        "md_batch_destroy": (C.c_int, [V]),
+        "md_batch_add": (C.c_int, [V, V, I64, C.c_double, PI64]),
+        "md_batch_remove": (C.c_int, [V, I64]),
+        "md_batch_launch": (C.c_int, [V, I64, PI64]),
+        "md_batch_wait": (C.c_int, [V]),
+        "md_batch_run": (C.c_int, [V, I64, PI64]),
+        "md_batch_remaining": (C.c_int, [V, I64, PI64, C.POINTER(C.c_int)]),
+        "md_batch_info": (C.c_int, [V, PI64, PI64, PI64, P]),
+        "md_serve_run": (C.c_int, [C.POINTER(MdConfig), C.POINTER(MdRequest), I64, C.POINTER(MdServeOpts),
+                                   C.POINTER(MdRequestResult), C.POINTER(MdServeStats)]),
         "md_noalloc_scratch_bytes": (C.c_size_t, []),
         "md_structure_factor_noalloc": (C.c_int, [V, V, I64, C.c_double, I64, C.c_double, V, PI64, V]),
     }

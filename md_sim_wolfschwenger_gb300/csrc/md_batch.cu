@@ -1,0 +1,399 @@
+// md_batch.cu -- packed stepping of several independent systems (replicas of
+// uneven N: field sweeps, seed ensembles, served requests).
+//
+// Each system keeps its own md_ctx (buffers, Ewald setup, device time, step
+// counter, records).  A batch launches every kernel of the step ONCE for all
+// of its systems: the grid of a packed launch is the concatenation of the
+// systems' own grids, listed in a task table (system, local block), and each
+// block reads its system's parameters from a device array.  The kernel bodies
+// are those of the single-system path, so a system's trajectory is the same,
+// bit for bit, alone or packed with others.  One step of the whole batch is
+// captured once into a CUDA graph and replayed; the graph is re-captured
+// only when the set of systems changes (the task tables and grid sizes
+// change), and parameter arrays are re-uploaded when a system's buffers move
+// (e.g. its neighbour list grew).
+//
+// Requirements: mixed precision, noise off or Philox (the uploaded-noise
+// mode reads host data per step), same device as the batch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "md_ctx_internal.h"
+#include "md_kernels.h"
+
+namespace {
+
+struct Slot {
+  md_ctx* ctx;
+  int64_t id;
+  int64_t left;  // steps still to run
+  double dt;
+  int status;    // MD_OK or the status of the last round (non-finite state)
+};
+
+}  // namespace
+
+struct md_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int64_t capacity = 0;
+  std::vector<Slot> slots;
+  int64_t next_id = 1;
+  // packed state
+  bool packed = false;        // tables, parameters and graph match `slots`
+  bool params_dirty = false;  // parameters must be re-uploaded (graph still valid)
+  std::vector<int> order;     // pack order (system index into slots)
+  CellParams* d_cell = nullptr;
+  RealParams *d_rfull = nullptr, *d_rfield = nullptr;
+  KParams *d_kfull = nullptr, *d_kfield = nullptr;
+  IntParams *d_i1 = nullptr, *d_i2 = nullptr;
+  ObsParams* d_obs = nullptr;
+  int* d_status = nullptr;
+  Task* d_tasks = nullptr;
+  size_t task_cap = 0;
+  Packed n256{}, sort{}, real{}, phase{}, sk{}, red{}, sc{};
+  int kcmax = 0, np = 64;
+  bool coat = false;
+  int64_t launches_per_step = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool running = false;  // a round was launched and not yet waited for
+  int64_t round_steps = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_round_ms = 0;
+};
+
+namespace {
+
+void drop_graph(md_batch* b) {
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->gexec = nullptr;
+  b->graph = nullptr;
+  b->packed = false;
+}
+
+template <typename P>
+int upload(P* d, const std::vector<P>& h, cudaStream_t st) {
+  if (h.empty()) return MD_OK;
+  cudaError_t e = cudaMemcpyAsync(d, h.data(), sizeof(P) * h.size(), cudaMemcpyHostToDevice, st);
+  return e == cudaSuccess ? MD_OK : set_err(nullptr, MD_ERR_CUDA, "parameter upload: %s", cudaGetErrorString(e));
+}
+
+// Parameters of every system in pack order.
+int upload_params(md_batch* b) {
+  const size_t R = b->order.size();
+  std::vector<CellParams> cell(R);
+  std::vector<RealParams> rfull(R), rfield(R);
+  std::vector<KParams> kfull(R), kfield(R);
+  std::vector<IntParams> i1(R), i2(R);
+  std::vector<ObsParams> obs(R);
+  for (size_t r = 0; r < R; r++) {
+    const Slot& s = b->slots[b->order[r]];
+    md_ctx* c = s.ctx;
+    cell[r] = cell_params(c);
+    rfull[r] = real_params(c, c->Br, c->Fr, c->ov);
+    rfull[r].npairs = nullptr;
+    rfield[r] = real_params(c, c->Br2, nullptr, nullptr);
+    kfull[r] = k_params(c, c->Bk, c->Fk);
+    kfield[r] = k_params(c, c->Bk2, nullptr);
+    i1[r] = int_params(c, s.dt, c->Br, c->Bk);
+    i2[r] = int_params(c, s.dt, c->Br2, c->Bk2);
+    obs[r] = obs_params(c, s.dt);
+    obs[r].status = b->d_status + r;
+  }
+  int st;
+  if ((st = upload(b->d_cell, cell, b->stream))) return st;
+  if ((st = upload(b->d_rfull, rfull, b->stream))) return st;
+  if ((st = upload(b->d_rfield, rfield, b->stream))) return st;
+  if ((st = upload(b->d_kfull, kfull, b->stream))) return st;
+  if ((st = upload(b->d_kfield, kfield, b->stream))) return st;
+  if ((st = upload(b->d_i1, i1, b->stream))) return st;
+  if ((st = upload(b->d_i2, i2, b->stream))) return st;
+  if ((st = upload(b->d_obs, obs, b->stream))) return st;
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "parameter upload: %s", cudaGetErrorString(e));
+  b->params_dirty = false;
+  return MD_OK;
+}
+
+// Task tables, parameters and the captured step for the current systems.
+int pack(md_batch* b) {
+  drop_graph(b);
+  const int R = (int)b->slots.size();
+  b->order.resize(R);
+  std::iota(b->order.begin(), b->order.end(), 0);
+  // larger systems first: their blocks start first in every packed grid
+  std::stable_sort(b->order.begin(), b->order.end(),
+                   [&](int x, int y) { return b->slots[x].ctx->n > b->slots[y].ctx->n; });
+  b->kcmax = 0;
+  b->coat = false;
+  for (const Slot& s : b->slots) {
+    b->kcmax = std::max<int>(b->kcmax, (int)s.ctx->kc);
+    b->coat = b->coat || s.ctx->cfg.ENABLE_COATING_POT;
+  }
+  b->np = scatter_particles(b->kcmax, false);
+  if (!b->np) return set_err(nullptr, MD_ERR_UNSUPPORTED, "kc too large for the packed k-space scatter");
+  // task tables, one segment per kernel shape
+  std::vector<Task> tasks;
+  auto table = [&](Packed& pk, auto blocks_of) {
+    const size_t start = tasks.size();
+    for (int r = 0; r < R; r++) {
+      const int nb = blocks_of(b->slots[b->order[r]].ctx);
+      for (int q = 0; q < nb; q++) tasks.push_back(Task{r, q});
+    }
+    pk.n = (int)(tasks.size() - start);
+    pk.tasks = reinterpret_cast<const Task*>(start);  // offset until the upload
+  };
+  table(b->n256, [](md_ctx* c) { return cell_blocks((int)c->n); });
+  table(b->sort, [](md_ctx* c) { return cell_sort_blocks(c->grid); });
+  table(b->real, [](md_ctx* c) { return real_blocks((int)c->n); });
+  table(b->phase, [](md_ctx* c) { return phase_blocks((int)c->n); });
+  table(b->sk, [](md_ctx* c) { return sk_blocks(k_params(c, nullptr, nullptr)); });
+  table(b->red, [](md_ctx* c) { return skred_blocks(k_params(c, nullptr, nullptr)); });
+  const int np = b->np;
+  table(b->sc, [np](md_ctx* c) { return scatter_blocks(k_params(c, nullptr, nullptr), np); });
+  if (tasks.size() > b->task_cap) {
+    if (b->d_tasks) cudaFree(b->d_tasks);
+    b->d_tasks = nullptr;
+    b->task_cap = 0;
+    const size_t cap = tasks.size() + tasks.size() / 4 + 1024;
+    cudaError_t e = cudaMalloc(&b->d_tasks, sizeof(Task) * cap);
+    if (e != cudaSuccess) return set_err(nullptr, MD_ERR_NOMEM, "task table: %s", cudaGetErrorString(e));
+    b->task_cap = cap;
+  }
+  for (Packed* pk : {&b->n256, &b->sort, &b->real, &b->phase, &b->sk, &b->red, &b->sc})
+    pk->tasks = b->d_tasks + reinterpret_cast<size_t>(pk->tasks);
+  int st;
+  if ((st = upload(b->d_tasks, tasks, b->stream))) return st;
+  if ((st = upload_params(b))) return st;
+  if (R == 0) {
+    b->packed = true;
+    b->launches_per_step = 0;
+    return MD_OK;
+  }
+  // capture one step of every system
+  cudaStream_t s = b->stream;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
+  int64_t l = 0;
+  l += launch_step_begin_packed(s, b->d_cell, R);
+  l += launch_cells_packed(s, b->d_cell, R, b->n256, b->sort);
+  l += launch_nbr_packed(s, b->d_rfull, R, b->real);
+  l += launch_phase_tables_packed(s, b->d_kfull, b->phase);
+  l += launch_real_packed(s, b->d_rfull, b->real, true, b->coat);
+  l += launch_kspace_packed(s, b->d_kfull, b->sk, b->red, b->sc, true, b->kcmax, b->np);
+  l += launch_heun1_packed(s, b->d_i1, b->n256);
+  l += launch_real_packed(s, b->d_rfield, b->real, false, false);
+  l += launch_kspace_packed(s, b->d_kfield, b->sk, b->red, b->sc, false, b->kcmax, b->np);
+  l += launch_heun2_packed(s, b->d_i2, b->n256);
+  l += launch_obs_packed(s, b->d_obs, R);
+  e = cudaStreamEndCapture(s, &b->graph);
+  if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&b->gexec, b->graph, 0);
+  if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  b->launches_per_step = l;
+  b->packed = true;
+  return MD_OK;
+}
+
+Slot* find(md_batch* b, int64_t id) {
+  for (Slot& s : b->slots)
+    if (s.id == id) return &s;
+  return nullptr;
+}
+
+template <typename P>
+int alloc_array(P** p, size_t n) {
+  cudaError_t e = cudaMalloc(p, sizeof(P) * std::max<size_t>(n, 1));
+  return e == cudaSuccess ? MD_OK : set_err(nullptr, MD_ERR_NOMEM, "batch arrays: %s", cudaGetErrorString(e));
+}
+
+// Completes the launched round: per-system status (non-finite state, list
+// overflow), step accounting.
+int finish_round(md_batch* b) {
+  if (!b->running) return MD_OK;
+  b->running = false;
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "batch round: %s", cudaGetErrorString(e));
+  cudaEventElapsedTime(&b->last_round_ms, b->ev0, b->ev1);
+  const size_t R = b->order.size();
+  std::vector<int> status(R);
+  if (R) {
+    e = cudaMemcpy(status.data(), b->d_status, sizeof(int) * R, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "batch status: %s", cudaGetErrorString(e));
+  }
+  int bad = MD_OK;
+  for (size_t r = 0; r < R; r++) {
+    Slot& s = b->slots[b->order[r]];
+    s.left -= b->round_steps;
+    s.ctx->have_geometry = true;
+    s.ctx->list_valid = true;
+    if (status[r] & 4) {
+      // the neighbour list did not fit (results are correct): grow it
+      const int64_t cap0 = s.ctx->nbr_cap;
+      int st = check_overflow(s.ctx);
+      if (st) return st;
+      if (s.ctx->nbr_cap != cap0) b->params_dirty = true;
+    }
+    if (status[r] & ~4) {
+      const int st = read_err_word(s.ctx);  // clears the word and records the message
+      if (st) {
+        s.status = st;
+        if (!bad) bad = set_err(nullptr, st, "system %lld: non-finite state", (long long)s.id);
+      }
+    }
+    if (status[r]) {
+      // the fixes above went through the system's own stream
+      e = cudaStreamSynchronize(s.ctx->stream);
+      if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "batch status: %s", cudaGetErrorString(e));
+    }
+  }
+  if (R) cudaMemset(b->d_status, 0, sizeof(int) * R);
+  return bad;
+}
+
+}  // namespace
+
+extern "C" {
+
+int md_batch_create(int64_t capacity, md_batch** out) {
+  if (!out || capacity < 1 || capacity > (1 << 20)) return set_err(nullptr, MD_ERR_INVALID, "bad batch capacity");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_err(nullptr, MD_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  md_batch* b = new md_batch();
+  cudaGetDevice(&b->device);
+  b->capacity = capacity;
+  int st = MD_OK;
+  auto fail = [&](int s) {
+    md_batch_destroy(b);
+    return s;
+  };
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
+    return fail(set_err(nullptr, MD_ERR_CUDA, "batch stream/events"));
+  const size_t C = (size_t)capacity;
+  if ((st = alloc_array(&b->d_cell, C)) || (st = alloc_array(&b->d_rfull, C)) || (st = alloc_array(&b->d_rfield, C)) ||
+      (st = alloc_array(&b->d_kfull, C)) || (st = alloc_array(&b->d_kfield, C)) || (st = alloc_array(&b->d_i1, C)) ||
+      (st = alloc_array(&b->d_i2, C)) || (st = alloc_array(&b->d_obs, C)) || (st = alloc_array(&b->d_status, C)))
+    return fail(st);
+  if (cudaMemset(b->d_status, 0, sizeof(int) * C) != cudaSuccess)
+    return fail(set_err(nullptr, MD_ERR_CUDA, "batch status init"));
+  *out = b;
+  return MD_OK;
+}
+
+int md_batch_destroy(md_batch* b) {
+  if (!b) return MD_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graph(b);
+  void* arrays[] = {b->d_cell, b->d_rfull, b->d_rfield, b->d_kfull, b->d_kfield, b->d_i1, b->d_i2, b->d_obs,
+                    b->d_status, b->d_tasks};
+  for (void* p : arrays)
+    if (p) cudaFree(p);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return MD_OK;
+}
+
+int md_batch_add(md_batch* b, md_ctx* c, int64_t nsteps, double dt, int64_t* id) {
+  if (!b || !c) return set_err(nullptr, MD_ERR_INVALID, "null batch or context");
+  if (b->running) return set_err(nullptr, MD_ERR_INVALID, "batch round in flight (md_batch_wait first)");
+  if ((int64_t)b->slots.size() >= b->capacity) return set_err(nullptr, MD_ERR_NOMEM, "batch is full");
+  if (nsteps < 0 || !(dt > 0)) return set_err(nullptr, MD_ERR_INVALID, "bad nsteps or dt");
+  int st = check_ready(c, true);
+  if (st) return st;
+  if (c->prec != MD_PREC_MIXED) return set_err(c, MD_ERR_UNSUPPORTED, "packed stepping runs mixed precision only");
+  if (c->noise == MD_NOISE_UPLOADED) return set_err(c, MD_ERR_UNSUPPORTED, "packed stepping: noise off or Philox");
+  if (c->device != b->device) return set_err(c, MD_ERR_INVALID, "context and batch on different devices");
+  for (const Slot& s : b->slots)
+    if (s.ctx == c) return set_err(c, MD_ERR_INVALID, "context already in the batch");
+  if (!scatter_particles((int)c->kc, false)) return set_err(c, MD_ERR_UNSUPPORTED, "kc too large");
+  if ((st = prepare_dt(c, dt))) return st;
+  if ((st = ensure_records(c, nsteps))) return st;
+  CK(c, cudaStreamSynchronize(c->stream));
+  Slot s{c, b->next_id++, nsteps, dt, MD_OK};
+  b->slots.push_back(s);
+  b->packed = false;
+  if (id) *id = s.id;
+  return MD_OK;
+}
+
+int md_batch_remove(md_batch* b, int64_t id) {
+  if (!b) return set_err(nullptr, MD_ERR_INVALID, "null batch");
+  if (b->running) return set_err(nullptr, MD_ERR_INVALID, "batch round in flight (md_batch_wait first)");
+  for (size_t k = 0; k < b->slots.size(); k++)
+    if (b->slots[k].id == id) {
+      b->slots.erase(b->slots.begin() + k);
+      b->packed = false;
+      return MD_OK;
+    }
+  return set_err(nullptr, MD_ERR_INVALID, "no system %lld in the batch", (long long)id);
+}
+
+int md_batch_launch(md_batch* b, int64_t max_steps, int64_t* steps) {
+  if (!b || max_steps < 0) return set_err(nullptr, MD_ERR_INVALID, "bad arguments");
+  if (b->running) return set_err(nullptr, MD_ERR_INVALID, "batch round in flight (md_batch_wait first)");
+  int64_t k = max_steps;
+  for (const Slot& s : b->slots) k = std::min(k, s.left);
+  if (b->slots.empty()) k = 0;
+  if (steps) *steps = k;
+  if (k <= 0) return MD_OK;
+  int st;
+  if (!b->packed) {
+    if ((st = pack(b))) return st;
+  } else if (b->params_dirty) {
+    if ((st = upload_params(b))) return st;
+  }
+  cudaEventRecord(b->ev0, b->stream);
+  for (int64_t q = 0; q < k; q++) {
+    cudaError_t e = cudaGraphLaunch(b->gexec, b->stream);
+    if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "graph launch: %s", cudaGetErrorString(e));
+  }
+  cudaEventRecord(b->ev1, b->stream);
+  b->round_steps = k;
+  b->running = true;
+  return MD_OK;
+}
+
+int md_batch_wait(md_batch* b) {
+  if (!b) return set_err(nullptr, MD_ERR_INVALID, "null batch");
+  return finish_round(b);
+}
+
+int md_batch_run(md_batch* b, int64_t max_steps, int64_t* steps) {
+  int st = md_batch_launch(b, max_steps, steps);
+  if (st) return st;
+  return finish_round(b);
+}
+
+int md_batch_remaining(const md_batch* b, int64_t id, int64_t* left, int* status) {
+  if (!b) return set_err(nullptr, MD_ERR_INVALID, "null argument");
+  Slot* s = find(const_cast<md_batch*>(b), id);
+  if (!s) return set_err(nullptr, MD_ERR_INVALID, "no system %lld in the batch", (long long)id);
+  if (left) *left = s->left;
+  if (status) *status = s->status;
+  return MD_OK;
+}
+
+int md_batch_info(const md_batch* b, int64_t* systems, int64_t* particles, int64_t* launches_per_step,
+                  double* last_round_ms) {
+  if (!b) return set_err(nullptr, MD_ERR_INVALID, "null batch");
+  int64_t np = 0;
+  for (const Slot& s : b->slots) np += s.ctx->n;
+  if (systems) *systems = (int64_t)b->slots.size();
+  if (particles) *particles = np;
+  if (launches_per_step) *launches_per_step = b->launches_per_step;
+  if (last_round_ms) *last_round_ms = b->last_round_ms;
+  return MD_OK;
+}
+
+}  // extern "C"

@@ -14,6 +14,9 @@
 // views are refreshed every step from the particle-order state through the
 // unchanged permutation.
 //
+// Every kernel is a block body with two entry points: one system (parameters
+// by value) and packed (a task table over several systems).
+//
 // Roofline: HBM/L2 bound, ~60 B per particle of algorithmic traffic
 // (pos 24 B read, cell id 4+4 B, sorted views 16+16+16 B written, index
 // arrays 8 B) plus 8 B per cell.
@@ -21,6 +24,8 @@
 #include "md_kernels.h"
 
 namespace md {
+
+constexpr int kCellThreads = 256;
 
 __device__ __forceinline__ int cell_coord(double xb, int ncx) {
   int c = (int)((xb + 0.5) * (double)ncx);
@@ -38,8 +43,7 @@ __device__ __forceinline__ bool skip(const StepFlags* f) { return f && !f->rebui
 // Start of a step: rebuild the cell order and the neighbour list if the host
 // asked for it or some particle moved more than half the skin since the last
 // build (box units).
-__global__ void k_step_begin(StepFlags* f, float half_skin) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void step_begin(StepFlags* f, float half_skin) {
   const int rb = f->force || __uint_as_float(f->maxdisp) > half_skin;
   f->rebuild = rb;
   if (rb) {
@@ -48,25 +52,33 @@ __global__ void k_step_begin(StepFlags* f, float half_skin) {
   }
 }
 
-__global__ void k_cell_assign(int n, const double* __restrict__ pos, double invL, int ncx, int* __restrict__ cellOf,
-                              int* __restrict__ count, const StepFlags* flags) {
-  if (skip(flags)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Cell of each particle (all-pairs grid: identity order, one cell).
+__device__ __forceinline__ void cell_assign(const CellParams& p, int bx) {
+  if (skip(p.flags)) return;
+  const int i = bx * kCellThreads + threadIdx.x, n = p.n;
   if (i >= n) return;
-  int cx = cell_coord(wrap_box(pos[i], invL), ncx);
-  int cy = cell_coord(wrap_box(pos[n + i], invL), ncx);
-  int cz = cell_coord(wrap_box(pos[2 * n + i], invL), ncx);
-  int c = (cz * ncx + cy) * ncx + cx;
-  cellOf[i] = c;
-  if (count) atomicAdd(&count[c], 1);
+  const int ncx = p.grid.ncx;
+  if (ncx == 1) {
+    p.s.perm[i] = i;
+    p.cellOf[i] = 0;
+    return;
+  }
+  const int cx = cell_coord(wrap_box(p.pos[i], p.invL), ncx);
+  const int cy = cell_coord(wrap_box(p.pos[n + i], p.invL), ncx);
+  const int cz = cell_coord(wrap_box(p.pos[2 * n + i], p.invL), ncx);
+  const int c = (cz * ncx + cy) * ncx + cx;
+  p.cellOf[i] = c;
+  atomicAdd(&p.count[c], 1);
 }
 
 // Exclusive scan of count[0..ncell) -> start[0..ncell]; count is zeroed so it
 // can serve as the fill counter of the scatter.  One block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_cell_scan(int ncell, int* __restrict__ count, int* __restrict__ start,
-                                                    const StepFlags* flags) {
-  if (skip(flags)) return;
+__device__ __forceinline__ void cell_scan(const CellParams& p) {
+  if (skip(p.flags) || p.grid.ncx == 1) return;
   __shared__ int wsum[32];
+  const int ncell = p.grid.ncell;
+  int* count = p.count;
+  int* start = p.s.cell_start;
   const int t = threadIdx.x, nt = blockDim.x;
   const int per = (ncell + nt - 1) / nt;
   const int b = t * per, e = min(ncell, b + per);
@@ -102,24 +114,26 @@ __global__ void __launch_bounds__(1024) k_cell_scan(int ncell, int* __restrict__
   if (t == nt - 1) start[ncell] = run;
 }
 
-__global__ void k_cell_scatter(int n, const int* __restrict__ cellOf, const int* __restrict__ start,
-                               int* __restrict__ fill, int* __restrict__ tmp, const StepFlags* flags) {
-  if (skip(flags)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int c = cellOf[i];
-  tmp[start[c] + atomicAdd(&fill[c], 1)] = i;
+__device__ __forceinline__ void cell_scatter(const CellParams& p, int bx) {
+  if (skip(p.flags) || p.grid.ncx == 1) return;
+  const int i = bx * kCellThreads + threadIdx.x;
+  if (i >= p.n) return;
+  const int c = p.cellOf[i];
+  p.tmp[p.s.cell_start[c] + atomicAdd(&p.count[c], 1)] = i;
 }
 
 // One warp per cell: rank of each element = number of smaller indices in the
 // segment (indices are distinct), so perm is the segment sorted ascending.
-__global__ void k_cell_sort(int ncell, const int* __restrict__ start, const int* __restrict__ tmp,
-                            int* __restrict__ perm, const StepFlags* flags) {
-  if (skip(flags)) return;
-  int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (c >= ncell) return;
-  int s = start[c], e = start[c + 1], len = e - s;
+// The cell's fill counter is zeroed for the next build.
+__device__ __forceinline__ void cell_sort(const CellParams& p, int bx) {
+  if (skip(p.flags) || p.grid.ncx == 1) return;
+  const int c = (bx * kCellThreads + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= p.grid.ncell) return;
+  const int* tmp = p.tmp;
+  int* perm = p.s.perm;
+  const int s = p.s.cell_start[c], e = p.s.cell_start[c + 1], len = e - s;
+  if (lane == 0) p.count[c] = 0;
   if (len <= 32) {
     int v = lane < len ? tmp[s + lane] : 0x7fffffff;
     int r = 0;
@@ -134,38 +148,30 @@ __global__ void k_cell_sort(int ncell, const int* __restrict__ start, const int*
   }
 }
 
-__global__ void k_identity(int n, int* __restrict__ perm, const StepFlags* flags) {
-  if (skip(flags)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) perm[i] = i;
-}
-
 // Sorted views.  Fixed point: x_fix = round(x_box * 2^32) as a wrapping
 // 32-bit integer, so x_fix[j] - x_fix[i] (mod 2^32) is the minimum-image
 // difference in units of L / 2^32 (about 4e-16 m at L = 1.7 um).  On a
 // rebuild the particle positions are recorded as the list's reference.
 template <typename T>
-__global__ void k_sorted_fill(int n, double invL, const double* __restrict__ pos, const double* __restrict__ mm,
-                              const double* __restrict__ magMom_u, const double* __restrict__ rMag_u,
-                              const int* __restrict__ cellOf, SortedView s, double* __restrict__ xbuild,
-                              const StepFlags* flags) {
+__device__ __forceinline__ void sorted_fill(const CellParams& p, int bx) {
   using T4 = typename V4<T>::t;
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = bx * kCellThreads + threadIdx.x, n = p.n;
   if (k >= n) return;
-  int i = s.perm[k];
-  const bool rb = !flags || flags->rebuild;
-  const double px = pos[i], py = pos[n + i], pz = pos[2 * n + i];
+  const SortedView& s = p.s;
+  const int i = s.perm[k];
+  const bool rb = !p.flags || p.flags->rebuild;
+  const double px = p.pos[i], py = p.pos[n + i], pz = p.pos[2 * n + i];
   if (rb) {
     s.rank[i] = k;
-    s.cell[k] = cellOf[i];
-    if (xbuild) {
-      xbuild[i] = px;
-      xbuild[n + i] = py;
-      xbuild[2 * n + i] = pz;
+    s.cell[k] = p.cellOf[i];
+    if (p.xbuild) {
+      p.xbuild[i] = px;
+      p.xbuild[n + i] = py;
+      p.xbuild[2 * n + i] = pz;
     }
   }
-  double x = wrap_box(px, invL), y = wrap_box(py, invL), z = wrap_box(pz, invL);
-  double rm = rMag_u[i];
+  const double x = wrap_box(px, p.invL), y = wrap_box(py, p.invL), z = wrap_box(pz, p.invL);
+  const double rm = p.rMag_u[i];
   s.xf[k] = make_float4((float)x, (float)y, (float)z, (float)rm);
   if constexpr (std::is_same<T, float>::value) {
     const double sc = 4294967296.0;
@@ -174,14 +180,66 @@ __global__ void k_sorted_fill(int n, double invL, const double* __restrict__ pos
   } else {
     s.xd[k] = make_double4_32a(x, y, z, rm);
   }
-  double mu = magMom_u[i];
+  const double mu = p.magMom_u[i];
   T4 m;
-  m.x = (T)(mm[i] * mu);
-  m.y = (T)(mm[n + i] * mu);
-  m.z = (T)(mm[2 * n + i] * mu);
+  m.x = (T)(p.mm[i] * mu);
+  m.y = (T)(p.mm[n + i] * mu);
+  m.z = (T)(p.mm[2 * n + i] * mu);
   m.w = (T)rm;
   ((T4*)s.mu)[k] = m;
 }
+
+// ------------------------------------------------------------ one system
+
+__global__ void k_step_begin(StepFlags* f, float half_skin) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) step_begin(f, half_skin);
+}
+__global__ void __launch_bounds__(kCellThreads) k_cell_assign(CellParams p) { cell_assign(p, blockIdx.x); }
+__global__ void __launch_bounds__(1024) k_cell_scan(CellParams p) { cell_scan(p); }
+__global__ void __launch_bounds__(kCellThreads) k_cell_scatter(CellParams p) { cell_scatter(p, blockIdx.x); }
+__global__ void __launch_bounds__(kCellThreads) k_cell_sort(CellParams p) { cell_sort(p, blockIdx.x); }
+template <typename T>
+__global__ void __launch_bounds__(kCellThreads) k_sorted_fill(CellParams p) {
+  sorted_fill<T>(p, blockIdx.x);
+}
+
+// ---------------------------------------------------------------- packed
+
+__global__ void k_step_begin_packed(const CellParams* __restrict__ ps, int R) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < R) step_begin(ps[r].flags, ps[r].half_skin);
+}
+__global__ void __launch_bounds__(kCellThreads) k_cell_assign_packed(const CellParams* __restrict__ ps,
+                                                                     const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const CellParams p = ps[t.rep];
+  cell_assign(p, t.blk);
+}
+__global__ void __launch_bounds__(1024) k_cell_scan_packed(const CellParams* __restrict__ ps) {
+  const CellParams p = ps[blockIdx.x];
+  cell_scan(p);
+}
+__global__ void __launch_bounds__(kCellThreads) k_cell_scatter_packed(const CellParams* __restrict__ ps,
+                                                                      const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const CellParams p = ps[t.rep];
+  cell_scatter(p, t.blk);
+}
+__global__ void __launch_bounds__(kCellThreads) k_cell_sort_packed(const CellParams* __restrict__ ps,
+                                                                   const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const CellParams p = ps[t.rep];
+  cell_sort(p, t.blk);
+}
+template <typename T>
+__global__ void __launch_bounds__(kCellThreads) k_sorted_fill_packed(const CellParams* __restrict__ ps,
+                                                                     const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const CellParams p = ps[t.rep];
+  sorted_fill<T>(p, t.blk);
+}
+
+// -------------------------------------------------------- other kernels
 
 // Moments for an explicit set of directions (CompDemagField input).
 template <typename T>
@@ -218,6 +276,11 @@ __global__ void k_disp_check(int n, const double* __restrict__ pos, const double
   if ((threadIdx.x & 31) == 0 && d > 0.f) atomicMax(&f->maxdisp, __float_as_uint(d));
 }
 
+// ------------------------------------------------------------- launchers
+
+int cell_blocks(int n) { return (n + kCellThreads - 1) / kCellThreads; }
+int cell_sort_blocks(const CellGrid& g) { return g.ncx == 1 ? 0 : (g.ncell * 32 + kCellThreads - 1) / kCellThreads; }
+
 int launch_disp_check(cudaStream_t st, int n, const double* pos, const double* xbuild, double L, StepFlags* flags) {
   k_disp_check<<<(n + 255) / 256, 256, 0, st>>>(n, pos, xbuild, L, flags);
   return 1;
@@ -228,30 +291,49 @@ int launch_step_begin(cudaStream_t st, StepFlags* flags, double half_skin) {
   return 1;
 }
 
-int launch_cells(cudaStream_t st, int n, const double* pos, const double* mm, const double* magMom_u,
-                 const double* rMag_u, double L, const CellGrid& g, int* cellOf, int* count, int* tmp,
-                 const SortedView& s, bool fp64, double* xbuild, const StepFlags* flags) {
-  const int tb = 256, nb = (n + tb - 1) / tb;
-  int launches = 0;
-  double invL = 1.0 / L;
-  if (g.ncx == 1) {
-    // all-pairs: one cell holding every particle in index order
-    k_identity<<<nb, tb, 0, st>>>(n, s.perm, flags);
-    k_cell_assign<<<nb, tb, 0, st>>>(n, pos, invL, 1, cellOf, nullptr, flags);
-    launches += 2;
-  } else {
-    cudaMemsetAsync(count, 0, sizeof(int) * g.ncell, st);
-    k_cell_assign<<<nb, tb, 0, st>>>(n, pos, invL, g.ncx, cellOf, count, flags);
-    k_cell_scan<<<1, 1024, 0, st>>>(g.ncell, count, s.cell_start, flags);
-    k_cell_scatter<<<nb, tb, 0, st>>>(n, cellOf, s.cell_start, count, tmp, flags);
-    k_cell_sort<<<(g.ncell * 32 + 255) / 256, 256, 0, st>>>(g.ncell, s.cell_start, tmp, s.perm, flags);
-    launches += 4;
+int launch_cells(cudaStream_t st, const CellParams& p, bool fp64) {
+  const int nb = cell_blocks(p.n);
+  int launches = 1;
+  k_cell_assign<<<nb, kCellThreads, 0, st>>>(p);
+  if (p.grid.ncx > 1) {
+    k_cell_scan<<<1, 1024, 0, st>>>(p);
+    k_cell_scatter<<<nb, kCellThreads, 0, st>>>(p);
+    k_cell_sort<<<cell_sort_blocks(p.grid), kCellThreads, 0, st>>>(p);
+    launches += 3;
   }
   if (fp64)
-    k_sorted_fill<double><<<nb, tb, 0, st>>>(n, invL, pos, mm, magMom_u, rMag_u, cellOf, s, xbuild, flags);
+    k_sorted_fill<double><<<nb, kCellThreads, 0, st>>>(p);
   else
-    k_sorted_fill<float><<<nb, tb, 0, st>>>(n, invL, pos, mm, magMom_u, rMag_u, cellOf, s, xbuild, flags);
+    k_sorted_fill<float><<<nb, kCellThreads, 0, st>>>(p);
   return launches + 1;
+}
+
+int launch_step_begin_packed(cudaStream_t st, const CellParams* ps, int R) {
+  k_step_begin_packed<<<(R + 127) / 128, 128, 0, st>>>(ps, R);
+  return 1;
+}
+
+int launch_cells_packed(cudaStream_t st, const CellParams* ps, int R, const Packed& n256, const Packed& sort) {
+  int l = 0;
+  if (n256.n) {
+    k_cell_assign_packed<<<n256.n, kCellThreads, 0, st>>>(ps, n256.tasks);
+    l++;
+  }
+  k_cell_scan_packed<<<R, 1024, 0, st>>>(ps);
+  l++;
+  if (n256.n) {
+    k_cell_scatter_packed<<<n256.n, kCellThreads, 0, st>>>(ps, n256.tasks);
+    l++;
+  }
+  if (sort.n) {
+    k_cell_sort_packed<<<sort.n, kCellThreads, 0, st>>>(ps, sort.tasks);
+    l++;
+  }
+  if (n256.n) {
+    k_sorted_fill_packed<float><<<n256.n, kCellThreads, 0, st>>>(ps, n256.tasks);
+    l++;
+  }
+  return l;
 }
 
 int launch_set_mu(cudaStream_t st, int n, const double* mm, const double* magMom_u, const double* rMag_u,

@@ -53,6 +53,33 @@ struct StepFlags {
   unsigned maxdisp;   // float bits of the largest displacement since the build (box units)
 };
 
+// Cell-list build of one system (positions in particle order, FP64).
+struct CellParams {
+  int n;
+  double invL;
+  CellGrid grid;
+  float half_skin;          // rebuild threshold: half the list skin, box units
+  const double* pos;
+  const double* mm;
+  const double* magMom_u;
+  const double* rMag_u;
+  int* cellOf;
+  int* count;               // [ncell] zero between builds
+  int* tmp;
+  SortedView s;
+  double* xbuild;           // positions at the last build (may be null)
+  StepFlags* flags;
+};
+
+// A packed launch runs one kernel over the blocks of several independent
+// systems: block b of the grid executes block tasks[b].blk of system
+// tasks[b].rep, with that system's parameters.  The kernel bodies are the
+// same as for a single system, so every system gets the same results alone
+// and packed.
+struct Task {
+  int rep, blk;
+};
+
 // ------------------------------------------------------- real space
 struct RealParams {
   int n;
@@ -82,7 +109,7 @@ struct RealParams {
   int* nbr_cnt;               // [n]
   int* nbr_off;               // [n + 1]
   long long nbr_cap;
-  const StepFlags* flags;     // rebuild / overflow
+  StepFlags* flags;           // rebuild / overflow
 };
 
 // --------------------------------------------------------- k space
@@ -162,6 +189,10 @@ struct ObsParams {
   double* records;           // [cap][8]
   long long* nrec;
   long long cap;
+  // packed runs: the system's error word and list overflow, copied to status
+  const int* err;
+  const StepFlags* flags;
+  int* status;               // may be null
 };
 
 // ------------------------------------------------------ device helpers

@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -21,8 +22,7 @@
 #include "md_common.cuh"
 #include "md_host.h"
 #include "md_kernels.h"
-
-using namespace md;
+#include "md_ctx_internal.h"
 
 namespace {
 
@@ -30,91 +30,7 @@ std::mutex g_err_mu;
 std::string g_err;
 int g_err_status = 0;
 
-struct DevScalars {
-  double time;
-  long long step;
-  long long nrec;
-  int err;
-  int pad;
-  double musum[3];
-  unsigned long long pairs;
-  StepFlags flags;
-};
-
 }  // namespace
-
-struct md_ctx {
-  md_config cfg{};
-  int64_t n = 0;
-  int prec = MD_PREC_MIXED;
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  int err_status = 0;
-  std::vector<void*> allocs;
-  int64_t bytes = 0;
-
-  // host state
-  mdh::Props props;
-  bool have_particles = false, have_state = false, have_ewald = false, have_geometry = false;
-  double L = 0, alpha = 0, rc = 0;
-  int64_t kc = 0;
-  CellGrid grid{1, 1, 0};
-  mdh::KList klist;
-  int nchunk = 1, chunk = 0;
-  int noise = MD_NOISE_PHILOX;
-  uint64_t seed = 1;
-  double cur_dt = -1;
-  bool graph_valid = false;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  int64_t launches = 0, launches_per_step = 0;
-
-  // device: master state & particle constants
-  double *pos = nullptr, *mm = nullptr, *ea = nullptr, *truePos = nullptr, *posRef = nullptr;
-  double *xi = nullptr, *tmpmm = nullptr, *Bout = nullptr, *Fout = nullptr;
-  double *magMom_u = nullptr, *rMag_u = nullptr, *invZt = nullptr, *velEa1 = nullptr, *velEa2 = nullptr;
-  double *sT = nullptr, *sB = nullptr, *sF = nullptr;
-  // cells and sorted views
-  int *cellOf = nullptr, *tmp = nullptr, *perm = nullptr, *rank = nullptr, *scell = nullptr;
-  int *count = nullptr, *cell_start = nullptr;
-  int ncell_cap = 0;
-  float4* xf = nullptr;
-  int4* xi4 = nullptr;
-  double4_32a* xd = nullptr;
-  void* mu = nullptr;
-  // stage outputs (T)
-  void *Br = nullptr, *Fr = nullptr, *ov = nullptr, *Bk = nullptr, *Fk = nullptr, *Br2 = nullptr, *Bk2 = nullptr;
-  void *k1m = nullptr, *k1e = nullptr, *m2 = nullptr, *e2 = nullptr, *th = nullptr;
-  double *Ppart = nullptr, *obs_part = nullptr;
-  DevScalars* sc = nullptr;
-  double* records = nullptr;
-  long long rec_cap = 0;
-  // k space
-  KSeg* kseg = nullptr;
-  int* koff = nullptr;
-  double* ek = nullptr;
-  KSeg* rseg = nullptr;
-  int* rowpos = nullptr;
-  int2* chunks = nullptr;
-  double2* Spart = nullptr;
-  double* musum_part = nullptr;
-  void* eS = nullptr;
-  double2* Sfull = nullptr;
-  void* ptab = nullptr;  // phase tables [3][kc+1][n]
-  size_t ptab_cap = 0;
-  size_t ksize_cap = 0, spart_cap = 0;
-  int musum_cap = 0;
-  // Verlet list (sorted indices) within rc + skin
-  int *nbr = nullptr, *nbr_cnt = nullptr, *nbr_off = nullptr;
-  long long nbr_cap = 0;
-  double* xbuild = nullptr;
-  double skin_frac = 0.02;  // skin = skin_frac * rc
-  bool list_valid = false;  // a build for the current particles, grid and skin exists
-  // profiling: events between the kernel segments of a step
-  bool prof = false;
-  cudaEvent_t ev[MD_NSEG + 1] = {};
-};
 
 // Records the boundary event `k` when profiling.
 static void mark(md_ctx* c, int k) {
@@ -123,7 +39,7 @@ static void mark(md_ctx* c, int k) {
 
 // ------------------------------------------------------------- helpers
 
-static int set_err(md_ctx* c, int status, const char* fmt, ...) {
+int set_err(md_ctx* c, int status, const char* fmt, ...) {
   char buf[1024];
   va_list ap;
   va_start(ap, fmt);
@@ -139,16 +55,8 @@ static int set_err(md_ctx* c, int status, const char* fmt, ...) {
   return status;
 }
 
-#define CK(ctx, call)                                                                              \
-  do {                                                                                             \
-    cudaError_t e_ = (call);                                                                       \
-    if (e_ != cudaSuccess)                                                                         \
-      return set_err(ctx, MD_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
-                     __FILE__, __LINE__);                                                          \
-  } while (0)
 
-template <typename P>
-static int dalloc(md_ctx* c, P** p, size_t bytes) {
+int dalloc_raw(md_ctx* c, void** p, size_t bytes) {
   void* q = nullptr;
   if (bytes == 0) bytes = 16;
   cudaError_t e = cudaMalloc(&q, bytes);
@@ -156,21 +64,21 @@ static int dalloc(md_ctx* c, P** p, size_t bytes) {
     return set_err(c, MD_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
   c->allocs.push_back(q);
   c->bytes += (int64_t)bytes;
-  *p = (P*)q;
+  *p = q;
   return MD_OK;
 }
 
-static void dfree(md_ctx* c, void* p) {
+void dfree(md_ctx* c, void* p) {
   if (!p) return;
   auto it = std::find(c->allocs.begin(), c->allocs.end(), p);
   if (it != c->allocs.end()) c->allocs.erase(it);
   cudaFree(p);
 }
 
-static bool fp64(const md_ctx* c) { return c->prec == MD_PREC_FP64; }
-static size_t tsz(const md_ctx* c) { return fp64(c) ? 8 : 4; }
+bool fp64(const md_ctx* c) { return c->prec == MD_PREC_FP64; }
+size_t tsz(const md_ctx* c) { return fp64(c) ? 8 : 4; }
 
-static void invalidate_graph(md_ctx* c) {
+void invalidate_graph(md_ctx* c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->graph) cudaGraphDestroy(c->graph);
   c->gexec = nullptr;
@@ -178,7 +86,7 @@ static void invalidate_graph(md_ctx* c) {
   c->graph_valid = false;
 }
 
-static SortedView sorted_view(md_ctx* c) {
+SortedView sorted_view(md_ctx* c) {
   SortedView s;
   s.xf = c->xf;
   s.xi = c->xi4;
@@ -191,10 +99,10 @@ static SortedView sorted_view(md_ctx* c) {
   return s;
 }
 
-static double B_unit(const md_ctx* c) { return c->cfg.facEwald * c->props.muMax / std::pow(c->L, 3.0); }
-static double F_unit(const md_ctx* c) { return c->cfg.facEwald * c->props.muMax * c->props.muMax / std::pow(c->L, 4.0); }
+double B_unit(const md_ctx* c) { return c->cfg.facEwald * c->props.muMax / std::pow(c->L, 3.0); }
+double F_unit(const md_ctx* c) { return c->cfg.facEwald * c->props.muMax * c->props.muMax / std::pow(c->L, 4.0); }
 
-static RealParams real_params(md_ctx* c, void* B, void* F, void* ov) {
+RealParams real_params(md_ctx* c, void* B, void* F, void* ov) {
   RealParams p{};
   const md_config& g = c->cfg;
   const double L = c->L, a = c->alpha * L, rcb = c->rc / L;
@@ -211,7 +119,7 @@ static RealParams real_params(md_ctx* c, void* B, void* F, void* ov) {
   p.cont_eps = 1e-10 / L;
   p.coat = (int)g.ENABLE_COATING_POT;
   const double Fu = F_unit(c);
-  p.rcut_sr2 = std::pow(c->props.rCutSR / L, 2.0);
+  p.rcut_sr2 = g.ENABLE_COATING_POT ? std::pow(c->props.rCutSR / L, 2.0) : -1.0;
   p.eff_len = g.effLenSurfMol / L;
   p.ster = g.sterRepFac * L * L / Fu;
   p.elec = g.electrostatRepFac * L / Fu;
@@ -235,7 +143,44 @@ static RealParams real_params(md_ctx* c, void* B, void* F, void* ov) {
   return p;
 }
 
-static KParams k_params(md_ctx* c, void* B, void* F) {
+CellParams cell_params(md_ctx* c) {
+  CellParams p{};
+  p.n = (int)c->n;
+  p.invL = 1.0 / c->L;
+  p.grid = c->grid;
+  p.half_skin = (float)(0.5 * c->skin_frac * c->rc / c->L);
+  p.pos = c->pos;
+  p.mm = c->mm;
+  p.magMom_u = c->magMom_u;
+  p.rMag_u = c->rMag_u;
+  p.cellOf = c->cellOf;
+  p.count = c->count;
+  p.tmp = c->tmp;
+  p.s = sorted_view(c);
+  p.xbuild = c->xbuild;
+  p.flags = &c->sc->flags;
+  return p;
+}
+
+ObsParams obs_params(md_ctx* c, double dt) {
+  ObsParams o{};
+  o.nblk_int = int_blocks((int)c->n);
+  o.obs_part = c->obs_part;
+  o.p_scale = c->L * F_unit(c) / (2.0 * std::pow(c->L, 3.0));
+  o.inv_n = 1.0 / (double)c->n;
+  o.dt = dt;
+  o.time = &c->sc->time;
+  o.stepno = &c->sc->step;
+  o.records = c->records;
+  o.nrec = &c->sc->nrec;
+  o.cap = c->rec_cap;
+  o.err = &c->sc->err;
+  o.flags = &c->sc->flags;
+  o.status = nullptr;
+  return o;
+}
+
+KParams k_params(md_ctx* c, void* B, void* F) {
   KParams p{};
   p.n = (int)c->n;
   p.kc = (int)c->kc;
@@ -265,7 +210,7 @@ static KParams k_params(md_ctx* c, void* B, void* F) {
   return p;
 }
 
-static IntParams int_params(md_ctx* c, double dt, const void* Br, const void* Bk) {
+IntParams int_params(md_ctx* c, double dt, const void* Br, const void* Bk) {
   IntParams p{};
   const md_config& g = c->cfg;
   const double a = c->alpha * c->L;
@@ -323,7 +268,7 @@ static IntParams int_params(md_ctx* c, double dt, const void* Br, const void* Bk
   return p;
 }
 
-static int check_ready(md_ctx* c, bool need_state) {
+int check_ready(md_ctx* c, bool need_state) {
   if (!c) return set_err(nullptr, MD_ERR_INVALID, "null context");
   if (!c->have_particles) return set_err(c, MD_ERR_INVALID, "particles not set (md_set_particles)");
   if (!c->have_ewald) return set_err(c, MD_ERR_INVALID, "Ewald parameters not set (md_set_ewald)");
@@ -334,12 +279,10 @@ static int check_ready(md_ctx* c, bool need_state) {
 // Field + force evaluation on the current master state (no integrator).
 static int issue_interactions(md_ctx* c) {
   int l = 0;
-  SortedView s = sorted_view(c);
   mark(c, MD_SEG_CELLS);
-  const double half_skin = 0.5 * c->skin_frac * c->rc / c->L;
-  l += launch_step_begin(c->stream, &c->sc->flags, half_skin);
-  l += launch_cells(c->stream, (int)c->n, c->pos, c->mm, c->magMom_u, c->rMag_u, c->L, c->grid, c->cellOf, c->count,
-                    c->tmp, s, fp64(c), c->xbuild, &c->sc->flags);
+  const CellParams cp = cell_params(c);
+  l += launch_step_begin(c->stream, cp.flags, cp.half_skin);
+  l += launch_cells(c->stream, cp, fp64(c));
   cudaMemsetAsync(&c->sc->pairs, 0, sizeof(unsigned long long), c->stream);
   l += launch_nbr(c->stream, real_params(c, nullptr, nullptr, nullptr), &c->sc->flags, fp64(c));
   l += launch_phase_tables(c->stream, k_params(c, nullptr, nullptr), fp64(c));
@@ -364,31 +307,20 @@ static int issue_step(md_ctx* c, double dt) {
   mark(c, MD_SEG_HEUN2);
   l += launch_heun2(c->stream, int_params(c, dt, c->Br2, c->Bk2), fp64(c));
   mark(c, MD_SEG_OBS);
-  ObsParams o{};
-  o.nblk_int = int_blocks((int)c->n);
-  o.obs_part = c->obs_part;
-  o.p_scale = c->L * F_unit(c) / (2.0 * std::pow(c->L, 3.0));
-  o.inv_n = 1.0 / (double)c->n;
-  o.dt = dt;
-  o.time = &c->sc->time;
-  o.stepno = &c->sc->step;
-  o.records = c->records;
-  o.nrec = &c->sc->nrec;
-  o.cap = c->rec_cap;
-  l += launch_obs(c->stream, o);
+  l += launch_obs(c->stream, obs_params(c, dt));
   mark(c, MD_NSEG);
   return l;
 }
 
 // Asks the device to rebuild the cell order and the neighbour list at the
 // start of the next evaluation.
-static int force_rebuild(md_ctx* c) {
+int force_rebuild(md_ctx* c) {
   static const int one = 1;
   CK(c, cudaMemcpyAsync(&c->sc->flags.force, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   return MD_OK;
 }
 
-static int alloc_nbr(md_ctx* c, long long cap) {
+int alloc_nbr(md_ctx* c, long long cap) {
   cap = std::min<long long>(cap, 0x7ffffffeLL);
   if (cap <= c->nbr_cap) return MD_OK;
   dfree(c, c->nbr);
@@ -403,7 +335,7 @@ static int alloc_nbr(md_ctx* c, long long cap) {
 
 // After work on the stream: a neighbour list that did not fit was replaced by
 // the direct cell scan (results are correct); grow it for the next steps.
-static int check_overflow(md_ctx* c) {
+int check_overflow(md_ctx* c) {
   StepFlags f;
   CK(c, cudaMemcpyAsync(&f, &c->sc->flags, sizeof f, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
@@ -418,7 +350,7 @@ static int check_overflow(md_ctx* c) {
   return force_rebuild(c);
 }
 
-static int read_err_word(md_ctx* c) {
+int read_err_word(md_ctx* c) {
   int e = 0;
   CK(c, cudaMemcpyAsync(&e, &c->sc->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
@@ -766,6 +698,8 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
     int st;
     if ((st = dalloc(c, &c->count, 4 * (size_t)(ncell + 1)))) return st;
     if ((st = dalloc(c, &c->cell_start, 4 * (size_t)(ncell + 1)))) return st;
+    // the cell fill counters are zero between builds (the build leaves them so)
+    CK(c, cudaMemset(c->count, 0, 4 * (size_t)(ncell + 1)));
     c->ncell_cap = ncell + 1;
   }
   if (c->grid.ncx == 1) {
@@ -882,7 +816,9 @@ int md_set_noise(md_ctx* c, int mode, uint64_t seed) {
   return MD_OK;
 }
 
-static int ensure_records(md_ctx* c, int64_t extra) {
+}  // extern "C"
+
+int ensure_records(md_ctx* c, int64_t extra) {
   long long nrec = 0;
   CK(c, cudaMemcpy(&nrec, &c->sc->nrec, sizeof nrec, cudaMemcpyDeviceToHost));
   if (nrec + extra <= c->rec_cap) return MD_OK;
@@ -898,23 +834,29 @@ static int ensure_records(md_ctx* c, int64_t extra) {
   return MD_OK;
 }
 
+int prepare_dt(md_ctx* c, double dt) {
+  if (dt == c->cur_dt) return MD_OK;
+  std::vector<double> a, b, d;
+  mdh::noise_scales(c->cfg, c->props, dt, &a, &b, &d);
+  const size_t N8 = 8 * (size_t)c->n;
+  CK(c, cudaMemcpyAsync(c->sT, a.data(), N8, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->sB, b.data(), N8, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->sF, d.data(), N8, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->cur_dt = dt;
+  invalidate_graph(c);
+  return MD_OK;
+}
+
+extern "C" {
+
 int md_step(md_ctx* c, int64_t nsteps, double dt, const double* xi) {
   int st = check_ready(c, true);
   if (st) return st;
   if (nsteps < 0 || !(dt > 0)) return set_err(c, MD_ERR_INVALID, "bad nsteps or dt");
   if (c->noise == MD_NOISE_UPLOADED && !xi) return set_err(c, MD_ERR_INVALID, "uploaded noise needs xi");
   if (nsteps == 0) return MD_OK;
-  if (dt != c->cur_dt) {
-    std::vector<double> a, b, d;
-    mdh::noise_scales(c->cfg, c->props, dt, &a, &b, &d);
-    const size_t N8 = 8 * (size_t)c->n;
-    CK(c, cudaMemcpyAsync(c->sT, a.data(), N8, cudaMemcpyHostToDevice, c->stream));
-    CK(c, cudaMemcpyAsync(c->sB, b.data(), N8, cudaMemcpyHostToDevice, c->stream));
-    CK(c, cudaMemcpyAsync(c->sF, d.data(), N8, cudaMemcpyHostToDevice, c->stream));
-    CK(c, cudaStreamSynchronize(c->stream));
-    c->cur_dt = dt;
-    invalidate_graph(c);
-  }
+  if ((st = prepare_dt(c, dt))) return st;
   if ((st = ensure_records(c, nsteps))) return st;
   if (c->noise == MD_NOISE_UPLOADED) {
     c->launches = 0;
@@ -1152,6 +1094,87 @@ int md_autotune_ewald(md_ctx* c, int ncand, double* alpha_out, double* rc_out, i
   if (rc_out) *rc_out = brc;
   if (kc_out) *kc_out = bk;
   if (best_ms) *best_ms = best;
+  return MD_OK;
+}
+
+// Ewald cutoff cache per (N, volume fraction) bucket: N in half octaves,
+// volume fraction in steps of 0.01.
+namespace {
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, double> g_tune;  // bucket -> rc / L
+std::pair<int, int> tune_key(int64_t n, double volFrac) {
+  return {(int)std::floor(2.0 * std::log2((double)n)), (int)std::lround(volFrac * 100.0)};
+}
+}  // namespace
+
+int md_autotune_ewald_cached(md_ctx* c, double volFrac, double* alpha, double* rc, int64_t* kc, int* hit) {
+  if (!c || !c->have_particles || !c->have_state) return set_err(c, MD_ERR_INVALID, "particles or state not set");
+  const auto key = tune_key(c->n, volFrac);
+  double x = -1;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) x = it->second;
+  }
+  if (hit) *hit = x > 0;
+  if (x > 0) {
+    mdh::EwaldModel m = mdh::ewald_model(c->cfg, c->props);
+    double a = 0, kr = 0;
+    if (mdh::ewald_for_rc(c->cfg, m, x * c->L, &a, &kr)) {
+      const int64_t k = std::max<int64_t>(1, (int64_t)std::floor(kr + 0.5));
+      int st = md_set_ewald(c, a, x * c->L, k);
+      if (st == MD_OK) {
+        if (alpha) *alpha = a;
+        if (rc) *rc = x * c->L;
+        if (kc) *kc = k;
+        return MD_OK;
+      }
+    }
+    if (hit) *hit = 0;  // the cached cutoff does not fit this system: tune it
+  }
+  double a = 0, r = 0;
+  int64_t k = 0;
+  int st = md_autotune_ewald(c, 5, &a, &r, &k, nullptr);
+  if (st) return st;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = r / c->L;
+  }
+  if (alpha) *alpha = a;
+  if (rc) *rc = r;
+  if (kc) *kc = k;
+  return MD_OK;
+}
+
+int md_tune_cache_save(const char* path) {
+  if (!path) return set_err(nullptr, MD_ERR_INVALID, "null path");
+  FILE* f = std::fopen(path, "w");
+  if (!f) return set_err(nullptr, MD_ERR_INVALID, "cannot write %s", path);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::fprintf(f, "# n_bucket(2*log2 N) volfrac_bucket(x100) rc_over_L\n");
+  for (const auto& kv : g_tune) std::fprintf(f, "%d %d %.17g\n", kv.first.first, kv.first.second, kv.second);
+  std::fclose(f);
+  return MD_OK;
+}
+
+int md_tune_cache_load(const char* path) {
+  if (!path) return set_err(nullptr, MD_ERR_INVALID, "null path");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return set_err(nullptr, MD_ERR_INVALID, "cannot read %s", path);
+  char line[256];
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  while (std::fgets(line, sizeof line, f)) {
+    int a = 0, b = 0;
+    double x = 0;
+    if (line[0] != '#' && std::sscanf(line, "%d %d %lf", &a, &b, &x) == 3 && x > 0 && x <= 0.5) g_tune[{a, b}] = x;
+  }
+  std::fclose(f);
+  return MD_OK;
+}
+
+int md_tune_cache_clear(void) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
   return MD_OK;
 }
 

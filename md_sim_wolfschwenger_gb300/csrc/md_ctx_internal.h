@@ -1,0 +1,144 @@
+// md_ctx_internal.h -- the context behind the C ABI (include/md_gb300.h):
+// host bookkeeping and the device buffers of one simulated system, plus the
+// helpers shared by md_ctx.cu (one system) and md_batch.cu (packed systems).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/md_gb300.h"
+#include "md_common.cuh"
+#include "md_err.h"
+#include "md_host.h"
+
+namespace md {
+
+// Device-resident scalars of one system.
+struct DevScalars {
+  double time;
+  long long step;
+  long long nrec;
+  int err;
+  int pad;
+  double musum[3];
+  unsigned long long pairs;
+  StepFlags flags;
+};
+
+}  // namespace md
+
+using namespace md;
+
+struct md_ctx {
+  md_config cfg{};
+  int64_t n = 0;
+  int prec = MD_PREC_MIXED;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int err_status = 0;
+  std::vector<void*> allocs;
+  int64_t bytes = 0;
+
+  // host state
+  mdh::Props props;
+  bool have_particles = false, have_state = false, have_ewald = false, have_geometry = false;
+  double L = 0, alpha = 0, rc = 0;
+  int64_t kc = 0;
+  CellGrid grid{1, 1, 0};
+  mdh::KList klist;
+  int nchunk = 1, chunk = 0;
+  int noise = MD_NOISE_PHILOX;
+  uint64_t seed = 1;
+  double cur_dt = -1;
+  bool graph_valid = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t launches = 0, launches_per_step = 0;
+
+  // device: master state & particle constants
+  double *pos = nullptr, *mm = nullptr, *ea = nullptr, *truePos = nullptr, *posRef = nullptr;
+  double *xi = nullptr, *tmpmm = nullptr, *Bout = nullptr, *Fout = nullptr;
+  double *magMom_u = nullptr, *rMag_u = nullptr, *invZt = nullptr, *velEa1 = nullptr, *velEa2 = nullptr;
+  double *sT = nullptr, *sB = nullptr, *sF = nullptr;
+  // cells and sorted views
+  int *cellOf = nullptr, *tmp = nullptr, *perm = nullptr, *rank = nullptr, *scell = nullptr;
+  int *count = nullptr, *cell_start = nullptr;
+  int ncell_cap = 0;
+  float4* xf = nullptr;
+  int4* xi4 = nullptr;
+  double4_32a* xd = nullptr;
+  void* mu = nullptr;
+  // stage outputs (T)
+  void *Br = nullptr, *Fr = nullptr, *ov = nullptr, *Bk = nullptr, *Fk = nullptr, *Br2 = nullptr, *Bk2 = nullptr;
+  void *k1m = nullptr, *k1e = nullptr, *m2 = nullptr, *e2 = nullptr, *th = nullptr;
+  double *Ppart = nullptr, *obs_part = nullptr;
+  DevScalars* sc = nullptr;
+  double* records = nullptr;
+  long long rec_cap = 0;
+  // k space
+  KSeg* kseg = nullptr;
+  int* koff = nullptr;
+  double* ek = nullptr;
+  KSeg* rseg = nullptr;
+  int* rowpos = nullptr;
+  int2* chunks = nullptr;
+  double2* Spart = nullptr;
+  double* musum_part = nullptr;
+  void* eS = nullptr;
+  double2* Sfull = nullptr;
+  void* ptab = nullptr;  // phase tables [3][kc+1][n]
+  size_t ptab_cap = 0;
+  size_t ksize_cap = 0, spart_cap = 0;
+  int musum_cap = 0;
+  // Verlet list (sorted indices) within rc + skin
+  int *nbr = nullptr, *nbr_cnt = nullptr, *nbr_off = nullptr;
+  long long nbr_cap = 0;
+  double* xbuild = nullptr;
+  double skin_frac = 0.02;  // skin = skin_frac * rc
+  bool list_valid = false;  // a build for the current particles, grid and skin exists
+  // profiling: events between the kernel segments of a step
+  bool prof = false;
+  cudaEvent_t ev[MD_NSEG + 1] = {};
+};
+
+// ------------------------------------------------------------ helpers
+
+#define CK(ctx, call)                                                                              \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return set_err(ctx, MD_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                     __FILE__, __LINE__);                                                          \
+  } while (0)
+
+int dalloc_raw(md_ctx* c, void** p, size_t bytes);
+template <typename P>
+inline int dalloc(md_ctx* c, P** p, size_t bytes) {
+  void* q = nullptr;
+  const int st = dalloc_raw(c, &q, bytes);
+  if (st == MD_OK) *p = (P*)q;
+  return st;
+}
+void dfree(md_ctx* c, void* p);
+bool fp64(const md_ctx* c);
+size_t tsz(const md_ctx* c);
+void invalidate_graph(md_ctx* c);
+md::SortedView sorted_view(md_ctx* c);
+double B_unit(const md_ctx* c);
+double F_unit(const md_ctx* c);
+md::CellParams cell_params(md_ctx* c);
+md::RealParams real_params(md_ctx* c, void* B, void* F, void* ov);
+md::KParams k_params(md_ctx* c, void* B, void* F);
+md::IntParams int_params(md_ctx* c, double dt, const void* Br, const void* Bk);
+md::ObsParams obs_params(md_ctx* c, double dt);
+int check_ready(md_ctx* c, bool need_state);
+int force_rebuild(md_ctx* c);
+int alloc_nbr(md_ctx* c, long long cap);
+int check_overflow(md_ctx* c);
+int ensure_records(md_ctx* c, int64_t extra);
+int read_err_word(md_ctx* c);
+// Thermal-noise scales for the step dt (DefThermFluct prefactors).
+int prepare_dt(md_ctx* c, double dt);

@@ -574,3 +574,187 @@ md::CellGrid choose_grid(double rc_box, int64_t n, int reach) {
 }
 
 }  // namespace mdh
+
+namespace mdh {
+
+// ----------------------------------------------------- initial systems
+
+namespace {
+
+// xoshiro256** (Blackman & Vigna, 2018), seeded through splitmix64.
+struct Xoshiro {
+  uint64_t s[4];
+  explicit Xoshiro(uint64_t seed) {
+    for (int i = 0; i < 4; i++) {
+      seed += 0x9E3779B97F4A7C15ull;
+      uint64_t z = seed;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      s[i] = z ^ (z >> 31);
+    }
+  }
+  static uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+  uint64_t next() {
+    const uint64_t r = rotl(s[1] * 5, 7) * 9, t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl(s[3], 45);
+    return r;
+  }
+  double uniform() { return (double)(next() >> 11) * 0x1.0p-53; }  // [0, 1)
+  double balanced() { return 2.0 * uniform() - 1.0; }              // [-1, 1)
+  double normal() {                                                 // Marsaglia polar method
+    for (;;) {
+      const double u = balanced(), v = balanced(), q = u * u + v * v;
+      if (q > 0 && q < 1) return u * std::sqrt(-2.0 * std::log(q) / q);
+    }
+  }
+};
+
+}  // namespace
+
+int init_system(const md_config& c, int64_t n, uint64_t seed, double* rMag, double* rHydr, double* pos, double* mm,
+                double* ea, double* lBox, std::string* err) {
+  if (n < 1 || !rMag || !pos || !mm || !ea) {
+    *err = "bad arguments";
+    return MD_ERR_INVALID;
+  }
+  Xoshiro rng(seed);
+  // sizes (InitParticleProps, src/simulation.cpp:162-212)
+  if (c.SIZE_DIST == 1) {
+    double mu, sl;
+    if (c.sigmaLog > 0) {
+      mu = std::log(c.rMagMean);
+      sl = c.sigmaLog;
+    } else {
+      mu = std::log(c.rMagMean * c.rMagMean / std::sqrt(c.rMagMean * c.rMagMean + c.sigma * c.sigma));
+      sl = std::sqrt(std::log(1.0 + std::pow(c.sigma / c.rMagMean, 2.0)));
+    }
+    for (int64_t i = 0; i < n; i++) rMag[i] = std::exp(mu + sl * rng.normal());
+  } else {
+    for (int64_t i = 0; i < n; i++) rMag[i] = c.rMagMean;
+  }
+  Props p;
+  int st = make_props(c, rMag, nullptr, n, &p, err);
+  if (st) return st;
+  if (rHydr)
+    for (int64_t i = 0; i < n; i++) rHydr[i] = p.rHydr[i];
+  const double L = p.lBox;
+  *lBox = L;
+  // positions (InitCoordsFromSketch, src/simulation.cpp:229-288)
+  if (c.INIT_CONFIG_TRANS == 2) {
+    const int64_t d = (int64_t)std::llround(std::cbrt((double)n));
+    if (d * d * d != n) {
+      *err = "INIT_CONFIG_TRANS = 2 needs a cubic particle count";
+      return MD_ERR_INVALID;
+    }
+    const double gap = L / (double)d;
+    int64_t ip = 0;
+    for (int64_t ix = 0; ix < d; ix++)
+      for (int64_t iy = 0; iy < d; iy++)
+        for (int64_t iz = 0; iz < d; iz++, ip++) {
+          pos[ip] = (ix + 0.5) * gap - L / 2.0;
+          pos[n + ip] = (iy + 0.5) * gap - L / 2.0;
+          pos[2 * n + ip] = (iz + 0.5) * gap - L / 2.0;
+        }
+  } else {
+    // random sequential addition on a cell grid (cells >= the largest
+    // contact distance, so a candidate only meets the 27 cells around it)
+    double rhmax = 0, rhmin = 1e300;
+    for (int64_t i = 0; i < n; i++) {
+      rhmax = std::max(rhmax, p.rHydr[i]);
+      rhmin = std::min(rhmin, p.rHydr[i]);
+    }
+    const int64_t nc = std::max<int64_t>(1, std::min<int64_t>(1024, (int64_t)std::floor(L / (2.0 * rhmax))));
+    const double cs = L / (double)nc;
+    std::vector<int64_t> head((size_t)(nc * nc * nc), -1), next((size_t)n, -1);
+    std::vector<int64_t> order((size_t)n);
+    for (int64_t i = 0; i < n; i++) order[i] = i;
+    if (rhmax > rhmin)
+      std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return p.rHydr[a] > p.rHydr[b]; });
+    auto cell_of = [&](double x) {
+      int64_t k = (int64_t)std::floor((x + L / 2.0) / cs);
+      return std::min<int64_t>(nc - 1, std::max<int64_t>(0, k));
+    };
+    const int64_t max_tries = 2000000;
+    for (int64_t q = 0; q < n; q++) {
+      const int64_t i = order[q];
+      const double ri = p.rHydr[i], ext = L / 2.0 - ri;
+      bool placed = false;
+      for (int64_t t = 0; t < max_tries && !placed; t++) {
+        const double x = rng.balanced() * ext, y = rng.balanced() * ext, z = rng.balanced() * ext;
+        const int64_t cx = cell_of(x), cy = cell_of(y), cz = cell_of(z);
+        bool ok = true;
+        for (int64_t dz = -1; dz <= 1 && ok; dz++)
+          for (int64_t dy = -1; dy <= 1 && ok; dy++)
+            for (int64_t dx = -1; dx <= 1 && ok; dx++) {
+              const int64_t ux = cx + dx, uy = cy + dy, uz = cz + dz;
+              if (ux < 0 || uy < 0 || uz < 0 || ux >= nc || uy >= nc || uz >= nc) continue;
+              for (int64_t j = head[(size_t)((uz * nc + uy) * nc + ux)]; j >= 0; j = next[(size_t)j]) {
+                const double ddx = pos[j] - x, ddy = pos[n + j] - y, ddz = pos[2 * n + j] - z;
+                const double rr = ri + p.rHydr[j];
+                if (ddx * ddx + ddy * ddy + ddz * ddz < rr * rr) {
+                  ok = false;
+                  break;
+                }
+              }
+            }
+        if (ok) {
+          pos[i] = x;
+          pos[n + i] = y;
+          pos[2 * n + i] = z;
+          const size_t cell = (size_t)((cz * nc + cy) * nc + cx);
+          next[(size_t)i] = head[cell];
+          head[cell] = i;
+          placed = true;
+        }
+      }
+      if (!placed) {
+        *err = "random sequential addition failed: volume fraction too high";
+        return MD_ERR_INVALID;
+      }
+    }
+  }
+  // orientations (src/simulation.cpp:292-349): azimuth 2 pi u, elevation
+  // 2 asin(sqrt(u)) -- uniform on the sphere
+  auto draw = [&](double* v) {
+    for (int64_t i = 0; i < n; i++) {
+      const double az = rng.uniform() * 2.0 * c.my_pi;
+      const double el = 2.0 * std::asin(std::sqrt(rng.uniform()));
+      v[i] = std::sin(el) * std::cos(az);
+      v[n + i] = std::sin(el) * std::sin(az);
+      v[2 * n + i] = std::cos(el);
+    }
+  };
+  auto set_z = [&](double* v) {
+    for (int64_t i = 0; i < n; i++) {
+      v[i] = 0.0;
+      v[n + i] = 0.0;
+      v[2 * n + i] = 1.0;
+    }
+  };
+  switch (c.INIT_CONFIG_ROT) {
+    case 1:
+      draw(ea);
+      set_z(mm);
+      break;
+    case 3:
+      set_z(ea);
+      std::copy(ea, ea + 3 * n, mm);
+      break;
+    case 4:
+      draw(ea);
+      draw(mm);
+      break;
+    default:
+      draw(ea);
+      std::copy(ea, ea + 3 * n, mm);
+      break;
+  }
+  return MD_OK;
+}
+
+}  // namespace mdh

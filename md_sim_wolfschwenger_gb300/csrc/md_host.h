@@ -67,6 +67,11 @@ struct KList {
 };
 KList build_klist(int kc, double w);
 
+// ------------------------------------------------------ initial systems
+// Sizes, box, positions and orientations of a new system (md_init_system).
+int init_system(const md_config& c, int64_t n, uint64_t seed, double* rMag, double* rHydr, double* pos, double* mm,
+                double* ea, double* lBox, std::string* err);
+
 // ----------------------------------------------------------- cell grid
 md::CellGrid choose_grid(double rc_box, int64_t n, int reach);
 

@@ -86,9 +86,9 @@ __device__ __forceinline__ void demag_si(const IntParams& p, int r, T b[3]) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kIntThreads) k_heun1(IntParams p) {
+__device__ __forceinline__ void heun1(const IntParams& p, int bx) {
   using T4 = typename V4<T>::t;
-  const int i = blockIdx.x * kIntThreads + threadIdx.x;
+  const int i = bx * kIntThreads + threadIdx.x;
   const int n = p.n;
   if (i >= n) return;
   const int r = p.s.rank[i];
@@ -146,8 +146,8 @@ __global__ void __launch_bounds__(kIntThreads) k_heun1(IntParams p) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kIntThreads) k_heun2(IntParams p) {
-  const int i = blockIdx.x * kIntThreads + threadIdx.x;
+__device__ __forceinline__ void heun2(const IntParams& p, int bx) {
+  const int i = bx * kIntThreads + threadIdx.x;
   const int n = p.n;
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   double disp2 = 0;  // squared displacement since the last neighbour-list build
@@ -230,11 +230,11 @@ __global__ void __launch_bounds__(kIntThreads) k_heun2(IntParams p) {
   if (threadIdx.x < 7) {
     double s = 0;
     for (int w = 0; w < kIntThreads / 32; w++) s += red[threadIdx.x][w];
-    p.obs_part[7 * blockIdx.x + threadIdx.x] = s;
+    p.obs_part[7 * bx + threadIdx.x] = s;
   }
 }
 
-__global__ void __launch_bounds__(256) k_obs(ObsParams p) {
+__device__ __forceinline__ void obs(const ObsParams& p) {
   __shared__ double red[7][8];
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < p.nblk_int; b += blockDim.x)
@@ -265,7 +265,35 @@ __global__ void __launch_bounds__(256) k_obs(ObsParams p) {
     }
     *p.time += p.dt;
     *p.stepno += 1;
+    if (p.status) *p.status = *p.err | (p.flags->overflow ? 4 : 0);
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kIntThreads) k_heun1(IntParams p) {
+  heun1<T>(p, blockIdx.x);
+}
+template <typename T>
+__global__ void __launch_bounds__(kIntThreads) k_heun2(IntParams p) {
+  heun2<T>(p, blockIdx.x);
+}
+__global__ void __launch_bounds__(256) k_obs(ObsParams p) { obs(p); }
+
+__global__ void __launch_bounds__(kIntThreads, 4) k_heun1_packed(const IntParams* __restrict__ ps,
+                                                             const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const IntParams p = ps[t.rep];
+  heun1<float>(p, t.blk);
+}
+__global__ void __launch_bounds__(kIntThreads, 4) k_heun2_packed(const IntParams* __restrict__ ps,
+                                                             const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const IntParams p = ps[t.rep];
+  heun2<float>(p, t.blk);
+}
+__global__ void __launch_bounds__(256) k_obs_packed(const ObsParams* __restrict__ ps) {
+  const ObsParams p = ps[blockIdx.x];
+  obs(p);
 }
 
 // B and F in SI, particle order; optional overlap push of the positions
@@ -307,6 +335,24 @@ int launch_heun2(cudaStream_t st, const IntParams& p, bool fp64) {
 
 int launch_obs(cudaStream_t st, const ObsParams& p) {
   k_obs<<<1, 256, 0, st>>>(p);
+  return 1;
+}
+
+int launch_heun1_packed(cudaStream_t st, const IntParams* ps, const Packed& n256) {
+  if (!n256.n) return 0;
+  k_heun1_packed<<<n256.n, kIntThreads, 0, st>>>(ps, n256.tasks);
+  return 1;
+}
+
+int launch_heun2_packed(cudaStream_t st, const IntParams* ps, const Packed& n256) {
+  if (!n256.n) return 0;
+  k_heun2_packed<<<n256.n, kIntThreads, 0, st>>>(ps, n256.tasks);
+  return 1;
+}
+
+int launch_obs_packed(cudaStream_t st, const ObsParams* ps, int R) {
+  if (!R) return 0;
+  k_obs_packed<<<R, 256, 0, st>>>(ps);
   return 1;
 }
 

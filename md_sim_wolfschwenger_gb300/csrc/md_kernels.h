@@ -1,45 +1,76 @@
 // md_kernels.h -- host-side launch wrappers of the device kernels.  Each
 // returns the number of kernel launches it issued on the stream.
+//
+// Two forms per kernel: one system (parameters by value), and packed: one
+// grid over several systems, whose parameters sit in device arrays indexed
+// by replica and whose blocks are listed in a task table (Task, built by the
+// host from the per-system block counts below).  Packed launches exist for
+// the mixed-precision path.
 #pragma once
 #include "md_common.cuh"
 
 namespace md {
 
+// Task table of one packed launch (device memory) and its length = grid size.
+struct Packed {
+  const Task* tasks;
+  int n;
+};
+
+// Blocks of one system per kernel shape (task-table construction).
+int cell_blocks(int n);                 // cell assign/scatter/fill, integrator
+int cell_sort_blocks(const CellGrid& g);
+int real_blocks(int n);                 // real space and neighbour list
+int phase_blocks(int n);
+int sk_blocks(const KParams& p);
+int skred_blocks(const KParams& p);
+int scatter_blocks(const KParams& p, int np);
+int int_blocks(int n);
+
 // Step start: decides whether this step rebuilds the cell order and the
 // neighbour list (host request, or a particle moved more than half_skin).
 int launch_step_begin(cudaStream_t st, StepFlags* flags, double half_skin);
+int launch_step_begin_packed(cudaStream_t st, const CellParams* ps, int R);
 // Raises the displacement since the last build after new positions arrived.
 int launch_disp_check(cudaStream_t st, int n, const double* pos, const double* xbuild, double L, StepFlags* flags);
 // Cell order (skipped unless the step rebuilds) and the sorted views.
-int launch_cells(cudaStream_t st, int n, const double* pos, const double* mm, const double* magMom_u,
-                 const double* rMag_u, double L, const CellGrid& g, int* cellOf, int* count, int* tmp,
-                 const SortedView& s, bool fp64, double* xbuild, const StepFlags* flags);
+int launch_cells(cudaStream_t st, const CellParams& p, bool fp64);
+int launch_cells_packed(cudaStream_t st, const CellParams* ps, int R, const Packed& n256, const Packed& sort);
 // Neighbour list within rc + skin (count, scan, fill; skipped unless rebuilding).
 int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64);
+int launch_nbr_packed(cudaStream_t st, const RealParams* ps, int R, const Packed& real);
 int launch_set_mu(cudaStream_t st, int n, const double* mm, const double* magMom_u, const double* rMag_u,
                   const SortedView& s, bool fp64);
 
 // Real space: full (field + force + pressure + overlap) or field only.
-int real_blocks(int n);
 int launch_real(cudaStream_t st, const RealParams& p, bool full, bool fp64);
+int launch_real_packed(cudaStream_t st, const RealParams* ps, const Packed& real, bool full, bool coat);
 
 // k space: structure factor partials, reduction, scatter (full or field only).
 // ev (optional): two events recorded after the structure factor and after
 // the reduction.
 int launch_kspace(cudaStream_t st, const KParams& p, bool full, bool fp64, cudaEvent_t* ev = nullptr);
+// Packed k space; kcmax bounds the shared-memory tables, np = particles per
+// scatter block (scatter_particles(kcmax)).
+int launch_kspace_packed(cudaStream_t st, const KParams* ps, const Packed& sk, const Packed& red, const Packed& sc,
+                         bool full, int kcmax, int np);
 // Per-particle phase tables (once per step; positions are frozen across the
 // two Heun stages).
 int launch_phase_tables(cudaStream_t st, const KParams& p, bool fp64);
+int launch_phase_tables_packed(cudaStream_t st, const KParams* ps, const Packed& phase);
 // FP32 FMA-chain calibration: returns FLOPs issued by one launch.
 double launch_fma_calibration(cudaStream_t st, float* out, int blocks, int threads);
 size_t kscatter_smem(int kc, bool fp64);
 size_t ksf_smem(int kc, bool fp64);
+int scatter_particles(int kc, bool fp64);
 
 // Integrator.
-int int_blocks(int n);
 int launch_heun1(cudaStream_t st, const IntParams& p, bool fp64);
 int launch_heun2(cudaStream_t st, const IntParams& p, bool fp64);
 int launch_obs(cudaStream_t st, const ObsParams& p);
+int launch_heun1_packed(cudaStream_t st, const IntParams* ps, const Packed& n256);
+int launch_heun2_packed(cudaStream_t st, const IntParams* ps, const Packed& n256);
+int launch_obs_packed(cudaStream_t st, const ObsParams* ps, int R);
 // B, F in SI (orig order, double) from the stage outputs; optional overlap push.
 int launch_combine(cudaStream_t st, const IntParams& p, double* Bout, double* Fout, int apply_overlap,
                    bool fp64);

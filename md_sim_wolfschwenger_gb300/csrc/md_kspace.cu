@@ -76,10 +76,12 @@ __device__ __forceinline__ void particle_coord(const SortedView& s, int k, int a
 
 // ------------------------------------------------------------ phase tables
 
+constexpr int kPhaseThreads = 256;
+
 template <typename T>
-__global__ void k_phase_tables(KParams p) {
+__device__ __forceinline__ void phase_tables(const KParams& p, int bx) {
   using T2 = typename V2<T>::t;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = bx * kPhaseThreads + threadIdx.x;
   if (t >= 3 * p.n) return;
   const int ax = t / p.n, k = t - ax * p.n;
   unsigned sf;
@@ -110,7 +112,7 @@ __global__ void k_phase_tables(KParams p) {
 // ------------------------------------------------------ structure factor
 
 template <typename T>
-__global__ void __launch_bounds__(kSkThreads, 3) k_sk(KParams p) {
+__device__ __forceinline__ void sk_body(const KParams& p, int bx, int by) {
   using T2 = typename V2<T>::t;
   using T4 = typename V4<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -119,8 +121,8 @@ __global__ void __launch_bounds__(kSkThreads, 3) k_sk(KParams p) {
   T4* mus = (T4*)(tab + kSkTile * E3);       // [kSkTile]
   const T2* gtab = (const T2*)p.tab;
   const int tid = threadIdx.x;
-  const int sidx = blockIdx.x * kSkThreads + tid;
-  const int chunk = blockIdx.y;
+  const int sidx = bx * kSkThreads + tid;
+  const int chunk = by;
   const int p0 = chunk * p.chunk, p1 = min(p.n, p0 + p.chunk);
   const bool has = sidx < p.nseg;
   KSeg sg = {0, 0, 0, 0};
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(kSkThreads, 3) k_sk(KParams p) {
     for (int c = 0; c < kSegMax; c++)
       if (c < len) out[c] = make_double2((double)sc[c], (double)ss[c]);
   }
-  if (blockIdx.x == 0) {
+  if (bx == 0) {
     // sum of moments of this chunk (surface term), FP64
     double m0 = 0, m1 = 0, m2 = 0;
     for (int q = p0 + tid; q < p1; q += kSkThreads) {
@@ -203,11 +205,11 @@ __global__ void __launch_bounds__(kSkThreads, 3) k_sk(KParams p) {
 
 // Sum of the chunk partials: block = 32 k's x 8 chunk groups, fixed order.
 template <typename T>
-__global__ void __launch_bounds__(256) k_sk_reduce(KParams p) {
+__device__ __forceinline__ void sk_reduce(const KParams& p, int bx) {
   using T2 = typename V2<T>::t;
   __shared__ double2 red[8][32];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int kk = blockIdx.x * 32 + tx;
+  const int kk = bx * 32 + tx;
   double a = 0, b = 0;
   if (kk < p.nk)
     for (int c = ty; c < p.nchunk; c += 8) {
@@ -229,7 +231,7 @@ __global__ void __launch_bounds__(256) k_sk_reduce(KParams p) {
     o.y = (T)(e * b);
     ((T2*)p.eS)[p.rowpos[kk]] = o;
   }
-  if (blockIdx.x == 0 && threadIdx.x < 3) {
+  if (bx == 0 && threadIdx.x < 3) {
     double s = 0;
     for (int c = 0; c < p.nchunk; c++) s += p.musum_part[3 * c + threadIdx.x];
     p.musum[threadIdx.x] = s;
@@ -250,7 +252,7 @@ __device__ __forceinline__ void kahan_add(T& s, T& c, T v) {
 }
 
 template <typename T, int NP, bool FULL>
-__global__ void __launch_bounds__(NP * kScatterParts) k_kscatter(KParams p) {
+__device__ __forceinline__ void kscatter(const KParams& p, int bx, int kcmax) {
   using T2 = typename V2<T>::t;
   using T4 = typename V4<T>::t;
   constexpr int NT = NP * kScatterParts;
@@ -258,12 +260,12 @@ __global__ void __launch_bounds__(NP * kScatterParts) k_kscatter(KParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int K1 = p.kc + 1, E3 = 3 * K1;
   T2* tab = (T2*)smem_raw;                       // [3 * K1][NP]
-  T2* es_all = tab + E3 * NP;                    // [parts][kKChunk]
+  T2* es_all = tab + 3 * (kcmax + 1) * NP;       // [parts][kKChunk]
   KSeg* seg_all = (KSeg*)(es_all + kScatterParts * kKChunk);  // [parts][kSegChunk]
   T* red = (T*)es_all;                           // [parts][6][NP], after the loop
   const int tid = threadIdx.x;
   const int part = tid / NP, lp = tid - part * NP;
-  const int base = blockIdx.x * NP;
+  const int base = bx * NP;
   const int k = base + lp;
   const bool active = k < p.n;
   const int kk = active ? k : p.n - 1;
@@ -393,6 +395,57 @@ __global__ void __launch_bounds__(NP * kScatterParts) k_kscatter(KParams p) {
   }
 }
 
+// ------------------------------------------------------------ entry points
+
+template <typename T>
+__global__ void __launch_bounds__(kPhaseThreads) k_phase_tables(KParams p) {
+  phase_tables<T>(p, blockIdx.x);
+}
+template <typename T>
+__global__ void __launch_bounds__(kSkThreads, 3) k_sk(KParams p) {
+  sk_body<T>(p, blockIdx.x, blockIdx.y);
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_sk_reduce(KParams p) {
+  sk_reduce<T>(p, blockIdx.x);
+}
+template <typename T, int NP, bool FULL>
+__global__ void __launch_bounds__(NP * kScatterParts) k_kscatter(KParams p) {
+  kscatter<T, NP, FULL>(p, blockIdx.x, p.kc);
+}
+
+__global__ void __launch_bounds__(kPhaseThreads) k_phase_tables_packed(const KParams* __restrict__ ps,
+                                                                       const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const KParams p = ps[t.rep];
+  phase_tables<float>(p, t.blk);
+}
+__global__ void __launch_bounds__(kSkThreads, 3) k_sk_packed(const KParams* __restrict__ ps,
+                                                              const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const KParams p = ps[t.rep];
+  const int nsb = (p.nseg + kSkThreads - 1) / kSkThreads;
+  sk_body<float>(p, t.blk % nsb, t.blk / nsb);
+}
+__global__ void __launch_bounds__(256) k_sk_reduce_packed(const KParams* __restrict__ ps,
+                                                          const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const KParams p = ps[t.rep];
+  sk_reduce<float>(p, t.blk);
+}
+template <int NP, bool FULL>
+__global__ void __launch_bounds__(NP * kScatterParts) k_kscatter_packed(const KParams* __restrict__ ps,
+                                                                        const Task* __restrict__ tk, int kcmax) {
+  const Task t = tk[blockIdx.x];
+  const KParams p = ps[t.rep];
+  kscatter<float, NP, FULL>(p, t.blk, kcmax);
+}
+
+int phase_blocks(int n) { return (3 * n + kPhaseThreads - 1) / kPhaseThreads; }
+int sk_blocks(const KParams& p) { return (p.nseg + kSkThreads - 1) / kSkThreads * p.nchunk; }
+int skred_blocks(const KParams& p) { return (p.nk + 31) / 32; }
+int scatter_blocks(const KParams& p, int np) { return (p.n + np - 1) / np; }
+
 size_t ksf_smem(int kc, bool fp64) {
   const size_t e = fp64 ? 16 : 8;
   return (size_t)kSkTile * 3 * (kc + 1) * e + (size_t)kSkTile * (fp64 ? 32 : 16);
@@ -404,7 +457,7 @@ static size_t scatter_bytes(int kc, bool fp64, int np) {
          (size_t)kScatterParts * (kKChunk / 4) * sizeof(KSeg);
 }
 
-static int scatter_particles(int kc, bool fp64) {
+int scatter_particles(int kc, bool fp64) {
   for (int np : {64, 32})
     if (scatter_bytes(kc, fp64, np) <= 200 * 1024) return np;
   return 0;
@@ -450,12 +503,52 @@ int launch_kspace(cudaStream_t st, const KParams& p, bool full, bool fp64, cudaE
 }
 
 int launch_phase_tables(cudaStream_t st, const KParams& p, bool fp64) {
-  const int nt = 3 * p.n;
   if (fp64)
-    k_phase_tables<double><<<(nt + 255) / 256, 256, 0, st>>>(p);
+    k_phase_tables<double><<<phase_blocks(p.n), kPhaseThreads, 0, st>>>(p);
   else
-    k_phase_tables<float><<<(nt + 255) / 256, 256, 0, st>>>(p);
+    k_phase_tables<float><<<phase_blocks(p.n), kPhaseThreads, 0, st>>>(p);
   return 1;
+}
+
+int launch_phase_tables_packed(cudaStream_t st, const KParams* ps, const Packed& phase) {
+  if (!phase.n) return 0;
+  k_phase_tables_packed<<<phase.n, kPhaseThreads, 0, st>>>(ps, phase.tasks);
+  return 1;
+}
+
+template <int NP>
+static void scatter_packed(cudaStream_t st, const KParams* ps, const Packed& sc, bool full, int kcmax, size_t smem) {
+  if (full) {
+    cudaFuncSetAttribute(k_kscatter_packed<NP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_kscatter_packed<NP, true><<<sc.n, NP * kScatterParts, smem, st>>>(ps, sc.tasks, kcmax);
+  } else {
+    cudaFuncSetAttribute(k_kscatter_packed<NP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_kscatter_packed<NP, false><<<sc.n, NP * kScatterParts, smem, st>>>(ps, sc.tasks, kcmax);
+  }
+}
+
+int launch_kspace_packed(cudaStream_t st, const KParams* ps, const Packed& sk, const Packed& red, const Packed& sc,
+                         bool full, int kcmax, int np) {
+  int l = 0;
+  if (sk.n) {
+    const size_t sm1 = ksf_smem(kcmax, false);
+    cudaFuncSetAttribute(k_sk_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+    k_sk_packed<<<sk.n, kSkThreads, sm1, st>>>(ps, sk.tasks);
+    l++;
+  }
+  if (red.n) {
+    k_sk_reduce_packed<<<red.n, 256, 0, st>>>(ps, red.tasks);
+    l++;
+  }
+  if (sc.n) {
+    const size_t sm2 = scatter_bytes(kcmax, false, np);
+    if (np == 64)
+      scatter_packed<64>(st, ps, sc, full, kcmax, sm2);
+    else
+      scatter_packed<32>(st, ps, sc, full, kcmax, sm2);
+    l++;
+  }
+  return l;
 }
 
 // FP32 throughput calibration: 8 independent FMA chains per thread, 4096

@@ -296,11 +296,11 @@ __device__ __forceinline__ void scan_rows(const RealParams& p, int k, int lane, 
 
 // Count (FILL = false) or write (FILL = true) the neighbours within rc + skin.
 template <typename T, bool FILL>
-__global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build(RealParams p) {
+__device__ __forceinline__ void nbr_build(const RealParams& p, int bx) {
   if (!p.flags->rebuild) return;
   if (FILL && p.flags->overflow) return;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int k = blockIdx.x * kRealWarps + wib;
+  const int k = bx * kRealWarps + wib;
   if (k >= p.n) return;
   const Self<T> me = load_self<T, false>(p, k);
   int cnt = 0;
@@ -314,7 +314,8 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build(RealParams p) {
 }
 
 // Exclusive scan of the counts (one block); flags overflow.
-__global__ void __launch_bounds__(1024) k_nbr_scan(RealParams p, StepFlags* flags) {
+__device__ __forceinline__ void nbr_scan(const RealParams& p) {
+  StepFlags* flags = p.flags;
   if (!flags->rebuild) return;
   __shared__ long long wsum[32];
   const int t = threadIdx.x, nt = blockDim.x, n = p.n;
@@ -356,12 +357,12 @@ __global__ void __launch_bounds__(1024) k_nbr_scan(RealParams p, StepFlags* flag
 // ------------------------------------------------------------ evaluation
 
 template <typename T, bool FULL, bool COAT>
-__global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
+__device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
   using T4 = typename V4<T>::t;
   constexpr bool F32 = std::is_same<T, float>::value;
   __shared__ float4 q[kRealWarps][64];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int k = blockIdx.x * kRealWarps + wib;
+  const int k = bx * kRealWarps + wib;
   if (k >= p.n) return;  // whole warp; no block-level synchronisation below
   Acc<T> a;
   const T4 mi = ((const T4*)p.s.mu)[k];
@@ -485,6 +486,37 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
   }
 }
 
+// ------------------------------------------------------------ entry points
+
+template <typename T, bool FILL>
+__global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build(RealParams p) {
+  nbr_build<T, FILL>(p, blockIdx.x);
+}
+__global__ void __launch_bounds__(1024) k_nbr_scan(RealParams p) { nbr_scan(p); }
+template <typename T, bool FULL, bool COAT>
+__global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
+  real_eval<T, FULL, COAT>(p, blockIdx.x);
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build_packed(const RealParams* __restrict__ ps,
+                                                                      const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const RealParams p = ps[t.rep];
+  nbr_build<float, FILL>(p, t.blk);
+}
+__global__ void __launch_bounds__(1024) k_nbr_scan_packed(const RealParams* __restrict__ ps) {
+  const RealParams p = ps[blockIdx.x];
+  nbr_scan(p);
+}
+template <bool FULL, bool COAT>
+__global__ void __launch_bounds__(kRealWarps * 32, COAT ? 2 : 4) k_real_packed(const RealParams* __restrict__ ps,
+                                                                 const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const RealParams p = ps[t.rep];
+  real_eval<float, FULL, COAT>(p, t.blk);
+}
+
 int real_blocks(int n) { return (n + kRealWarps - 1) / kRealWarps; }
 
 int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64) {
@@ -493,7 +525,8 @@ int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64
     k_nbr_build<double, false><<<grid, block, 0, st>>>(p);
   else
     k_nbr_build<float, false><<<grid, block, 0, st>>>(p);
-  k_nbr_scan<<<1, 1024, 0, st>>>(p, flags);
+  (void)flags;
+  k_nbr_scan<<<1, 1024, 0, st>>>(p);
   if (fp64)
     k_nbr_build<double, true><<<grid, block, 0, st>>>(p);
   else
@@ -516,6 +549,23 @@ int launch_real(cudaStream_t st, const RealParams& p, bool full, bool fp64) {
     else
       k_real<float, false, false><<<grid, block, 0, st>>>(p);
   }
+  return 1;
+}
+
+int launch_nbr_packed(cudaStream_t st, const RealParams* ps, int R, const Packed& real) {
+  if (real.n) k_nbr_build_packed<false><<<real.n, kRealWarps * 32, 0, st>>>(ps, real.tasks);
+  k_nbr_scan_packed<<<R, 1024, 0, st>>>(ps);
+  if (real.n) k_nbr_build_packed<true><<<real.n, kRealWarps * 32, 0, st>>>(ps, real.tasks);
+  return 3;
+}
+
+int launch_real_packed(cudaStream_t st, const RealParams* ps, const Packed& real, bool full, bool coat) {
+  if (!real.n) return 0;
+  if (full)
+    coat ? k_real_packed<true, true><<<real.n, kRealWarps * 32, 0, st>>>(ps, real.tasks)
+         : k_real_packed<true, false><<<real.n, kRealWarps * 32, 0, st>>>(ps, real.tasks);
+  else
+    k_real_packed<false, false><<<real.n, kRealWarps * 32, 0, st>>>(ps, real.tasks);
   return 1;
 }
 

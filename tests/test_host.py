@@ -143,3 +143,62 @@ def test_cost_model_cutoff_is_valid():
     assert 0.08 * lb.value <= r.value <= 0.5 * lb.value
     assert 2 <= k.value <= 64
     assert ef.value < 2e-5 and math.isfinite(et.value)
+
+
+def _init(n, seed, **kw):
+    import md_sim_wolfschwenger_gb300 as m
+    cfg = m.Configuration.default().set(numbPartOverride=n, **kw)
+    return m.init_system(cfg, n, seed)
+
+
+@pytest.mark.parametrize("kw", [dict(volFrac=0.05, rMagMean=1e-8),
+                                dict(volFrac=0.2, SIZE_DIST=1, sigmaLog=0.25, rMagMean=1.25e-8),
+                                dict(volFrac=0.1, SIZE_DIST=1, rMagMean=1e-8)])
+def test_init_system_places_non_overlapping_spheres(kw):
+    rMag, rHydr, pos, mm, ea, L = _init(3000, 5, **kw)
+    c = kw["rMagMean"]
+    if kw.get("SIZE_DIST"):
+        assert rMag.std() > 0
+    else:
+        assert np.all(rMag == c)
+    assert L == pytest.approx((np.sum(4 / 3 * 3.14159265359 * rHydr ** 3) / kw["volFrac"]) ** (1 / 3), rel=1e-12)
+    # inside [-(L/2 - r_h), L/2 - r_h] and no overlap of hydrodynamic spheres
+    assert np.all(np.abs(pos) <= L / 2 - rHydr[None, :] + 1e-20)
+    from scipy.spatial import cKDTree
+    t = cKDTree(pos.T)
+    for i, j in t.query_pairs(2 * rHydr.max()):
+        assert np.linalg.norm(pos[:, i] - pos[:, j]) >= rHydr[i] + rHydr[j]
+    assert np.allclose((mm ** 2).sum(0), 1) and np.allclose((ea ** 2).sum(0), 1)
+
+
+def test_init_system_orientations_and_grid():
+    _, _, pos, mm, ea, L = _init(512, 3, volFrac=0.05, INIT_CONFIG_TRANS=2, INIT_CONFIG_ROT=1)
+    xs = np.unique(np.round(pos[0] / L, 12))
+    assert xs.size == 8 and np.allclose(np.diff(xs), 1 / 8)
+    assert np.all(mm[2] == 1) and np.all(mm[:2] == 0)
+    assert abs(ea[2].mean()) < 0.1 and abs((ea[2] ** 2).mean() - 1 / 3) < 0.05   # uniform on the sphere
+    _, _, _, mm3, ea3, _ = _init(64, 3, volFrac=0.05, INIT_CONFIG_ROT=3)
+    assert np.all(ea3[2] == 1) and np.array_equal(mm3, ea3)
+    _, _, _, mm4, ea4, _ = _init(4000, 4, volFrac=0.05, INIT_CONFIG_ROT=4)
+    assert abs(np.mean((mm4 * ea4).sum(0))) < 0.05   # independent directions
+    a = _init(100, 9, volFrac=0.05)
+    b = _init(100, 9, volFrac=0.05)
+    assert all(np.array_equal(x, y) for x, y in zip(a[:5], b[:5]))
+
+
+def test_init_system_reports_jammed_packing():
+    import md_sim_wolfschwenger_gb300 as m
+    with pytest.raises(m.MdError):
+        _init(2000, 1, volFrac=0.6)
+
+
+def test_tune_cache_file_round_trip(tmp_path):
+    import md_sim_wolfschwenger_gb300 as m
+    p = tmp_path / "t.txt"
+    p.write_text("# header\n24 5 0.25\n26 10 0.3125\n")
+    m.tune_cache_clear()
+    m.tune_cache_load(p)
+    q = tmp_path / "u.txt"
+    m.tune_cache_save(q)
+    assert q.read_text().splitlines()[1:] == ["24 5 0.25", "26 10 0.3125"]
+    m.tune_cache_clear()
