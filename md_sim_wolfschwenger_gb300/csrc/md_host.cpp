@@ -368,21 +368,21 @@ EwaldModel ewald_model(const md_config& c, const Props& p) {
 
 // FunRealError (src/interaction.cpp:330-338).
 double fun_real_error(const md_config& c, const EwaldModel& m, double x, double rc) {
-  double a = x * rc;
-  double b = m.M / std::sqrt(std::pow(m.L, 3.0) * std::pow(rc, 9.0) * m.n * std::pow(x, 4.0));
-  double cc = 4.0 * std::pow(a, 4.0) + 6.0 * std::pow(a, 2.0) + 3.0;
-  double d = 8.0 * std::pow(a, 6.0) + 20.0 * std::pow(a, 4.0) + 30.0 * std::pow(a, 2.0) + 15.0;
+  const double a = x * rc, a2 = a * a, a4 = a2 * a2, a6 = a4 * a2;
+  const double rc3 = rc * rc * rc, L3 = m.L * m.L * m.L;
+  const double b = m.M / (x * x * std::sqrt(L3 * rc3 * rc3 * rc3 * m.n));
+  const double cc = 4.0 * a4 + 6.0 * a2 + 3.0;
+  const double d = 8.0 * a6 + 20.0 * a4 + 30.0 * a2 + 15.0;
   return c.facEwald * b * std::sqrt(13.0 / 6.0 * cc * cc + 2.0 / 15.0 * d * d - 13.0 / 15.0 * cc * d) *
-             std::exp(-a * a) / m.fAl -
+             std::exp(-a2) / m.fAl -
          c.errTolEwald / std::sqrt(2.0);
 }
 
 // FunRezError (src/interaction.cpp:344-347).
 double fun_rez_error(const md_config& c, const EwaldModel& m, double alpha, double x) {
-  const double pi = c.my_pi;
-  return c.facEwald * 8.0 * m.M * pi / std::pow(m.L, 3.0) * alpha *
-             std::sqrt(2.0 * pi * x * x * x / (15.0 * m.n)) * std::exp(-std::pow(pi * x / (alpha * m.L), 2.0)) /
-             m.fAl -
+  const double pi = c.my_pi, q = pi * x / (alpha * m.L);
+  return c.facEwald * 8.0 * m.M * pi / (m.L * m.L * m.L) * alpha * std::sqrt(2.0 * pi * x * x * x / (15.0 * m.n)) *
+             std::exp(-q * q) / m.fAl -
          c.errTolEwald / std::sqrt(2.0);
 }
 
@@ -456,13 +456,16 @@ double model_cost(double rc_box, int64_t kc, int64_t n) {
 }
 
 double choose_rc(const md_config& c, const EwaldModel& m, int64_t n, double* alpha_out, int64_t* kc_out) {
+  // every candidate rc = 0.08 L .. 0.5 L in steps of 0.005 L (the cost is not
+  // unimodal in rc, so no candidate is skipped)
   double best = 1e300, best_rc = 0.5;
-  for (double x = 0.08; x <= 0.5 + 1e-12; x += 0.005) {
+  for (int q = 0; q <= 84; q++) {
+    const double x = 0.08 + 0.005 * q;
     double a, k;
     if (!ewald_for_rc(c, m, x * m.L, &a, &k)) continue;
-    int64_t kc = (int64_t)std::floor(k + 0.5);
+    const int64_t kc = (int64_t)std::floor(k + 0.5);
     if (kc > 64) continue;
-    double cost = model_cost(x, kc, n);
+    const double cost = model_cost(x, kc, n);
     if (cost < best) {
       best = cost;
       best_rc = x;
