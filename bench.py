@@ -60,13 +60,19 @@ BYTES_HEUN2 = 404.0       # per particle
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=300)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     p.add_argument("--workload", choices=sorted(WORKLOADS), default="large")
     p.add_argument("--n", type=int, default=0, help="override the workload's particle count")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison")
+    p.add_argument("--sweep-replicas", type=int, default=256, help="field-sweep sample: replicas (0 skips it)")
+    p.add_argument("--sweep-steps", type=int, default=100, help="field-sweep sample: steps per replica")
+    p.add_argument("--serve-requests", type=int, default=256, help="served-stream sample: requests (0 skips it)")
+    p.add_argument("--serve-step-scale", type=float, default=0.01,
+                   help="served-stream sample: factor on the drawn step counts (1e3..1e5 log-uniform)")
     p.add_argument("--autotune", type=int, default=0, help="candidate cutoffs timed (0: the cost-model choice, the same one the reference arm uses)")
     return p.parse_args()
 
@@ -121,6 +127,9 @@ class ClockSampler:
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.02)
         except OSError:
             self.proc = None
 
@@ -259,6 +268,167 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------ secondary workloads
+
+
+def _pct(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = (len(xs) - 1) * q
+    lo, hi = int(math.floor(k)), int(math.ceil(k))
+    return xs[lo] + (xs[hi] - xs[lo]) * (k - lo)
+
+
+def fp64_plain(n, sysd, ewald, seed, steps=4, warm=1):
+    """The same system and Ewald parameters on the plain FP64 path
+    (MD_PREC_FP64, one instance): particle-steps/s from CUDA events on the
+    library's stream."""
+    import torch
+    from md_sim_wolfschwenger_gb300 import MD_NOISE_PHILOX, MD_PREC_FP64, Simulation
+    rMag, rHydr, L, pos, mm, ea = sysd
+    sim = Simulation(workload_config(n, seed), n, MD_PREC_FP64, rMag=rMag, rHydr=rHydr)
+    sim.set_state(pos, mm, ea)
+    sim.set_ewald(*ewald)
+    sim.set_noise(MD_NOISE_PHILOX, seed)
+    sim.step(warm, 1e-12)
+    sim.sync()
+    ext = torch.cuda.ExternalStream(sim.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(ext):
+        e0.record()
+    sim.step(steps, 1e-12)
+    with torch.cuda.stream(ext):
+        e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    sim.close()
+    return {"value": n / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms, "steps": steps,
+            "dtype": "f64", "note": "same system and Ewald parameters, plain FP64 path, one instance"}
+
+
+def sweep_sample(replicas, steps, seed=3):
+    """Field sweep (magnetisation curve): `replicas` independent systems with
+    N uniform in 256..8192, monodisperse 20/30 nm, volume fraction 0.05,
+    static fields evenly spaced 0..50 mT, advanced together by packed
+    launches (md_batch_*); `steps` steps each (the full sweep runs 5e4)."""
+    import md_sim_wolfschwenger_gb300 as m
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(256, 8193, replicas)
+    fields = np.linspace(0.0, 0.05, replicas)
+    t0 = time.perf_counter()
+    sims = []
+    for i, (n, b0) in enumerate(zip(ns, fields)):
+        cfg = m.Configuration.default().set(numbPartOverride=int(n), volFrac=0.05, rMagMean=1e-8, dShell=5e-9,
+                                            visOverride=1e-3, INIT_CONFIG_ROT=4, SIZE_DIST=0, magFluxDens=float(b0),
+                                            tMag=1.0, errTolEwald=1e-5)
+        rMag, rHydr, pos, mm, ea, L = m.init_system(cfg, int(n), 100 + i)
+        sim = m.Simulation(cfg, int(n), m.MD_PREC_MIXED, rMag=rMag)
+        a, r, k, _, _ = sim.ewald_params()
+        sim.set_ewald(a, r, k)
+        sim.set_state(pos, mm, ea)
+        sim.set_noise(m.MD_NOISE_PHILOX, 100 + i)
+        sims.append(sim)
+    setup_s = time.perf_counter() - t0
+    b = m.Batch(replicas)
+    for sim in sims:
+        b.add(sim, steps + 2, 1e-12)
+    b.run(2)  # warm-up: graph capture and first launches
+    gpu_ms, t0 = 0.0, time.perf_counter()
+    left = steps
+    while left > 0:
+        k = b.run(left)
+        gpu_ms += b.info()[3]
+        left -= k
+    wall = time.perf_counter() - t0
+    _, parts, lps, _ = b.info()
+    mz = [float(sim.records()[-1, 1]) for sim in sims]
+    b.close()
+    for sim in sims:
+        sim.close()
+    total = float(ns.sum()) * steps
+    return {"value": total / wall, "unit": "particle-steps/s", "gpu_value": total / (gpu_ms * 1e-3),
+            "replicas": replicas, "particles": int(ns.sum()), "steps": steps, "launches_per_step": lps,
+            "setup_s": setup_s,
+            "mz_at_0_25_50_mT": [mz[0], mz[len(mz) // 2], mz[-1]],
+            "sample": f"{replicas} replicas, N uniform 256..8192 (seeded), monodisperse 20/30 nm, volume fraction "
+                      f"0.05, static fields 0..50 mT, {steps} steps each (the full sweep runs 5e4), one packed "
+                      f"launch per kernel per step for all replicas under a captured CUDA graph"}
+
+
+def serve_stream(nreq, step_scale, seed=4):
+    """Requests of the served stream: Poisson arrivals at 200/s; N log-uniform
+    in 128..16384; volume fraction uniform in 0.02..0.15; steps log-uniform in
+    1e3..1e5 (times step_scale); sinusoidal field, amplitude uniform in
+    10..30 mT, frequency uniform in 10..100 kHz."""
+    rng = np.random.default_rng(seed)
+    arr = np.cumsum(rng.exponential(1.0 / 200.0, nreq))
+    out = []
+    for i in range(nreq):
+        n = int(round(math.exp(rng.uniform(math.log(128), math.log(16384)))))
+        phi = float(rng.uniform(0.02, 0.15))
+        st = max(1, int(round(math.exp(rng.uniform(math.log(1e3), math.log(1e5))) * step_scale)))
+        amp, freq = float(rng.uniform(0.01, 0.03)), float(rng.uniform(1e4, 1e5))
+        out.append(dict(n=n, volFrac=phi, steps=st, dt=1e-12, fieldKind=1, fieldAmp=amp, fieldFreq=freq,
+                        seed=5000 + i, arrival=float(arr[i])))
+    return out
+
+
+def serve_base_config():
+    import md_sim_wolfschwenger_gb300 as m
+    return m.Configuration.default().set(rMagMean=1e-8, dShell=5e-9, visOverride=1e-3, INIT_CONFIG_ROT=4,
+                                         SIZE_DIST=0, errTolEwald=1e-5)
+
+
+def serve_sample(nreq, step_scale, plain_sample=8):
+    """The served stream through md_serve_run (continuous batching under a
+    150 GB device-memory budget, real-time arrivals), and the plain FP64
+    single-instance path timed on a seeded subsample of the same requests
+    (each alone, back to back) for the ratio."""
+    import md_sim_wolfschwenger_gb300 as m
+    reqs = serve_stream(nreq, step_scale)
+    cfg = serve_base_config()
+    res, st = m.serve(cfg, reqs, hbm_budget=150e9, max_systems=256, round_steps=100, realtime=True)
+    ok = [r for r in res if r["status"] == 0]
+    lat = [r["latency"] for r in ok]
+    value = st["particle_steps"] / st["wall"]
+    # plain FP64 single instance on a subsample of the same requests
+    rng = np.random.default_rng(11)
+    idx = sorted(rng.choice(nreq, size=min(plain_sample, nreq), replace=False).tolist())
+    ps, secs = 0.0, 0.0
+    for i in idx:
+        q = reqs[i]
+        c = serve_base_config().set(numbPartOverride=q["n"], volFrac=q["volFrac"], seed=q["seed"], fieldKind=1,
+                                    fieldAmp=q["fieldAmp"], fieldFreq=q["fieldFreq"])
+        rMag, rHydr, pos, mm, ea, L = m.init_system(c, q["n"], q["seed"])
+        sim = m.Simulation(c, q["n"], m.MD_PREC_FP64, rMag=rMag)
+        a, r, k, _, _ = sim.ewald_params()
+        sim.set_ewald(a, r, k)
+        sim.set_state(pos, mm, ea)
+        sim.set_noise(m.MD_NOISE_PHILOX, q["seed"])
+        sim.step(1, 1e-12)
+        sim.sync()
+        k = max(2, min(q["steps"], 6))
+        t0 = time.perf_counter()
+        sim.step(k, 1e-12)
+        sim.sync()
+        secs += time.perf_counter() - t0
+        ps += q["n"] * k
+        sim.close()
+    plain = ps / secs if secs > 0 else None
+    return {"value": value, "unit": "particle-steps/s", "requests": nreq, "completed": len(ok),
+            "p50_latency_s": _pct(lat, 0.5), "p99_latency_s": _pct(lat, 0.99), "wall_s": st["wall"],
+            "gpu_ms": st["gpu_ms"], "admit_ms": st["admit_ms"], "rounds": st["rounds"],
+            "peak_systems": st["peak_systems"], "peak_bytes": st["peak_bytes"],
+            "plain_fp64_single_instance": {"value": plain, "unit": "particle-steps/s",
+                                           "sample": f"{len(idx)} requests of the stream, each alone on the "
+                                                     f"FP64 path (MD_PREC_FP64), a few steps each"},
+            "vs_plain_fp64": (value / plain) if plain else None,
+            "sample": f"first {nreq} requests of the stream (Poisson 200/s; N log-uniform 128..16384; volume "
+                      f"fraction 0.02..0.15; steps log-uniform 1e3..1e5 scaled by {step_scale}; sinusoidal "
+                      f"field 10..30 mT, 10..100 kHz); 150 GB budget, realtime admission, mixed precision"}
+
+
 # ----------------------------------------------------------- our arm
 
 
@@ -303,7 +473,6 @@ def run_ours(args):
         seg_sum = seg if seg_sum is None else {k: seg_sum[k] + v for k, v in seg.items()}
     torch.cuda.synchronize()
     barrier(ws)
-    clk = clocks.stop()
     total_ms = allmax(total_ms, ws)
     value = ws * n * args.steps / (total_ms * 1e-3)
     seg_mean = {k: v / args.steps for k, v in seg_sum.items()}
@@ -321,6 +490,7 @@ def run_ours(args):
         e1.record()
     torch.cuda.synchronize()
     cont_ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()  # sampled over both timed runs
 
     # end to end through the C ABI with pinned host buffers, copies timed
     host_in = [torch.empty((3, n), dtype=torch.float64).pin_memory().numpy() for _ in range(3)]
@@ -371,8 +541,11 @@ def run_ours(args):
     dom = max((k for k in segs if k in work), key=lambda k: segs[k]["ms"])
     traffic = None
     try:
-        traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(dom)
-    except Exception:
+        for ln in open(os.path.join(ROOT, "profiles", "traffic.txt")):
+            f = ln.split()
+            if len(f) == 2 and f[0] == dom and not ln.startswith("#"):
+                traffic = float(f[1])
+    except OSError:
         pass
     d = segs[dom]
     roofline = {"kernel": dom, "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"], "unit": d["unit"],
@@ -387,6 +560,15 @@ def run_ours(args):
         cpu = {"value": n / per[0], "unit": "particle-steps/s", "cores": 1, "kind": "port",
                "sample": f"1 step of the same N={n} system and Ewald parameters, single thread (the reference "
                          f"is single-threaded): all-pairs list, FP64, Philox noise; {per[0]:.1f} s"}
+
+    fp64 = sweep = serving = None
+    if rank == 0 and ws == 1:
+        if not args.no_fp64:
+            fp64 = fp64_plain(n, sysd, (alpha, rc, kc), seed)
+        if args.sweep_replicas > 0:
+            sweep = sweep_sample(args.sweep_replicas, args.sweep_steps)
+        if args.serve_requests > 0:
+            serving = serve_sample(args.serve_requests, args.serve_step_scale)
 
     if rank == 0:
         line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
@@ -407,7 +589,9 @@ def run_ours(args):
                 "e2e": e2e, "roofline": roofline, "segments": segs,
                 "continuous": {"ms_per_step": cont_ms, "value": ws * n / (cont_ms * 1e-3),
                                "note": "graph replays back to back without L2 flush"},
-                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches_per_step * args.steps}
+                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches_per_step * args.steps,
+                "fp64_plain": fp64, "mixed_over_fp64_plain": (value / fp64["value"]) if fp64 else None,
+                "sweep": sweep, "serving": serving}
         print(json.dumps(line), flush=True)
     sim.close()
 
@@ -416,7 +600,8 @@ def main():
     args = parse()
     W.clear()
     W.update(WORKLOADS[args.workload])
-    if args.n > 0:
+    if args.n > 0 and args.n != W["n"]:
+        W["desc"] = W["desc"].replace(f"N={W['n']}", f"N={args.n}")
         W["n"] = args.n
     args.n = W["n"]
     if args.impl == "reference":

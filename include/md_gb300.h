@@ -372,6 +372,34 @@ typedef struct md_serve_stats {
 int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, const md_serve_opts* opts,
                  md_request_result* results, md_serve_stats* stats);
 
+/* ------------------------------------------------------ output files */
+/* The reference's text outputs, written from host arrays with the bytes its
+ * Eigen stream output produces (6 significant digits, columns aligned to the
+ * widest coefficient, each matrix followed by an empty line).  A time label
+ * tInt of exactly 0 truncates the file, any other value appends -- the rule
+ * of saveData (src/postprocessing.cpp:15-32). */
+/* saveData: rows x cols matrix a (col_major != 0: a[i + j rows], else
+ * a[i cols + j]). */
+int md_write_matrix_txt(const char* path, const double* a, int64_t rows, int64_t cols, int col_major, double tInt);
+/* WriteCoords2TXT (src/postprocessing.cpp:82-101): one frame of n rows
+ * {x y z m_x m_y m_z n_x n_y n_z label}, the label column holding tInt in
+ * row 0 and zeros below. */
+int md_write_coords_txt(const char* path, int64_t n, const double* pos, const double* mm, const double* ea,
+                        double tInt);
+/* WriteData2TXT (src/postprocessing.cpp:106-133): n rows {rHydr rMag meta},
+ * meta = box length, N, field, Ms, T, tMag, tRelax, tEnd, volFrac, the two
+ * INIT_CONFIG keys, seed, K, surfactant density and length, Hamaker constant,
+ * valency, epsilon_r, gamma_0, absTol, errTolEwald, errTolSR in rows 0..21
+ * (rows beyond n are left out; the reference needs n >= 22). */
+int md_write_data_txt(const char* path, const md_config* cfg, int64_t n, const double* rMag, const double* rHydr,
+                      double lBox);
+/* ExportDiffVis (src/postprocessing.cpp:222-231) and the m_z / time exports
+ * of RunSimulation (src/simulation.cpp:532-536): dtMean.txt = tInt / steps,
+ * then Pxy, Pxz, Pyz, MSDx, MSDy, MSDz, mz and t .txt as column vectors from
+ * count records {t, mz, MSDx, MSDy, MSDz, Pxy, Pxz, Pyz} (row-major, as
+ * md_records returns them).  dir NULL or "": the working directory. */
+int md_export_records_txt(const char* dir, const double* obs, int64_t count, double tInt, int64_t steps);
+
 /* ------------------------------------------- structure factor, no allocation */
 /* This entry point has no counterpart in the reference.  It exists for
  * callers that cannot call cudaMalloc -- a host framework that owns all

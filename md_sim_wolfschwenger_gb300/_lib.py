@@ -145,6 +145,10 @@ def lib():
         "md_batch_info": (C.c_int, [V, PI64, PI64, PI64, P]),
         "md_serve_run": (C.c_int, [C.POINTER(MdConfig), C.POINTER(MdRequest), I64, C.POINTER(MdServeOpts),
                                    C.POINTER(MdRequestResult), C.POINTER(MdServeStats)]),
+        "md_write_matrix_txt": (C.c_int, [C.c_char_p, P, I64, I64, C.c_int, C.c_double]),
+        "md_write_coords_txt": (C.c_int, [C.c_char_p, I64, P, P, P, C.c_double]),
+        "md_write_data_txt": (C.c_int, [C.c_char_p, C.POINTER(MdConfig), I64, P, P, C.c_double]),
+        "md_export_records_txt": (C.c_int, [C.c_char_p, P, I64, C.c_double, I64]),
         "md_noalloc_scratch_bytes": (C.c_size_t, []),
         "md_structure_factor_noalloc": (C.c_int, [V, V, I64, C.c_double, I64, C.c_double, V, PI64, V]),
     }

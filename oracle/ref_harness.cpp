@@ -21,7 +21,10 @@
 //     the fixed value before every step (the reference's own loop,
 //     simulation.cpp:466-520, would otherwise let it grow).
 //
-// I/O: argv[1] = input file, argv[2] = output file (formats: oracle/ref_io.py).
+// I/O: argv[1] = input file, argv[2] = output file (formats: oracle/ref_io.py);
+// optional argv[3] = a directory where, after the last step, the reference's
+// own writers put its text outputs (data.txt, coords.txt with two frames,
+// dtMean/P/MSD .txt, mz.txt, t.txt), as RunSimulation would.
 // The working directory must have ../configuration.ini (configuration.cpp:6).
 
 #include <cmath>
@@ -34,6 +37,7 @@
 #include <iostream>
 #include <map>
 #include <set>
+#include <unistd.h>
 #include <string>
 #include <vector>
 #include <Eigen/Dense>
@@ -201,6 +205,8 @@ int main(int argc, char** argv) {
     elapsed += (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
     EvalTransCoeffs(pW, &buffer, &outputVar, &params);
     double mz = pW->coordsRot.posMm.col(2).mean();
+    outputVar.t.push_back(tInt);
+    outputVar.mz.push_back(mz);
     if (in.dump_level >= 1) {
       putArr(fo, pW->coordsTrans.pos);
       putArr(fo, pW->coordsRot.posMm);
@@ -218,5 +224,14 @@ int main(int argc, char** argv) {
   putArr(fo, pW->coordsRot.posEa);
   put1(fo, elapsed);
   fclose(fo);
+  if (argc > 3) {
+    if (chdir(argv[3]) != 0) { perror("txt dir"); return 2; }
+    WriteData2TXT(pW, &params, "data.txt");
+    WriteCoords2TXT(pW, "coords.txt", 0.0);
+    WriteCoords2TXT(pW, "coords.txt", tInt);
+    ExportDiffVis(&outputVar, tInt, (int)in.nsteps);
+    saveData("mz.txt", Map<VectorXd, Unaligned>(outputVar.mz.data(), outputVar.mz.size()), 0);
+    saveData("t.txt", Map<VectorXd, Unaligned>(outputVar.t.data(), outputVar.t.size()), 0);
+  }
   return 0;
 }

@@ -82,11 +82,13 @@ def available() -> bool:
 
 
 def run_ref(ini, n, nsteps, dt, alpha=0.0, rc=0.0, kc=0.0, vis=0.0, rmag=None, pos=None,
-            mm=None, ea=None, dump_level=1, ewald_search=False, timeout=3600):
+            mm=None, ea=None, dump_level=1, ewald_search=False, timeout=3600, txt_dir=None):
     """Runs the reference harness and returns a dict of arrays.
 
     Per-step arrays (dump_level >= 1) are stacked along axis 0 and reshaped to
-    (nsteps, 3, N) so that [s, c, i] is component c of particle i.
+    (nsteps, 3, N) so that [s, c, i] is component c of particle i.  With
+    txt_dir, the reference's own writers also put its text output files
+    there after the last step.
     """
     if not available():
         raise RuntimeError("reference harness not built (oracle/build_ref.sh)")
@@ -102,7 +104,8 @@ def run_ref(ini, n, nsteps, dt, alpha=0.0, rc=0.0, kc=0.0, vis=0.0, rmag=None, p
             for a in (rmag, pos, mm, ea):
                 if a is not None:
                     f.write(np.ascontiguousarray(a, dtype=np.float64).tobytes())
-        r = subprocess.run([REF_HARNESS, fin, fout], cwd=run, capture_output=True, text=True,
+        argv = [REF_HARNESS, fin, fout] + ([os.path.abspath(txt_dir)] if txt_dir else [])
+        r = subprocess.run(argv, cwd=run, capture_output=True, text=True,
                            timeout=timeout)
         if r.returncode != 0:
             raise RuntimeError(f"ref_harness failed ({r.returncode}): {r.stderr[-2000:]}")

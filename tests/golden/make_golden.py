@@ -2,12 +2,15 @@
 simulator's own code (oracle/_ref/ref_harness, built from the reference
 sources by oracle/build_ref.sh) on seeded initial states.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [case ...]
 Each case stores its inputs (configuration, radii, state, Ewald parameters,
 dt) and the reference's FP64 outputs per step: B after CompInteractions, F
 (including the thermal force), the thermal arrays, the positions after the
 overlap push, B at the Heun predictor, the state after the step and the
-per-step records {t, mz, MSDx, MSDy, MSDz, Pxy, Pxz, Pyz}.
+per-step records {t, mz, MSDx, MSDy, MSDz, Pxy, Pxz, Pyz}.  Cases with
+txt=True also keep the text files the reference's own writers produce after
+the last step (data.txt, coords.txt, dtMean/P/MSD/mz/t .txt) in
+tests/golden/<case>_txt/.
 """
 import json
 import os
@@ -25,7 +28,7 @@ VIS = 1e-3  # water, the BASELINE viscosity (the reference's Vogel formula gives
 
 
 def case(name, n, nsteps, rc_frac, seed, noise=True, coating=False, lognormal=False, overlap=False, dt=1e-12,
-         B0=0.01, rot=3):
+         B0=0.01, rot=3, txt=False):
     ini = ref_io.ini_dict(npDim=round(n ** (1 / 3)) if round(n ** (1 / 3)) ** 3 == n else 4,
                           ENABLE_THERM_FIELD="true" if noise else "false",
                           ENABLE_THERM_TORQUE="true" if noise else "false",
@@ -48,15 +51,20 @@ def case(name, n, nsteps, rc_frac, seed, noise=True, coating=False, lognormal=Fa
         for a in range(0, 8, 2):
             pos[:, a + 1] = pos[:, a] + np.array([1.2e-8, 0.8e-8, 0.0])[:, None][:, 0] * (1 + 0.1 * a)
     alpha, kc, _ = O.ewald_for_rc(d, rMag, rHydr, L, rc_frac * L)
+    txt_dir = None
+    if txt:
+        txt_dir = os.path.join(OUT, name + "_txt")
+        os.makedirs(txt_dir, exist_ok=True)
     ref = ref_io.run_ref(ini, n, nsteps, dt, alpha=alpha, rc=rc_frac * L, kc=kc, vis=VIS,
                          rmag=rMag if (lognormal or coating) else None, pos=pos.ravel(), mm=mm.ravel(),
-                         ea=ea.ravel())
+                         ea=ea.ravel(), txt_dir=txt_dir)
     assert abs(ref["lBox"] - L) <= 1e-15 * L, (ref["lBox"], L)
     out = dict(n=n, nsteps=nsteps, dt=dt, alpha=alpha, rc=rc_frac * L, kc=kc, vis=VIS, lBox=L, rMag=rMag,
                rHydr=ref["rHydr"], pos=pos, mm=mm, ea=ea, rCutSR=ref["rCutSR"])
     for k in ("B1", "F1", "thermTorque", "thermField", "thermForce", "posCorr", "B2", "pos", "mm", "ea", "obs",
               "pairs"):
         out["ref_" + k] = ref[k]
+    out["ref_posF"], out["ref_mmF"], out["ref_eaF"] = ref["posF"], ref["mmF"], ref["eaF"]
     np.savez_compressed(os.path.join(OUT, name + ".npz"), ini=json.dumps(ini), **out)
     print(name, "n", n, "L", L, "alpha*L", alpha * L, "kc", kc, "pairs", ref["pairs"])
 
@@ -79,10 +87,15 @@ def O_eff(d, dmag):
 if __name__ == "__main__":
     if not ref_io.available():
         sys.exit("build the reference harness first: oracle/build_ref.sh")
-    case("n64_noiseoff", 64, 3, 0.45, seed=11, noise=False)
-    case("n64_refnoise", 64, 3, 0.45, seed=12, noise=True)
-    case("n512_cfg1_noiseoff", 512, 2, 0.45, seed=1, noise=False)
-    case("n512_cfg1_refnoise", 512, 2, 0.3, seed=1, noise=True)
-    case("n64_coating", 64, 1, 0.45, seed=13, noise=False, coating=True)
-    case("n64_lognormal", 64, 2, 0.4, seed=14, noise=True, lognormal=True)
-    case("n64_overlap", 64, 1, 0.45, seed=15, noise=False, overlap=True)
+    CASES = {
+        "n64_noiseoff": lambda: case("n64_noiseoff", 64, 3, 0.45, seed=11, noise=False),
+        "n64_refnoise": lambda: case("n64_refnoise", 64, 3, 0.45, seed=12, noise=True),
+        "n512_cfg1_noiseoff": lambda: case("n512_cfg1_noiseoff", 512, 2, 0.45, seed=1, noise=False),
+        "n512_cfg1_refnoise": lambda: case("n512_cfg1_refnoise", 512, 2, 0.3, seed=1, noise=True),
+        "n64_coating": lambda: case("n64_coating", 64, 1, 0.45, seed=13, noise=False, coating=True),
+        "n64_lognormal": lambda: case("n64_lognormal", 64, 2, 0.4, seed=14, noise=True, lognormal=True),
+        "n64_overlap": lambda: case("n64_overlap", 64, 1, 0.45, seed=15, noise=False, overlap=True),
+        "n64_outputs": lambda: case("n64_outputs", 64, 6, 0.4, seed=16, noise=True, lognormal=True, txt=True),
+    }
+    for name in (sys.argv[1:] or CASES):
+        CASES[name]()

@@ -12,7 +12,7 @@ import ref_io
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 GOLDEN_CASES = ["n64_noiseoff", "n64_refnoise", "n512_cfg1_noiseoff", "n512_cfg1_refnoise", "n64_coating",
-                "n64_lognormal", "n64_overlap"]
+                "n64_lognormal", "n64_overlap", "n64_outputs"]
 
 # Tolerances (contact-normalised RMS, the metric of CheckEwaldSum,
 # src/interaction.cpp:741-754).
