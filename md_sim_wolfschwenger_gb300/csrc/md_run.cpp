@@ -1,0 +1,250 @@
+// md_run.cpp -- drop-in executable for MD_Sim_Wolfschwenger's `main`
+// (src/simulation.cpp:24-31): InitSimulation then RunSimulation, with the
+// time step on the GPU through the library's C ABI (include/md_gb300.h).
+//
+// Same inputs and outputs as the reference program: the keys of
+// configuration.ini (read from ../configuration.ini unless a path is given,
+// src/configuration.cpp:6), and in the working directory (or --out DIR)
+// data.txt, coords.txt (a frame whenever floor(tInt / tEnd * npCoords)
+// reaches the next count, plus the final frame), dtMean.txt, Pxy/Pxz/Pyz.txt,
+// MSDx/MSDy/MSDz.txt, mz.txt and t.txt, written with the reference's text
+// format (src/postprocessing.cpp, src/simulation.cpp:466-537).
+//
+// Differences, stated on stdout when they apply:
+//   * the time step is fixed at deltaTinit (SOLVER = 0, Heun, with every step
+//     accepted); SOLVER = 1, 2 (adaptive Bogacki-Shampine / Dormand-Prince)
+//     are reported and run as fixed-step Heun;
+//   * thermal noise comes from the counter-based Philox generator (or is off,
+//     per the [gb300] noise key), not EigenRand's Mersenne Twister;
+//   * READ_FROM_FILE reads the last frame of coords_final.txt in the layout
+//     WriteCoords2TXT writes (x y z | m | n | label); the reference reads the
+//     moments and axes from columns 6-11 of that file, which its own writer
+//     does not produce (src/simulation.cpp:375-381 vs
+//     src/postprocessing.cpp:84-97).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/md_gb300.h"
+
+namespace {
+
+struct Opts {
+  std::string ini = "../configuration.ini";
+  std::string out;           // output directory ("" = working directory)
+  int precision = -1;        // -1: the configuration's [gb300] precision key
+  int autotune = 0;          // candidate cut-offs timed on the device (0: error model + cost model)
+  int device = 0;
+  int64_t chunk = 100000;    // steps between record read-backs
+  bool quiet = false;
+};
+
+void usage() {
+  std::printf(
+      "usage: md_run [configuration.ini] [--out DIR] [--precision mixed|fp64] [--autotune K]\n"
+      "              [--device D] [--chunk STEPS] [--quiet]\n"
+      "Runs MD_Sim_Wolfschwenger's simulation (InitSimulation + RunSimulation) with the time step on\n"
+      "the GPU; the configuration defaults to ../configuration.ini like the reference.\n");
+}
+
+[[noreturn]] void die(md_ctx* ctx, int st, const char* what) {
+  char buf[1024] = {0};
+  md_last_error(ctx, buf, sizeof buf);
+  std::fprintf(stderr, "md_run: %s failed: %s (%s)\n", what, md_strerror(st), buf);
+  std::exit(1);
+}
+
+#define CALL(ctx, expr)                   \
+  do {                                    \
+    const int st_ = (expr);               \
+    if (st_ != MD_OK) die(ctx, st_, #expr); \
+  } while (0)
+
+std::string path_in(const Opts& o, const char* name) {
+  if (o.out.empty()) return name;
+  return o.out + (o.out.back() == '/' ? "" : "/") + name;
+}
+
+// Last frame of a coords file written by WriteCoords2TXT: rows of 10
+// numbers, frames separated by empty lines.
+bool read_last_frame(const std::string& path, int64_t n, std::vector<double>* pos, std::vector<double>* mm,
+                     std::vector<double>* ea) {
+  std::ifstream f(path);
+  if (!f) return false;
+  std::vector<std::vector<double>> frame, last;
+  std::string line;
+  while (std::getline(f, line)) {
+    std::istringstream ss(line);
+    std::vector<double> row;
+    double v;
+    while (ss >> v) row.push_back(v);
+    if (row.empty()) {
+      if (!frame.empty()) last.swap(frame);
+      frame.clear();
+      continue;
+    }
+    if (row.size() < 9) return false;
+    frame.push_back(row);
+  }
+  if (!frame.empty()) last.swap(frame);
+  if ((int64_t)last.size() != n) return false;
+  for (int64_t i = 0; i < n; i++)
+    for (int c = 0; c < 3; c++) {
+      (*pos)[(size_t)(i + c * n)] = last[(size_t)i][(size_t)c];
+      (*mm)[(size_t)(i + c * n)] = last[(size_t)i][(size_t)(3 + c)];
+      (*ea)[(size_t)(i + c * n)] = last[(size_t)i][(size_t)(6 + c)];
+    }
+  return true;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  Opts o;
+  for (int i = 1; i < argc; i++) {
+    const std::string a = argv[i];
+    auto next = [&](const char* what) -> const char* {
+      if (i + 1 >= argc) {
+        std::fprintf(stderr, "md_run: %s needs a value\n", what);
+        std::exit(2);
+      }
+      return argv[++i];
+    };
+    if (a == "-h" || a == "--help") {
+      usage();
+      return 0;
+    } else if (a == "--out") {
+      o.out = next("--out");
+    } else if (a == "--precision") {
+      const std::string p = next("--precision");
+      if (p == "mixed") o.precision = MD_PREC_MIXED;
+      else if (p == "fp64") o.precision = MD_PREC_FP64;
+      else { std::fprintf(stderr, "md_run: precision must be mixed or fp64\n"); return 2; }
+    } else if (a == "--autotune") {
+      o.autotune = std::atoi(next("--autotune"));
+    } else if (a == "--device") {
+      o.device = std::atoi(next("--device"));
+    } else if (a == "--chunk") {
+      o.chunk = std::max<int64_t>(1, std::atoll(next("--chunk")));
+    } else if (a == "--quiet") {
+      o.quiet = true;
+    } else if (!a.empty() && a[0] == '-') {
+      std::fprintf(stderr, "md_run: unknown option %s\n", a.c_str());
+      usage();
+      return 2;
+    } else {
+      o.ini = a;
+    }
+  }
+
+  // ----------------------------------------------------- InitSimulation
+  md_config cfg;
+  CALL(nullptr, md_config_load_ini(o.ini.c_str(), &cfg));
+  const int prec = o.precision >= 0 ? o.precision : (int)cfg.precision;
+  const int64_t n = md_config_numb_part(&cfg);
+  if (cfg.SOLVER != 0)
+    std::printf("note: SOLVER = %lld (adaptive) is run as Heun with the fixed step deltaTinit = %g s\n",
+                (long long)cfg.SOLVER, cfg.deltaTinit);
+  std::vector<double> rMag((size_t)n), rHydr((size_t)n), pos(3 * (size_t)n), mm(3 * (size_t)n), ea(3 * (size_t)n);
+  double lBox = 0;
+  CALL(nullptr, md_init_system(&cfg, n, (uint64_t)cfg.seed, rMag.data(), rHydr.data(), pos.data(), mm.data(),
+                               ea.data(), &lBox));
+  if (cfg.READ_FROM_FILE) {
+    const std::string src = path_in(o, "coords_final.txt");
+    if (!read_last_frame(src, n, &pos, &mm, &ea)) {
+      std::fprintf(stderr, "md_run: READ_FROM_FILE: %s does not hold a frame of %lld particles\n", src.c_str(),
+                   (long long)n);
+      return 1;
+    }
+  }
+  CALL(nullptr, md_select_device(o.device));
+  md_ctx* ctx = nullptr;
+  CALL(nullptr, md_ctx_create(&cfg, n, prec, &ctx));
+  CALL(ctx, md_set_particles(ctx, rMag.data(), rHydr.data()));
+  CALL(ctx, md_set_box(ctx, lBox));
+  CALL(ctx, md_state_upload(ctx, pos.data(), mm.data(), ea.data(), 1));
+  double alpha = 0, rc = 0, errF = 0, errT = 0, ms = 0;
+  int64_t kc = 0;
+  if (o.autotune > 0) {
+    CALL(ctx, md_autotune_ewald(ctx, o.autotune, &alpha, &rc, &kc, &ms));
+  } else {
+    CALL(ctx, md_ewald_params(ctx, -1.0, &alpha, &rc, &kc, &errF, &errT));
+    CALL(ctx, md_set_ewald(ctx, alpha, rc, kc));
+  }
+  CALL(ctx, md_ewald_params(ctx, rc, &alpha, &rc, &kc, &errF, &errT));
+  std::printf("particles: %lld, box length: %g m, precision: %s\n", (long long)n, lBox,
+              prec == MD_PREC_FP64 ? "fp64" : "mixed");
+  std::printf("Ewald: alpha = %g 1/m, rc = %g m (%.4g L), kc = %lld; predicted force error %.3g, torque error "
+              "%.3g (relative to contact)\n",
+              alpha, rc, rc / lBox, (long long)kc, errF, errT);
+  CALL(ctx, md_set_noise(ctx, (int)cfg.noise, (uint64_t)cfg.seed));
+  CALL(nullptr, md_write_data_txt(path_in(o, "data.txt").c_str(), &cfg, n, rMag.data(), rHydr.data(), lBox));
+
+  // ------------------------------------------------------ RunSimulation
+  // The loop's time points and the coords frames, with the reference's own
+  // double arithmetic (tInt += deltaT; the frame test at the top of the
+  // loop body, written after the step, src/simulation.cpp:466-520).
+  const double dt = cfg.deltaTinit, tEnd = cfg.tEnd;
+  struct Frame {
+    int64_t step;
+    double t;
+  };
+  std::vector<Frame> frames;
+  int64_t steps = 0;
+  double tInt = 0;
+  {
+    int64_t count = 0;
+    while (tInt <= tEnd) {
+      if (std::floor(tInt / tEnd * cfg.npCoords) == (double)count) {
+        frames.push_back({steps, tInt});
+        count++;
+      }
+      tInt += dt;
+      steps++;
+    }
+  }
+  std::vector<double> rec;
+  rec.reserve(8 * (size_t)steps);
+  int64_t done = 0;
+  auto advance = [&](int64_t upto) {  // runs steps [done, upto)
+    while (done < upto) {
+      const int64_t k = std::min(o.chunk, upto - done);
+      CALL(ctx, md_step(ctx, k, dt, nullptr));
+      int64_t nr = 0;
+      CALL(ctx, md_num_records(ctx, &nr));
+      const size_t at = rec.size();
+      rec.resize(at + 8 * (size_t)nr);
+      CALL(ctx, md_records(ctx, 0, nr, rec.data() + at));
+      CALL(ctx, md_clear_records(ctx));
+      done += k;
+    }
+  };
+  const std::string coords = path_in(o, "coords.txt");
+  for (size_t f = 0; f < frames.size(); f++) {
+    advance(frames[f].step + 1);
+    CALL(ctx, md_state_download(ctx, pos.data(), mm.data(), ea.data()));
+    CALL(nullptr, md_write_coords_txt(coords.c_str(), n, pos.data(), mm.data(), ea.data(), frames[f].t));
+    if (!o.quiet)
+      std::printf("actual time: %gs\nsimulation progress: %g%%\n", frames[f].t, f / cfg.npCoords * 100.0);
+  }
+  advance(steps);
+  double tDev = 0;
+  int64_t sDev = 0;
+  CALL(ctx, md_get_time(ctx, &tDev, &sDev));
+  std::printf("simulation progress: 100%%\n%lld timesteps needed\n", (long long)steps);
+  CALL(ctx, md_state_download(ctx, pos.data(), mm.data(), ea.data()));
+  CALL(nullptr, md_write_coords_txt(coords.c_str(), n, pos.data(), mm.data(), ea.data(), tInt));
+  CALL(nullptr, md_export_records_txt(o.out.c_str(), rec.data(), (int64_t)(rec.size() / 8), tInt, steps));
+  if (tDev != tInt || sDev != steps)
+    std::printf("note: device time %.17g after %lld steps, host %.17g after %lld\n", tDev, (long long)sDev, tInt,
+                (long long)steps);
+  md_ctx_destroy(ctx);
+  std::printf("simulation ended successfully\n");
+  return 0;
+}

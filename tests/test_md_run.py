@@ -1,0 +1,103 @@
+"""The drop-in executable md_run (InitSimulation + RunSimulation of the
+reference, src/simulation.cpp:24-537, with the step on the GPU): command line
+and errors on CPU; on the GPU, the output files it writes equal those written
+from the same system stepped through the Python API, byte for byte."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import ref_io
+from helpers import ROOT
+
+EXE = os.path.join(ROOT, "md_sim_wolfschwenger_gb300", "_lib", "md_run")
+
+
+def _run(args, cwd, timeout=600):
+    return subprocess.run([EXE] + args, cwd=cwd, capture_output=True, text=True, timeout=timeout)
+
+
+def test_help_and_bad_arguments(tmp_path):
+    r = _run(["--help"], tmp_path)
+    assert r.returncode == 0 and "usage: md_run" in r.stdout
+    r = _run(["--bogus"], tmp_path)
+    assert r.returncode == 2 and "unknown option" in r.stderr
+    r = _run(["--precision", "half"], tmp_path)
+    assert r.returncode == 2
+
+
+def test_missing_configuration_is_reported(tmp_path):
+    run = tmp_path / "run"
+    run.mkdir()
+    r = _run([], run)  # ../configuration.ini does not exist
+    assert r.returncode == 1 and "md_config_load_ini" in r.stderr
+
+
+def _frames(path):
+    """coords.txt frames (lists of rows) and their time labels."""
+    frames, cur = [], []
+    for line in open(path):
+        vals = line.split()
+        if not vals:
+            if cur:
+                frames.append(np.array(cur, dtype=float))
+            cur = []
+            continue
+        cur.append([float(v) for v in vals])
+    if cur:
+        frames.append(np.array(cur, dtype=float))
+    return frames
+
+
+@pytest.mark.gpu
+def test_outputs_equal_python_api_run(tmp_path):
+    import md_sim_wolfschwenger_gb300 as m
+    from md_sim_wolfschwenger_gb300 import outputs
+    ini = ref_io.ini_dict(npDim=4, tMag=1e-10, tRelax=5e-11, deltaTinit=1e-12, magFluxDens=0.02, seed=7,
+                          INIT_CONFIG_ROT=2, volFrac=0.05)
+    ini["output_settings"]["npCoords"] = 10
+    ref_io.write_ini(tmp_path / "configuration.ini", ini)
+    run = tmp_path / "run"
+    run.mkdir()
+    r = _run(["--precision", "mixed", "--chunk", "37", "--quiet"], run)
+    assert r.returncode == 0, r.stderr
+    assert "simulation ended successfully" in r.stdout
+    names = sorted(os.listdir(run))
+    assert names == sorted(["data.txt", "coords.txt", "dtMean.txt", "Pxy.txt", "Pxz.txt", "Pyz.txt", "MSDx.txt",
+                            "MSDy.txt", "MSDz.txt", "mz.txt", "t.txt"])
+
+    # the same run through the Python API
+    cfg = m.Configuration.from_ini(tmp_path / "configuration.ini")
+    n = cfg.numb_part()
+    rMag, rHydr, pos, mm, ea, L = m.init_system(cfg, n, 7)
+    sim = m.Simulation(cfg, n, m.MD_PREC_MIXED, rMag=rMag, rHydr=rHydr)
+    sim.set_state(pos, mm, ea)
+    a, rc, kc, _, _ = sim.ewald_params()
+    sim.set_ewald(a, rc, kc)
+    sim.set_noise(m.MD_NOISE_PHILOX, 7)
+    t, steps, nframes = 0.0, 0, 0
+    while t <= cfg.c.tEnd:  # RunSimulation's loop and frame test, src/simulation.cpp:466-494
+        if np.floor(t / cfg.c.tEnd * cfg.c.npCoords) == nframes:
+            nframes += 1
+        t += cfg.c.deltaTinit
+        steps += 1
+    sim.step(steps, cfg.c.deltaTinit)
+    rec = sim.records()
+    p, mm2, ea2 = sim.get_state()
+    sim.close()
+    ref = tmp_path / "api"
+    ref.mkdir()
+    outputs.export_records(str(ref), rec, t, steps)
+    outputs.write_data(ref / "data.txt", cfg, rMag, rHydr, L)
+    for nm in ("dtMean.txt", "Pxy.txt", "Pxz.txt", "Pyz.txt", "MSDx.txt", "MSDy.txt", "MSDz.txt", "mz.txt", "t.txt",
+               "data.txt"):
+        assert (run / nm).read_bytes() == (ref / nm).read_bytes(), nm
+    # coords: the loop's frames plus the final one; the last equals the API's final state
+    fr = _frames(run / "coords.txt")
+    assert nframes >= 10 and len(fr) == nframes + 1 and all(f.shape == (n, 10) for f in fr)
+    assert fr[0][0, 9] == 0.0 and fr[-1][0, 9] == float(f"{t:g}")
+    outputs.write_coords(ref / "final.txt", p, mm2, ea2, 0.0)
+    last = _frames(ref / "final.txt")[0]
+    np.testing.assert_array_equal(fr[-1][:, :9], last[:, :9])
+    assert len(np.loadtxt(run / "mz.txt")) == steps
