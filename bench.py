@@ -84,20 +84,17 @@ def workload_config(n, seed):
             volFrac=W["phi"], magFluxDens=W["B0"], tMag=1.0,
             tRelax=0.0, deltaTinit=1e-12, satMag=4.8e5, anisEn=1.1e4, magDamp=0.1, temp=300.0, visOverride=1e-3,
             numbPartOverride=n, errTolEwald=1e-5, seed=seed, SOLVER=0, ENABLE_MOBILIZATION=1, ENABLE_THERM_FIELD=1,
-            ENABLE_THERM_TORQUE=1, ENABLE_THERM_FORCE=1, ENABLE_COATING_POT=0, INIT_CONFIG_ROT=2,
+            ENABLE_THERM_TORQUE=1, ENABLE_THERM_FORCE=1, ENABLE_COATING_POT=0, INIT_CONFIG_ROT=4,
             INIT_CONFIG_TRANS=1, precision=MD_PREC_MIXED, noise=MD_NOISE_PHILOX)
     return cfg
 
 
 def workload_state(n, seed):
-    from md_sim_wolfschwenger_gb300 import init
-    rng = np.random.default_rng(1000 + seed)
-    rMag = init.lognormal_radii(n, W["median"], W["sigma"], rng)
-    rHydr = rMag + 5e-9
-    L = init.box_length(rHydr, W["phi"])
-    pos = init.rsa_positions(L, rHydr, rng)
-    mm = init.uniform_directions(n, rng)
-    ea = init.uniform_directions(n, rng)
+    """Initial system from the library's InitParticleProps + InitCoordsFromSketch
+    (md_init_system: log-normal radii, random sequential addition placed
+    largest first, moments and easy axes independent and uniform)."""
+    import md_sim_wolfschwenger_gb300 as m
+    rMag, rHydr, pos, mm, ea, L = m.init_system(workload_config(n, seed), n, 1000 + seed)
     return rMag, rHydr, L, pos, mm, ea
 
 
@@ -280,14 +277,48 @@ def _pct(xs, q):
     return xs[lo] + (xs[hi] - xs[lo]) * (k - lo)
 
 
+def contact_scales(cfg, rMag, rHydr):
+    """Contact force, field and torque of the smallest particles
+    (CompEwaldParams / CheckEwaldSum, src/interaction.cpp:180-181, 743-753):
+    the scales of the reference's relative error."""
+    mu0, pi, ms = cfg.c.mu0, cfg.c.my_pi, cfg.c.satMag
+    mmin = float(np.min(ms * 4.0 / 3.0 * pi * np.asarray(rMag) ** 3))
+    rh = float(np.min(rHydr))
+    return (3 * mu0 * mmin ** 2 / (2 * pi * (2 * rh) ** 4), mu0 * mmin / (2 * pi * (2 * rh) ** 3),
+            mmin ** 2 * mu0 / (16 * pi * rh ** 3))
+
+
+def rms_rel(a, b, scale):
+    d = np.asarray(a) - np.asarray(b)
+    return math.sqrt(float((d * d).sum()) / d.shape[-1]) / scale
+
+
 def fp64_plain(n, sysd, ewald, seed, steps=4, warm=1):
     """The same system and Ewald parameters on the plain FP64 path
     (MD_PREC_FP64, one instance): particle-steps/s from CUDA events on the
-    library's stream."""
+    library's stream; and the mixed path's error against it on the initial
+    state (CompInteractions: field, force, torque mu x B; contact-normalised
+    RMS over particles, the reference's error metric)."""
     import torch
-    from md_sim_wolfschwenger_gb300 import MD_NOISE_PHILOX, MD_PREC_FP64, Simulation
+    from md_sim_wolfschwenger_gb300 import MD_NOISE_PHILOX, MD_PREC_FP64, MD_PREC_MIXED, Simulation
     rMag, rHydr, L, pos, mm, ea = sysd
-    sim = Simulation(workload_config(n, seed), n, MD_PREC_FP64, rMag=rMag, rHydr=rHydr)
+    cfg = workload_config(n, seed)
+    out = {}
+    for prec in (MD_PREC_MIXED, MD_PREC_FP64):
+        sim = Simulation(cfg, n, prec, rMag=rMag, rHydr=rHydr)
+        sim.set_state(pos, mm, ea)
+        sim.set_ewald(*ewald)
+        out[prec] = sim.CompInteractions()[:2]
+        sim.close()
+    fAl, bAl, tAl = contact_scales(cfg, rMag, rHydr)
+    mom = cfg.c.satMag * 4.0 / 3.0 * cfg.c.my_pi * np.asarray(rMag) ** 3
+    tq = {p: np.cross((np.asarray(mm) * mom).T, out[p][0].T).T for p in out}
+    err = {"B": rms_rel(out[MD_PREC_MIXED][0], out[MD_PREC_FP64][0], bAl),
+           "F": rms_rel(out[MD_PREC_MIXED][1], out[MD_PREC_FP64][1], fAl),
+           "torque": rms_rel(tq[MD_PREC_MIXED], tq[MD_PREC_FP64], tAl),
+           "metric": "RMS over particles of |mixed - fp64| / contact value (CheckEwaldSum's metric); the "
+                     "Ewald truncation budget is 1e-5"}
+    sim = Simulation(cfg, n, MD_PREC_FP64, rMag=rMag, rHydr=rHydr)
     sim.set_state(pos, mm, ea)
     sim.set_ewald(*ewald)
     sim.set_noise(MD_NOISE_PHILOX, seed)
@@ -304,7 +335,8 @@ def fp64_plain(n, sysd, ewald, seed, steps=4, warm=1):
     ms = e0.elapsed_time(e1) / steps
     sim.close()
     return {"value": n / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms, "steps": steps,
-            "dtype": "f64", "note": "same system and Ewald parameters, plain FP64 path, one instance"}
+            "dtype": "f64", "note": "same system and Ewald parameters, plain FP64 path, one instance",
+            "mixed_error_vs_fp64": err}
 
 
 def sweep_sample(replicas, steps, seed=3):
@@ -453,36 +485,37 @@ def run_ours(args):
         sim.set_ewald(alpha, rc, kc)
     _, _, _, errF, errT = sim.ewald_params(rc)
     sim.set_noise(MD_NOISE_PHILOX, seed)
-    sim.profile(True)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     sim.step(args.warmup, 1e-12)
     sim.sync()
     launches_per_step = sim.launches() // max(1, args.warmup)
-    seg_sum = None
+    ext = torch.cuda.ExternalStream(sim.stream())
     clocks = ClockSampler(local)
     barrier(ws)
     torch.cuda.synchronize()
     clocks.start()
-    total_ms = 0.0
+    # timed steps: the production graph (real- and k-space branches
+    # concurrent), CUDA events on the library's stream around each step,
+    # L2 flushed before each
+    evs = []
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            e0.record()
         sim.step(1, 1e-12)
-        seg = sim.profile_read()
-        total_ms += sum(seg.values())
-        seg_sum = seg if seg_sum is None else {k: seg_sum[k] + v for k, v in seg.items()}
+        with torch.cuda.stream(ext):
+            e1.record()
+        evs.append((e0, e1))
     torch.cuda.synchronize()
     barrier(ws)
+    total_ms = sum(a.elapsed_time(b) for a, b in evs)
     total_ms = allmax(total_ms, ws)
     value = ws * n * args.steps / (total_ms * 1e-3)
-    seg_mean = {k: v / args.steps for k, v in seg_sum.items()}
-    pairs = sim.pairs()
-    nk_real = len(sim.debug_structure_factor())
 
     # continuous run (graph replays back to back, no flush) for reference
-    sim.profile(False)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ext = torch.cuda.ExternalStream(sim.stream())
     with torch.cuda.stream(ext):
         e0.record()
     sim.step(args.steps, 1e-12)
@@ -490,6 +523,23 @@ def run_ours(args):
         e1.record()
     torch.cuda.synchronize()
     cont_ms = e0.elapsed_time(e1) / args.steps
+
+    # per-kernel durations: a profiled pass, kernels one after another with
+    # CUDA events between them (inside the replayed graph), L2 flushed per step
+    sim.profile(True)
+    sim.step(1, 1e-12)
+    seg_sum, psteps = None, max(5, min(args.steps, 50))
+    for _ in range(psteps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        sim.step(1, 1e-12)
+        seg = sim.profile_read()
+        seg_sum = seg if seg_sum is None else {k: seg_sum[k] + v for k, v in seg.items()}
+    sim.profile(False)
+    seg_mean = {k: v / psteps for k, v in seg_sum.items()}
+    serial_ms = sum(seg_mean.values())
+    pairs = sim.pairs()
+    nk_real = len(sim.debug_structure_factor())
     clk = clocks.stop()  # sampled over both timed runs
 
     # end to end through the C ABI with pinned host buffers, copies timed
@@ -578,17 +628,21 @@ def run_ours(args):
                 "precision": ("fp64 (plain)" if prec == MD_PREC_FP64 else
                               "mixed: FP32 pair maths, phases, scatter and integrator; FP64 structure-factor "
                               "sums across chunks, self/surface terms, positions, reductions"),
-                "data": "synthetic (seeded log-normal radii, random sequential addition, uniform orientations)",
+                "data": "synthetic (seeded log-normal radii, random sequential addition, moments and easy axes "
+                        "independent and uniform on the sphere)",
                 "config": {"workload": W["desc"], "n": n, "lBox_m": L, "replicas_per_gpu": 1,
                            "parallelism": f"replicas x{ws}" if ws > 1 else "single instance",
                            "ewald": {"alpha_L": alpha * L, "rc_over_L": rc / L, "kc": kc,
                                      "pred_force_err_rel_contact": errF, "pred_torque_err_rel_contact": errT,
                                      "pairs": pairs, "k_vectors": nk_real},
-                           "l2": "flushed between timed steps (256 MiB write); step time from in-graph CUDA events "
-                                 "on the library's stream"},
+                           "l2": "flushed between timed steps (256 MiB write); step time from CUDA events on the "
+                                 "library's stream around each step's graph launch"},
                 "e2e": e2e, "roofline": roofline, "segments": segs,
                 "continuous": {"ms_per_step": cont_ms, "value": ws * n / (cont_ms * 1e-3),
                                "note": "graph replays back to back without L2 flush"},
+                "serialized": {"ms_per_step": serial_ms, "steps": psteps,
+                               "note": "the profiled pass: the same kernels one after another (no branch "
+                                       "concurrency), the sum of the segments; per-kernel figures come from it"},
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches_per_step * args.steps,
                 "fp64_plain": fp64, "mixed_over_fp64_plain": (value / fp64["value"]) if fp64 else None,
                 "sweep": sweep, "serving": serving}

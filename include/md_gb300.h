@@ -225,6 +225,10 @@ int md_debug_launches(const md_ctx* ctx, int64_t* launches);
 /* In-range particle pairs (each unordered pair once) of the last full
  * real-space evaluation: the entries CompInteractVecs would list. */
 int md_debug_pairs(md_ctx* ctx, int64_t* pairs);
+/* Real-space field and force alone (no k-space, self or surface terms) of
+ * the last md_compute_interactions, N x 3 column-major SI: the part of
+ * CompDipInteractEwaldR (src/interaction.cpp:383-422). */
+int md_debug_real_part(md_ctx* ctx, double* B, double* F);
 /* Skin of the real-space neighbour list as a fraction of rc (default 0.02):
  * the list holds pairs within rc (1 + skin) and is rebuilt on the device when
  * a particle has moved more than skin rc / 2 since the last build. */

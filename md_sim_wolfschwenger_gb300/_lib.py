@@ -124,6 +124,7 @@ def lib():
         "md_debug_structure_factor": (C.c_int, [V, PI64, P]),
         "md_debug_launches": (C.c_int, [V, PI64]),
         "md_debug_pairs": (C.c_int, [V, PI64]),
+        "md_debug_real_part": (C.c_int, [V, P, P]),
         "md_set_neighbor_skin": (C.c_int, [V, C.c_double]),
         "md_debug_neighbor_capacity": (C.c_int, [V, I64, PI64]),
         "md_profile": (C.c_int, [V, C.c_int]),

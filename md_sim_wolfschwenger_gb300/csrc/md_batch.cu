@@ -64,6 +64,9 @@ struct md_batch {
   int64_t round_steps = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_round_ms = 0;
+  // k-space branch of the packed step, concurrent with the real-space branch
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev[2] = {}, join_ev[2] = {};
 };
 
 namespace {
@@ -180,15 +183,30 @@ int pack(md_batch* b) {
   cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
   if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
   int64_t l = 0;
+  // the k-space branches run on the side stream, concurrently with the
+  // real-space branches (parallel branches of the captured graph)
+  cudaStream_t k = b->side;
+  auto fork = [&](int q) {
+    cudaEventRecord(b->fork_ev[q], s);
+    cudaStreamWaitEvent(k, b->fork_ev[q], 0);
+  };
+  auto join = [&](int q) {
+    cudaEventRecord(b->join_ev[q], k);
+    cudaStreamWaitEvent(s, b->join_ev[q], 0);
+  };
   l += launch_step_begin_packed(s, b->d_cell, R);
   l += launch_cells_packed(s, b->d_cell, R, b->n256, b->sort);
+  fork(0);
+  l += launch_phase_tables_packed(k, b->d_kfull, b->phase);
+  l += launch_kspace_packed(k, b->d_kfull, b->sk, b->red, b->sc, true, b->kcmax, b->np);
   l += launch_nbr_packed(s, b->d_rfull, R, b->real);
-  l += launch_phase_tables_packed(s, b->d_kfull, b->phase);
   l += launch_real_packed(s, b->d_rfull, b->real, true, b->coat);
-  l += launch_kspace_packed(s, b->d_kfull, b->sk, b->red, b->sc, true, b->kcmax, b->np);
+  join(0);
   l += launch_heun1_packed(s, b->d_i1, b->n256);
+  fork(1);
+  l += launch_kspace_packed(k, b->d_kfield, b->sk, b->red, b->sc, false, b->kcmax, b->np);
   l += launch_real_packed(s, b->d_rfield, b->real, false, false);
-  l += launch_kspace_packed(s, b->d_kfield, b->sk, b->red, b->sc, false, b->kcmax, b->np);
+  join(1);
   l += launch_heun2_packed(s, b->d_i2, b->n256);
   l += launch_obs_packed(s, b->d_obs, R);
   e = cudaStreamEndCapture(s, &b->graph);
@@ -276,8 +294,13 @@ int md_batch_create(int64_t capacity, md_batch** out) {
     return s;
   };
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
     return fail(set_err(nullptr, MD_ERR_CUDA, "batch stream/events"));
+  for (int q = 0; q < 2; q++)
+    if (cudaEventCreateWithFlags(&b->fork_ev[q], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->join_ev[q], cudaEventDisableTiming) != cudaSuccess)
+      return fail(set_err(nullptr, MD_ERR_CUDA, "batch events"));
   const size_t C = (size_t)capacity;
   if ((st = alloc_array(&b->d_cell, C)) || (st = alloc_array(&b->d_rfull, C)) || (st = alloc_array(&b->d_rfield, C)) ||
       (st = alloc_array(&b->d_kfull, C)) || (st = alloc_array(&b->d_kfield, C)) || (st = alloc_array(&b->d_i1, C)) ||
@@ -299,6 +322,11 @@ int md_batch_destroy(md_batch* b) {
     if (p) cudaFree(p);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
+  for (int q = 0; q < 2; q++) {
+    if (b->fork_ev[q]) cudaEventDestroy(b->fork_ev[q]);
+    if (b->join_ev[q]) cudaEventDestroy(b->join_ev[q]);
+  }
+  if (b->side) cudaStreamDestroy(b->side);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return MD_OK;

@@ -63,6 +63,7 @@ int dalloc_raw(md_ctx* c, void** p, size_t bytes) {
   if (e != cudaSuccess)
     return set_err(c, MD_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
   c->allocs.push_back(q);
+  c->alloc_bytes.push_back(bytes);
   c->bytes += (int64_t)bytes;
   *p = q;
   return MD_OK;
@@ -71,7 +72,12 @@ int dalloc_raw(md_ctx* c, void** p, size_t bytes) {
 void dfree(md_ctx* c, void* p) {
   if (!p) return;
   auto it = std::find(c->allocs.begin(), c->allocs.end(), p);
-  if (it != c->allocs.end()) c->allocs.erase(it);
+  if (it != c->allocs.end()) {
+    const size_t k = (size_t)(it - c->allocs.begin());
+    c->bytes -= (int64_t)c->alloc_bytes[k];
+    c->alloc_bytes.erase(c->alloc_bytes.begin() + (ptrdiff_t)k);
+    c->allocs.erase(it);
+  }
   cudaFree(p);
 }
 
@@ -111,6 +117,7 @@ RealParams real_params(md_ctx* c, void* B, void* F, void* ov) {
   p.alpha = a;
   p.rc = rcb;
   p.rc2 = rcb * rcb;
+  p.rc2_fix = (unsigned long long)std::ldexp(rcb * rcb, 64);  // rcb <= 1/2: below 2^62
   const double rt = rcb * (1.0 + 1e-6) + 2e-7;
   p.rc2_test = rt * rt;
   p.c2a = 2.0 * a * g.irPi;
@@ -276,6 +283,33 @@ int check_ready(md_ctx* c, bool need_state) {
   return MD_OK;
 }
 
+// Real-space work and k-space work read the same sorted state and write
+// separate outputs: they run concurrently, the k-space branch on the side
+// stream (fork/join through events, which stream capture turns into parallel
+// graph branches), so each fills the SMs the other's partial waves leave
+// idle.  Each branch is a short preparation (neighbour list / phase tables)
+// and its main kernels.  While per-segment profiling is on, everything runs
+// on the main stream in the order prep, prep, real, k-space, with the
+// segment events before the real and the k-space kernels.
+template <class RP, class RM, class KP, class KM>
+static int fork_join(md_ctx* c, int q, int seg_real, int seg_k, RP&& real_prep, RM&& real, KP&& k_prep,
+                     KM&& kspace) {
+  if (c->prof) {
+    int l = real_prep(c->stream) + k_prep(c->stream);
+    mark(c, seg_real);
+    l += real(c->stream);
+    mark(c, seg_k);
+    return l + kspace(c->stream);
+  }
+  cudaEventRecord(c->fork_ev[q], c->stream);
+  cudaStreamWaitEvent(c->side, c->fork_ev[q], 0);
+  int l = k_prep(c->side) + kspace(c->side);
+  l += real_prep(c->stream) + real(c->stream);
+  cudaEventRecord(c->join_ev[q], c->side);
+  cudaStreamWaitEvent(c->stream, c->join_ev[q], 0);
+  return l;
+}
+
 // Field + force evaluation on the current master state (no integrator).
 static int issue_interactions(md_ctx* c) {
   int l = 0;
@@ -284,26 +318,38 @@ static int issue_interactions(md_ctx* c) {
   l += launch_step_begin(c->stream, cp.flags, cp.half_skin);
   l += launch_cells(c->stream, cp, fp64(c));
   cudaMemsetAsync(&c->sc->pairs, 0, sizeof(unsigned long long), c->stream);
-  l += launch_nbr(c->stream, real_params(c, nullptr, nullptr, nullptr), &c->sc->flags, fp64(c));
-  l += launch_phase_tables(c->stream, k_params(c, nullptr, nullptr), fp64(c));
-  mark(c, MD_SEG_REAL_FULL);
-  l += launch_real(c->stream, real_params(c, c->Br, c->Fr, c->ov), true, fp64(c));
-  mark(c, MD_SEG_KSF_FULL);
-  l += launch_kspace(c->stream, k_params(c, c->Bk, c->Fk), true, fp64(c), c->prof ? &c->ev[MD_SEG_KRED_FULL] : nullptr);
+  l += fork_join(
+      c, 0, MD_SEG_REAL_FULL, MD_SEG_KSF_FULL,
+      [&](cudaStream_t st) { return launch_nbr(st, real_params(c, nullptr, nullptr, nullptr), &c->sc->flags, fp64(c)); },
+      [&](cudaStream_t st) { return launch_real(st, real_params(c, c->Br, c->Fr, c->ov), true, fp64(c)); },
+      [&](cudaStream_t st) { return launch_phase_tables(st, k_params(c, nullptr, nullptr), fp64(c)); },
+      [&](cudaStream_t st) {
+        return launch_kspace(st, k_params(c, c->Bk, c->Fk), true, fp64(c),
+                             c->prof ? &c->ev[MD_SEG_KRED_FULL] : nullptr);
+      });
   c->have_geometry = true;
   c->list_valid = true;
   return l;
+}
+
+// Field-only evaluation (CompDemagField) for the moments in the sorted view.
+static int issue_field(md_ctx* c) {
+  auto none = [](cudaStream_t) { return 0; };
+  return fork_join(
+      c, 1, MD_SEG_REAL_FIELD, MD_SEG_KSF_FIELD, none,
+      [&](cudaStream_t st) { return launch_real(st, real_params(c, c->Br2, nullptr, nullptr), false, fp64(c)); },
+      none,
+      [&](cudaStream_t st) {
+        return launch_kspace(st, k_params(c, c->Bk2, nullptr), false, fp64(c),
+                             c->prof ? &c->ev[MD_SEG_KRED_FIELD] : nullptr);
+      });
 }
 
 static int issue_step(md_ctx* c, double dt) {
   int l = issue_interactions(c);
   mark(c, MD_SEG_HEUN1);
   l += launch_heun1(c->stream, int_params(c, dt, c->Br, c->Bk), fp64(c));
-  mark(c, MD_SEG_REAL_FIELD);
-  l += launch_real(c->stream, real_params(c, c->Br2, nullptr, nullptr), false, fp64(c));
-  mark(c, MD_SEG_KSF_FIELD);
-  l += launch_kspace(c->stream, k_params(c, c->Bk2, nullptr), false, fp64(c),
-                     c->prof ? &c->ev[MD_SEG_KRED_FIELD] : nullptr);
+  l += issue_field(c);
   mark(c, MD_SEG_HEUN2);
   l += launch_heun2(c->stream, int_params(c, dt, c->Br2, c->Bk2), fp64(c));
   mark(c, MD_SEG_OBS);
@@ -345,8 +391,9 @@ int check_overflow(md_ctx* c) {
   const long long need = (total > 0 && total < 0x7fffffff) ? (long long)(total * 1.25) + 16LL * c->n : 2 * c->nbr_cap;
   int st = alloc_nbr(c, need);
   if (st) return st;
-  static const int zero = 0;
-  CK(c, cudaMemcpyAsync(&c->sc->flags.overflow, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  // The overflow flag stays set until the next rebuild (which recounts the
+  // list against the new capacity): a field-only evaluation before that
+  // (md_compute_field) must scan the cells, since the list was never filled.
   return force_rebuild(c);
 }
 
@@ -453,8 +500,13 @@ int md_ctx_create(const md_config* cfg, int64_t n, int precision, md_ctx** out) 
     md_ctx_destroy(c);
     return s;
   };
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess)
     return fail(set_err(nullptr, MD_ERR_CUDA, "cudaStreamCreate failed"));
+  for (int q = 0; q < 2; q++)
+    if (cudaEventCreateWithFlags(&c->fork_ev[q], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->join_ev[q], cudaEventDisableTiming) != cudaSuccess)
+      return fail(set_err(nullptr, MD_ERR_CUDA, "cudaEventCreate failed"));
   const size_t N = (size_t)n, T = tsz(c);
   double** d3[] = {&c->pos, &c->mm, &c->ea, &c->truePos, &c->posRef, &c->tmpmm, &c->Bout, &c->Fout};
   for (auto p : d3)
@@ -497,8 +549,15 @@ int md_ctx_destroy(md_ctx* c) {
   invalidate_graph(c);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  if (c->side) cudaStreamSynchronize(c->side);
   for (void* p : c->allocs) cudaFree(p);
   c->allocs.clear();
+  c->alloc_bytes.clear();
+  for (int q = 0; q < 2; q++) {
+    if (c->fork_ev[q]) cudaEventDestroy(c->fork_ev[q]);
+    if (c->join_ev[q]) cudaEventDestroy(c->join_ev[q]);
+  }
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return MD_OK;
@@ -679,12 +738,16 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
   const double w = std::pow(c->cfg.my_pi / ab, 2.0);
   c->klist = mdh::build_klist((int)kc, w);
   c->grid = mdh::choose_grid(rc / c->L, c->n, 2);
-  // structure-factor grid: ~4 waves of blocks over the SMs
+  // structure-factor grid (segment blocks x particle chunks): the fewest
+  // whole waves of resident blocks that keep every FP32 chunk sum within 512
+  // particles, with the chunk count chosen to fill those waves
   int nsm = 148;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
-  const int nsegb = (int)((c->klist.seg.size() + 255) / 256);
-  int nch = std::max(1, (4 * nsm + nsegb - 1) / nsegb);
-  nch = std::max<int64_t>(nch, (c->n + 511) / 512);  // FP32 sums over <= 512 particles
+  const int nsegb = (int)((c->klist.seg.size() + md::sk_threads() - 1) / md::sk_threads());
+  const int64_t slots = (int64_t)nsm * md::sk_resident_blocks((int)kc, fp64(c));
+  const int64_t nch_min = std::max<int64_t>(1, (c->n + 511) / 512);
+  const int64_t waves = std::max<int64_t>(1, (nsegb * nch_min + slots - 1) / slots);
+  int64_t nch = std::max<int64_t>(nch_min, waves * slots / nsegb);
   nch = std::min<int64_t>(nch, (c->n + 31) / 32);
   c->chunk = (int)(((c->n + nch - 1) / nch + 31) / 32 * 32);
   c->nchunk = (int)((c->n + c->chunk - 1) / c->chunk);
@@ -798,8 +861,7 @@ int md_compute_field(md_ctx* c, const double* mm, double* B) {
   CK(c, cudaMemcpyAsync(c->tmpmm, mm, 24 * (size_t)c->n, cudaMemcpyHostToDevice, c->stream));
   SortedView s = sorted_view(c);
   c->launches = launch_set_mu(c->stream, (int)c->n, c->tmpmm, c->magMom_u, c->rMag_u, s, fp64(c));
-  c->launches += launch_real(c->stream, real_params(c, c->Br2, nullptr, nullptr), false, fp64(c));
-  c->launches += launch_kspace(c->stream, k_params(c, c->Bk2, nullptr), false, fp64(c));
+  c->launches += issue_field(c);
   IntParams ip = int_params(c, 0.0, c->Br2, c->Bk2);
   c->launches += launch_combine(c->stream, ip, c->Bout, nullptr, 0, fp64(c));
   CK(c, cudaGetLastError());
@@ -974,6 +1036,18 @@ int md_set_neighbor_skin(md_ctx* c, double skin_frac) {
     if (int st = alloc_nbr(c, (long long)(1.3 * est) + 64LL * c->n)) return st;
   }
   return force_rebuild(c);
+}
+
+int md_debug_real_part(md_ctx* c, double* B, double* F) {
+  if (!c || !B || !F) return set_err(c, MD_ERR_INVALID, "null argument");
+  if (!c->have_geometry) return set_err(c, MD_ERR_INVALID, "call md_compute_interactions first");
+  IntParams ip = int_params(c, 0.0, c->Br, c->Bk);
+  launch_real_part(c->stream, ip, c->Bout, c->Fout, fp64(c));
+  CK(c, cudaGetLastError());
+  CK(c, cudaMemcpyAsync(B, c->Bout, 24 * (size_t)c->n, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(F, c->Fout, 24 * (size_t)c->n, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return MD_OK;
 }
 
 int md_debug_neighbor_capacity(md_ctx* c, int64_t cap, int64_t* used) {

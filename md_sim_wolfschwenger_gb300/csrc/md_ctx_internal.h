@@ -37,9 +37,14 @@ struct md_ctx {
   int prec = MD_PREC_MIXED;
   int device = 0;
   cudaStream_t stream = nullptr;
+  // second stream of the step: the k-space branch runs on it concurrently
+  // with the real-space branch (fork/join events; captured into the graph)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev[2] = {}, join_ev[2] = {};
   std::string err;
   int err_status = 0;
   std::vector<void*> allocs;
+  std::vector<size_t> alloc_bytes;  // size of each entry of allocs
   int64_t bytes = 0;
 
   // host state

@@ -69,9 +69,11 @@ __device__ __forceinline__ void rk(const IntParams& p, const T m[3], const T e[3
   km[2] = -vm * (x2 + md * y2);
 }
 
-// Demagnetising field of particle i (sorted slot r) in SI.
-template <typename T>
-__device__ __forceinline__ void demag_si(const IntParams& p, int r, T b[3]) {
+// Demagnetising field of particle i (sorted slot r) in SI: the real- and
+// k-space sums and the self and surface terms combined in FP64, then
+// returned in the integrator's type T.
+template <typename T, typename R = T>
+__device__ __forceinline__ void demag_si(const IntParams& p, int r, R b[3]) {
   using T4 = typename V4<T>::t;
   const int n = p.n;
   const T* Br = (const T*)p.Br;
@@ -81,7 +83,7 @@ __device__ __forceinline__ void demag_si(const IntParams& p, int r, T b[3]) {
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     const double selfsurf = p.cself * mu3[a] - p.csurf * p.musum[a];
-    b[a] = (T)((((double)Br[a * n + r] + (double)Bk[a * n + r]) + selfsurf) * p.B_unit);
+    b[a] = (R)((((double)Br[a * n + r] + (double)Bk[a * n + r]) + selfsurf) * p.B_unit);
   }
 }
 
@@ -304,15 +306,38 @@ __global__ void k_combine(IntParams p, double* Bout, double* Fout, int apply_ove
   const int n = p.n;
   if (i >= n) return;
   const int r = p.s.rank[i];
-  T b[3];
-  demag_si<T>(p, r, b);
+  double b[3];  // reported field: no rounding to the integrator's type
+  demag_si<T, double>(p, r, b);
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    if (Bout) Bout[a * n + i] = (double)b[a];
+    if (Bout) Bout[a * n + i] = b[a];
     if (Fout)
       Fout[a * n + i] = ((double)((const T*)p.Fr)[a * n + r] + (double)((const T*)p.Fk)[a * n + r]) * p.F_unit;
     if (apply_overlap) p.pos[a * n + i] += (double)((const T*)p.ov)[a * n + r] * p.L;
   }
+}
+
+// Real-space part alone (field without the k-space, self and surface terms;
+// force without the k-space force), particle order, SI.
+template <typename T>
+__global__ void k_real_part(IntParams p, double* Bout, double* Fout) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = p.n;
+  if (i >= n) return;
+  const int r = p.s.rank[i];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    Bout[a * n + i] = (double)((const T*)p.Br)[a * n + r] * p.B_unit;
+    Fout[a * n + i] = (double)((const T*)p.Fr)[a * n + r] * p.F_unit;
+  }
+}
+
+int launch_real_part(cudaStream_t st, const IntParams& p, double* Bout, double* Fout, bool fp64) {
+  if (fp64)
+    k_real_part<double><<<(p.n + 255) / 256, 256, 0, st>>>(p, Bout, Fout);
+  else
+    k_real_part<float><<<(p.n + 255) / 256, 256, 0, st>>>(p, Bout, Fout);
+  return 1;
 }
 
 int int_blocks(int n) { return (n + kIntThreads - 1) / kIntThreads; }

@@ -23,6 +23,10 @@ int cell_sort_blocks(const CellGrid& g);
 int real_blocks(int n);                 // real space and neighbour list
 int phase_blocks(int n);
 int sk_blocks(const KParams& p);
+// Threads (segments) per structure-factor block, and how many such blocks
+// one SM holds at once for kc.
+int sk_threads();
+int sk_resident_blocks(int kc, bool fp64);
 int skred_blocks(const KParams& p);
 int scatter_blocks(const KParams& p, int np);
 int int_blocks(int n);
@@ -72,6 +76,8 @@ int launch_heun1_packed(cudaStream_t st, const IntParams* ps, const Packed& n256
 int launch_heun2_packed(cudaStream_t st, const IntParams* ps, const Packed& n256);
 int launch_obs_packed(cudaStream_t st, const ObsParams* ps, int R);
 // B, F in SI (orig order, double) from the stage outputs; optional overlap push.
+// Real-space field and force alone of the last full evaluation (test hook).
+int launch_real_part(cudaStream_t st, const IntParams& p, double* Bout, double* Fout, bool fp64);
 int launch_combine(cudaStream_t st, const IntParams& p, double* Bout, double* Fout, int apply_overlap,
                    bool fp64);
 

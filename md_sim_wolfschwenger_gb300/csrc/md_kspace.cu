@@ -37,7 +37,7 @@
 
 namespace md {
 
-constexpr int kSkThreads = 256;
+constexpr int kSkThreads = 128;
 constexpr int kSkTile = 64;
 constexpr int kSegMax = 16;
 
@@ -312,10 +312,12 @@ __device__ __forceinline__ void kscatter(const KParams& p, int bx, int kcmax) {
       if (sg.nx0 < 0) X.y = -X.y;
       T pr, pi;
       cmul<T>(X.x, X.y, yzr, yzi, pr, pi);
-      T nxf = (T)sg.nx0;
-      T w = 0;
-      if constexpr (FULL) w = nxf * mu.x + (T)sg.ny * mu.y + (T)sg.nz * mu.z;
-      T gx = 0, gs = 0, hx = 0, hs = 0;
+      // k = (nx0 + u, ny, nz), u = 0..len-1.  With G_u = Re(conj(eS) phase)
+      // and H_u = Im(conj(eS) phase), the field needs sum G_u n_u and the
+      // force sum H_u (n_u . mu) n_u; both follow from the moments
+      // sum u^p G_u (p <= 1) and sum u^p H_u (p <= 2), whose weights u, u^2
+      // are constants of the unrolled loop.
+      T g0 = 0, g1 = 0, h0 = 0, h1 = 0, h2 = 0;
       const T2* es_seg = es_s + ko;
 #pragma unroll
       for (int q = 0; q < kSegMax; q += 4) {
@@ -323,27 +325,30 @@ __device__ __forceinline__ void kscatter(const KParams& p, int bx, int kcmax) {
 #pragma unroll
         for (int u = 0; u < 4; u++) {
           const T2 es = es_seg[q + u];
+          const T uf = (T)(q + u);
           const T g = es.x * pr + es.y * pi;
-          gx += g * nxf;
-          gs += g;
+          g0 += g;
+          g1 += uf * g;
           if constexpr (FULL) {
-            const T h = (es.x * pi - es.y * pr) * w;
-            hx += h * nxf;
-            hs += h;
-            w += mu.x;
+            const T h = es.x * pi - es.y * pr;
+            h0 += h;
+            h1 += uf * h;
+            h2 += (uf * uf) * h;
           }
           const T npr = pr * E.x - pi * E.y;
           pi = pr * E.y + pi * E.x;
           pr = npr;
-          nxf += (T)1;
         }
       }
       ko += sg.len;
-      bb[0] += gx;
-      bb[1] += gs * (T)sg.ny;
-      bb[2] += gs * (T)sg.nz;
+      const T nx0 = (T)sg.nx0;
+      bb[0] += nx0 * g0 + g1;
+      bb[1] += g0 * (T)sg.ny;
+      bb[2] += g0 * (T)sg.nz;
       if constexpr (FULL) {
-        fb[0] += hx;
+        const T w0 = nx0 * mu.x + (T)sg.ny * mu.y + (T)sg.nz * mu.z;
+        const T hs = w0 * h0 + mu.x * h1;
+        fb[0] += w0 * nx0 * h0 + (w0 + mu.x * nx0) * h1 + mu.x * h2;
         fb[1] += hs * (T)sg.ny;
         fb[2] += hs * (T)sg.nz;
       }
@@ -402,7 +407,7 @@ __global__ void __launch_bounds__(kPhaseThreads) k_phase_tables(KParams p) {
   phase_tables<T>(p, blockIdx.x);
 }
 template <typename T>
-__global__ void __launch_bounds__(kSkThreads, 3) k_sk(KParams p) {
+__global__ void __launch_bounds__(kSkThreads, 6) k_sk(KParams p) {
   sk_body<T>(p, blockIdx.x, blockIdx.y);
 }
 template <typename T>
@@ -420,7 +425,7 @@ __global__ void __launch_bounds__(kPhaseThreads) k_phase_tables_packed(const KPa
   const KParams p = ps[t.rep];
   phase_tables<float>(p, t.blk);
 }
-__global__ void __launch_bounds__(kSkThreads, 3) k_sk_packed(const KParams* __restrict__ ps,
+__global__ void __launch_bounds__(kSkThreads, 6) k_sk_packed(const KParams* __restrict__ ps,
                                                               const Task* __restrict__ tk) {
   const Task t = tk[blockIdx.x];
   const KParams p = ps[t.rep];
@@ -439,6 +444,22 @@ __global__ void __launch_bounds__(NP * kScatterParts) k_kscatter_packed(const KP
   const Task t = tk[blockIdx.x];
   const KParams p = ps[t.rep];
   kscatter<float, NP, FULL>(p, t.blk, kcmax);
+}
+
+int sk_threads() { return kSkThreads; }
+
+int sk_resident_blocks(int kc, bool fp64) {
+  int nb = 0;
+  const size_t sm = ksf_smem(kc, fp64);
+  cudaError_t e;
+  if (fp64) {
+    cudaFuncSetAttribute(k_sk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_sk<double>, kSkThreads, sm);
+  } else {
+    cudaFuncSetAttribute(k_sk<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_sk<float>, kSkThreads, sm);
+  }
+  return (e == cudaSuccess && nb > 0) ? nb : 1;
 }
 
 int phase_blocks(int n) { return (3 * n + kPhaseThreads - 1) / kPhaseThreads; }

@@ -244,6 +244,12 @@ class Simulation:
         self._ck(self.L.md_debug_structure_factor(self.h, C.byref(nk), _P(out)))
         return out
 
+    def debug_real_part(self):
+        """Real-space (B, F) alone of the last CompInteractions, (3, N) SI."""
+        B, F = np.empty((3, self.n)), np.empty((3, self.n))
+        self._ck(self.L.md_debug_real_part(self.h, _P(B), _P(F)))
+        return B, F
+
     def launches(self):
         v = C.c_int64()
         self._ck(self.L.md_debug_launches(self.h, C.byref(v)))
