@@ -30,6 +30,8 @@ struct orc_ctx {
   double *jac; /* Jacobi overlap displacement, N x 3 */
   /* Heun work arrays (IntCoefficient_S) */
   double *k1m, *k1e, *k2m, *k2e, *c2m, *c2e, *beff, *b2, *b3, *dot;
+  /* adaptive solvers: stage slopes k_s (m, n) and stage coordinates */
+  double *skm[7], *ske[7], *scm, *sce, *ebuf;
   /* Ewald constants (InitEwaldConst, interaction.cpp:353-374) */
   double nc2, w, cFluxDens, cForce, cSurf, cSelf, alpha2, alpha4, volBox;
   double Pxy, Pxz, Pyz;
@@ -70,6 +72,13 @@ orc_ctx* orc_create(const orc_cfg* cfg) {
   for (size_t k = 0; k < sizeof arrs3 / sizeof *arrs3; k++) *arrs3[k] = zalloc(n3);
   c->tcos = zalloc(nt);
   c->tsin = zalloc(nt);
+  for (int q = 0; q < 7; q++) {
+    c->skm[q] = zalloc(n3);
+    c->ske[q] = zalloc(n3);
+  }
+  c->scm = zalloc(n3);
+  c->sce = zalloc(n3);
+  c->ebuf = zalloc(n3);
   ewald_consts(c);
   return c;
 }
@@ -82,6 +91,13 @@ void orc_destroy(orc_ctx* c) {
                    c->k2m, c->k2e, c->c2m, c->c2e, c->beff, c->b2, c->b3, c->tcos, c->tsin,
                    c->pvec, c->plen};
   for (size_t k = 0; k < sizeof all / sizeof *all; k++) free(all[k]);
+  for (int q = 0; q < 7; q++) {
+    free(c->skm[q]);
+    free(c->ske[q]);
+  }
+  free(c->scm);
+  free(c->sce);
+  free(c->ebuf);
   free(c->pidx);
   free(c->psr);
   free(c);
@@ -554,6 +570,202 @@ void orc_step(orc_ctx* c, double dt, int noise_mode, const double* xi, uint64_t 
   }
   c->t += dt;
   c->step++;
+}
+
+/* ------------------------------------------------------- adaptive solvers */
+
+/* Normalises the rows of mm and ea (simulation.cpp:869-870) and moves the
+ * particles with the step-start force for deltaTused (IntegrationTrans +
+ * ApplyBoundaryCondArr, simulation.cpp:959-962, 610-620), then the records
+ * (EvalTransCoeffs, postprocessing.cpp:167-187; mz, simulation.cpp:514-515). */
+static void finish_step(orc_ctx* c, double used, double* obs) {
+  int64_t n = c->n;
+  for (int64_t i = 0; i < n; i++) {
+    double nm = sqrt(AX(c->mm, i, 0, n) * AX(c->mm, i, 0, n) + AX(c->mm, i, 1, n) * AX(c->mm, i, 1, n) +
+                     AX(c->mm, i, 2, n) * AX(c->mm, i, 2, n));
+    double ne = sqrt(AX(c->ea, i, 0, n) * AX(c->ea, i, 0, n) + AX(c->ea, i, 1, n) * AX(c->ea, i, 1, n) +
+                     AX(c->ea, i, 2, n) * AX(c->ea, i, 2, n));
+    for (int a = 0; a < 3; a++) {
+      AX(c->mm, i, a, n) /= nm;
+      AX(c->ea, i, a, n) /= ne;
+    }
+  }
+  double L = c->cfg.lBox, h = L / 2;
+  for (int a = 0; a < 3; a++)
+    for (int64_t i = 0; i < n; i++) {
+      double x = AX(c->pos, i, a, n) + used * (AX(c->force, i, a, n) / c->zetaTrans[i]);
+      x -= L * (double)(x > h);
+      x += L * (double)(x < -h);
+      AX(c->pos, i, a, n) = x;
+    }
+  double msd[3] = {0, 0, 0}, mz = 0;
+  for (int a = 0; a < 3; a++)
+    for (int64_t i = 0; i < n; i++) {
+      double x = AX(c->pos, i, a, n);
+      double tp = x + round((AX(c->truePos, i, a, n) - x) / L) * L;
+      AX(c->truePos, i, a, n) = tp;
+      double d = tp - AX(c->posRef, i, a, n);
+      msd[a] += d * d;
+    }
+  for (int64_t i = 0; i < n; i++) mz += AX(c->mm, i, 2, n);
+  if (obs) {
+    obs[0] = c->t;
+    obs[1] = mz / (double)n;
+    for (int a = 0; a < 3; a++) obs[2 + a] = msd[a] / (double)n;
+    obs[5] = c->Pxy / c->volBox;
+    obs[6] = c->Pxz / c->volBox;
+    obs[7] = c->Pyz / c->volBox;
+  }
+  c->t += used;
+  c->step++;
+}
+
+/* row-wise Euclidean norm, maximum over rows (`rowwise().norm().maxCoeff()`) */
+static double max_row_norm(const double* v, int64_t n) {
+  double m = 0;
+  for (int64_t i = 0; i < n; i++) {
+    double s = AX(v, i, 0, n) * AX(v, i, 0, n) + AX(v, i, 1, n) * AX(v, i, 1, n) + AX(v, i, 2, n) * AX(v, i, 2, n);
+    s = sqrt(s);
+    if (s > m) m = s;
+  }
+  return m;
+}
+
+/* AdjustTimeStep (simulation.cpp:912-951), including its clamp: the
+ * min(., deltaTmax) result is overwritten by max(., deltaTmin), so deltaTmax
+ * is never applied.  On a rejection the thermal field, torque and force are
+ * rescaled by sqrt(new / old). */
+static void adjust_time_step(orc_ctx* c, const orc_adapt* ad, double error, double power, double* dt, int* cond,
+                             int* noFailed) {
+  double tnew;
+  if (error > ad->absTol) {
+    if (*noFailed) {
+      *noFailed = 0;
+      double q = 0.9 * pow(ad->absTol / error, power);
+      tnew = fmax(ad->dtMin, (*dt) * fmax(0.1, q));
+    } else {
+      tnew = fmax(ad->dtMin, (*dt) * 0.5);
+    }
+    double f = sqrt(tnew / (*dt));
+    for (int64_t k = 0; k < 3 * c->n; k++) {
+      c->tField[k] *= f;
+      c->tTorque[k] *= f;
+      c->tForce[k] *= f;
+    }
+  } else {
+    if (*noFailed)
+      tnew = (*dt) * fmin(fmax(0.9 * pow(ad->absTol / error, power), 0.2), 5.0);
+    else
+      tnew = *dt;
+    *cond = 0;
+  }
+  *dt = fmin(tnew, ad->dtMax);
+  *dt = fmax(tnew, ad->dtMin);
+}
+
+/* stage coordinates y0 + dt * sum_j a_j k_j, written to (scm, sce) */
+static void stage_coords(orc_ctx* c, double dt, int ns, const double* a) {
+  int64_t n3 = 3 * c->n;
+  for (int64_t k = 0; k < n3; k++) {
+    double sm = 0, se = 0;
+    for (int j = 0; j < ns; j++) {
+      if (a[j] == 0.0) continue;
+      sm += a[j] * c->skm[j][k];
+      se += a[j] * c->ske[j][k];
+    }
+    c->sce[k] = c->ea[k] + dt * se;
+    c->scm[k] = c->mm[k] + dt * sm;
+  }
+}
+
+void orc_step_adaptive(orc_ctx* c, const orc_adapt* ad, double* deltaT, int noise_mode, const double* xi,
+                       uint64_t seed, double* obs, double* used_out, int* attempts_out) {
+  int64_t n = c->n, n3 = 3 * n;
+  double ext[3];
+  ext_field(c, c->t, ext);
+  orc_thermal(c, *deltaT, noise_mode, xi, seed, c->tTorque, c->tField, c->tForce);
+  orc_compute_interactions(c, NULL, NULL, NULL);
+  /* IntegrationRot (simulation.cpp:707-871).  The slopes of stage 1 use the
+   * demagnetising field currently held: the step-start field on the first
+   * attempt, the last stage's field after a rejection (as the reference). */
+  static const double A_he[2][1] = {{0}, {1.0}};
+  static const double A_bs[4][3] = {{0, 0, 0}, {1.0 / 2.0, 0, 0}, {0, 3.0 / 4.0, 0}, {2.0 / 9.0, 1.0 / 3.0, 4.0 / 9.0}};
+  static const double A_dp[7][6] = {
+      {0, 0, 0, 0, 0, 0},
+      {1.0 / 5.0, 0, 0, 0, 0, 0},
+      {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0, 0},
+      {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0, 0, 0, 0},
+      {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0, 0, 0},
+      {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0, 0},
+      {35.0 / 384.0, 0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0}};
+  static const double E_he[2] = {0.5, -0.5};
+  static const double E_bs[4] = {-5.0 / 72.0, 1.0 / 12.0, 1.0 / 9.0, -1.0 / 8.0};
+  static const double E_dp[7] = {71.0 / 57600.0, 0, -71.0 / 16695.0, 71.0 / 1920.0, -17253.0 / 339200.0, 22.0 / 525.0,
+                                 -1.0 / 40.0};
+  int S;
+  double power;
+  const double* E;
+  if (ad->solver == 1) {
+    S = 4;
+    power = 1.0 / 3.0;
+    E = E_bs;
+  } else if (ad->solver == 2) {
+    S = 7;
+    power = 1.0 / 5.0;
+    E = E_dp;
+  } else {
+    S = 2;
+    power = 1.0 / 2.0;
+    E = E_he;
+  }
+  int cond = 1, noFailed = 1, attempts = 0;
+  double used = *deltaT;
+  while (cond) {
+    const double dt = *deltaT;
+    attempts++;
+    rk_coeffs(c, c->mm, c->ea, ext, c->skm[0], c->ske[0]);
+    for (int s = 1; s < S; s++) {
+      const double* a = ad->solver == 1 ? A_bs[s] : (ad->solver == 2 ? A_dp[s] : A_he[s]);
+      stage_coords(c, dt, s, a);
+      orc_compute_field(c, c->scm, NULL);
+      rk_coeffs(c, c->scm, c->sce, ext, c->skm[s], c->ske[s]);
+    }
+    for (int64_t k = 0; k < n3; k++) {
+      double e = 0;
+      for (int j = 0; j < S; j++)
+        if (E[j] != 0.0) e += E[j] * c->skm[j][k];
+      c->ebuf[k] = e;
+    }
+    double err = dt * max_row_norm(c->ebuf, n);
+    used = dt;
+    adjust_time_step(c, ad, err, power, deltaT, &cond, &noFailed);
+  }
+  if (ad->solver == 1) {
+    /* the third-order solution: the last stage's coordinates */
+    memcpy(c->mm, c->scm, (size_t)n3 * sizeof(double));
+    memcpy(c->ea, c->sce, (size_t)n3 * sizeof(double));
+  } else {
+    const double* b = ad->solver == 2 ? A_dp[6] : NULL;
+    for (int64_t k = 0; k < n3; k++) {
+      double sm, se;
+      if (ad->solver == 2) {
+        sm = se = 0;
+        for (int j = 0; j < 6; j++) {
+          if (b[j] == 0.0) continue;
+          sm += b[j] * c->skm[j][k];
+          se += b[j] * c->ske[j][k];
+        }
+      } else {
+        sm = 0.5 * c->skm[0][k] + 0.5 * c->skm[1][k];
+        se = 0.5 * c->ske[0][k] + 0.5 * c->ske[1][k];
+      }
+      c->ea[k] += used * se;
+      c->mm[k] += used * sm;
+    }
+  }
+  finish_step(c, used, obs);
+  if (used_out) *used_out = used;
+  if (attempts_out) *attempts_out = attempts;
 }
 
 /* ------------------------------------------------------------ error model */

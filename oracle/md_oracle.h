@@ -67,6 +67,20 @@ enum { ORC_NOISE_OFF = 0, ORC_NOISE_UPLOADED = 1, ORC_NOISE_PHILOX = 2 };
 void orc_step(orc_ctx* c, double dt, int noise_mode, const double* xi, uint64_t seed,
               double* B1, double* F1, double* B2, double* obs);
 
+/* Adaptive time stepping (IntegrationRot + AdjustTimeStep,
+ * simulation.cpp:707-871, 912-951): solver 0 Heun-Euler 1(2), 1
+ * Bogacki-Shampine 2(3), 2 Dormand-Prince 4(5) (the SOLVER key). */
+typedef struct orc_adapt {
+  int64_t solver;
+  double absTol, dtMin, dtMax;
+} orc_adapt;
+
+/* One accepted step of the reference loop with the adaptive solver: deltaT is
+ * the trial step on entry and the next trial step on exit; *used_out the step
+ * taken, *attempts_out the attempts (1 + rejections). */
+void orc_step_adaptive(orc_ctx* c, const orc_adapt* ad, double* deltaT, int noise_mode, const double* xi,
+                       uint64_t seed, double* obs, double* used_out, int* attempts_out);
+
 /* Thermal noise scaled as DefThermFluct (simulation.cpp:563-603). */
 void orc_thermal(orc_ctx* c, double dt, int noise_mode, const double* xi, uint64_t seed,
                  double* torque, double* field, double* force);

@@ -37,6 +37,10 @@ def build(force=False) -> str:
     return LIB
 
 
+class Adapt(C.Structure):
+    _fields_ = [("solver", C.c_int64), ("absTol", C.c_double), ("dtMin", C.c_double), ("dtMax", C.c_double)]
+
+
 class Cfg(C.Structure):
     _fields_ = [("n", C.c_int64), ("lBox", C.c_double), ("alpha", C.c_double), ("rCutLR", C.c_double),
                 ("nc", C.c_int64), ("rCutSR", C.c_double)] + [
@@ -65,6 +69,8 @@ def lib():
         L.orc_compute_field.argtypes = [C.c_void_p, P, P]
         L.orc_step.argtypes = [C.c_void_p, C.c_double, C.c_int, P, C.c_uint64, P, P, P, P]
         L.orc_thermal.argtypes = [C.c_void_p, C.c_double, C.c_int, P, C.c_uint64, P, P, P]
+        L.orc_step_adaptive.argtypes = [C.c_void_p, C.POINTER(Adapt), P, C.c_int, P, C.c_uint64, P, P,
+                                        C.POINTER(C.c_int)]
         L.orc_philox_normals.argtypes = [C.c_uint64, C.c_uint64, C.c_int64, P]
         L.orc_fun_real_error.restype = C.c_double
         L.orc_fun_real_error.argtypes = [C.c_double] * 8
@@ -262,6 +268,20 @@ class Oracle:
                         _p(obs))
         o["obs"] = obs
         return o
+
+    def step_adaptive(self, solver, dt, absTol, dtMin, dtMax, noise_mode=0, xi=None, seed=0):
+        """One accepted step with the reference's adaptive solver and time-step
+        control; returns (next trial dt, dt used, attempts, obs)."""
+        ad = Adapt(int(solver), float(absTol), float(dtMin), float(dtMax))
+        dtv, used, att = C.c_double(dt), C.c_double(), C.c_int()
+        obs = np.zeros(8)
+        xi_p = None
+        if xi is not None:
+            xi = np.ascontiguousarray(xi, dtype=np.float64)
+            xi_p = _p(xi)
+        self.L.orc_step_adaptive(self.h, C.byref(ad), C.byref(dtv), noise_mode, xi_p, seed, _p(obs), C.byref(used),
+                                 C.byref(att))
+        return dtv.value, used.value, att.value, obs
 
     def last_seconds(self):
         return self.L.orc_last_seconds(self.h)

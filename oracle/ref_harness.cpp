@@ -55,7 +55,7 @@ namespace {
 
 struct In {
   int64_t n = 0, nsteps = 0, dump_level = 1, ewald_search = 0;
-  int64_t has_radii = 0, has_pos = 0, has_orient = 0;
+  int64_t has_radii = 0, has_pos = 0, has_orient = 0, adaptive = 0;
   double dt = 1e-12, alpha = 0, rc = 0, kc = 0, vis = 0;
   std::vector<double> rmag, pos, mm, ea;
 };
@@ -80,7 +80,9 @@ int main(int argc, char** argv) {
   int64_t hdr[8];
   double dh[5];
   if (!rd(fi, hdr, sizeof hdr) || !rd(fi, dh, sizeof dh)) { fprintf(stderr, "short header\n"); return 2; }
-  if (hdr[0] != 0x4d44524546ll) { fprintf(stderr, "bad magic\n"); return 2; }
+  // magic "MDREF": fixed step; "MDREG": one more header word, the adaptive flag
+  if (hdr[0] != 0x4d44524546ll && hdr[0] != 0x4d44524547ll) { fprintf(stderr, "bad magic\n"); return 2; }
+  if (hdr[0] == 0x4d44524547ll && !rd(fi, &in.adaptive, sizeof in.adaptive)) { fprintf(stderr, "short header\n"); return 2; }
   in.n = hdr[1]; in.nsteps = hdr[2]; in.dump_level = hdr[3]; in.ewald_search = hdr[4];
   in.has_radii = hdr[5]; in.has_pos = hdr[6]; in.has_orient = hdr[7];
   in.dt = dh[0]; in.alpha = dh[1]; in.rc = dh[2]; in.kc = dh[3]; in.vis = dh[4];
@@ -97,7 +99,9 @@ int main(int argc, char** argv) {
   // Extensions the reference cannot express (values only; formulas unchanged).
   config->numbPart_ = (int)n;
   if (in.vis > 0) config->vis_ = in.vis;
-  config->absTol_ = 1e300;
+  // fixed step: every step accepted; adaptive: the INI's absTol and the
+  // reference's own step control, with in.dt as the first trial step
+  if (!in.adaptive) config->absTol_ = 1e300;
 
   WorkingVar_S* pW = &workVar;
   // particle properties: the reference's own routine, or injected radii
@@ -176,7 +180,8 @@ int main(int argc, char** argv) {
   timespec t0, t1;
   double elapsed = 0;
   for (int64_t s = 0; s < in.nsteps; s++) {
-    deltaT = in.dt;
+    if (!in.adaptive) deltaT = in.dt;
+    if (in.adaptive) put1(fo, deltaT);  // the trial step DefThermFluct scales the noise with
     clock_gettime(CLOCK_MONOTONIC, &t0);
     DefExtField(&pW->extFluxDens, tInt);
     DefThermFluct(pW, &buffer.buffer1d, deltaT);
@@ -217,6 +222,7 @@ int main(int argc, char** argv) {
                        outputVar.PxyVec.back(), outputVar.PxzVec.back(), outputVar.PyzVec.back()};
       put(fo, obs, 8);
     }
+    if (in.adaptive) put1(fo, deltaTused);
     tInt += deltaTused;
   }
   putArr(fo, pW->coordsTrans.pos);

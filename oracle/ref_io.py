@@ -82,7 +82,7 @@ def available() -> bool:
 
 
 def run_ref(ini, n, nsteps, dt, alpha=0.0, rc=0.0, kc=0.0, vis=0.0, rmag=None, pos=None,
-            mm=None, ea=None, dump_level=1, ewald_search=False, timeout=3600, txt_dir=None):
+            mm=None, ea=None, dump_level=1, ewald_search=False, timeout=3600, txt_dir=None, adaptive=False):
     """Runs the reference harness and returns a dict of arrays.
 
     Per-step arrays (dump_level >= 1) are stacked along axis 0 and reshaped to
@@ -98,9 +98,12 @@ def run_ref(ini, n, nsteps, dt, alpha=0.0, rc=0.0, kc=0.0, vis=0.0, rmag=None, p
         write_ini(os.path.join(td, "configuration.ini"), ini)
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
-            f.write(struct.pack("<8q", 0x4D44524546, n, nsteps, dump_level, int(ewald_search),
+            magic = 0x4D44524547 if adaptive else 0x4D44524546
+            f.write(struct.pack("<8q", magic, n, nsteps, dump_level, int(ewald_search),
                                 rmag is not None, pos is not None, mm is not None))
             f.write(struct.pack("<5d", dt, alpha, rc, kc, vis))
+            if adaptive:
+                f.write(struct.pack("<q", 1))
             for a in (rmag, pos, mm, ea):
                 if a is not None:
                     f.write(np.ascontiguousarray(a, dtype=np.float64).tobytes())
@@ -110,10 +113,10 @@ def run_ref(ini, n, nsteps, dt, alpha=0.0, rc=0.0, kc=0.0, vis=0.0, rmag=None, p
         if r.returncode != 0:
             raise RuntimeError(f"ref_harness failed ({r.returncode}): {r.stderr[-2000:]}")
         raw = np.fromfile(fout, dtype=np.float64)
-    return parse_out(raw, n, nsteps, dump_level)
+    return parse_out(raw, n, nsteps, dump_level, adaptive)
 
 
-def parse_out(raw, n, nsteps, dump_level):
+def parse_out(raw, n, nsteps, dump_level, adaptive=False):
     o = {}
     p = 0
 
@@ -127,8 +130,10 @@ def parse_out(raw, n, nsteps, dump_level):
     o["rMag"], o["rHydr"] = take(n).copy(), take(n).copy()
     o["pos0"], o["mm0"], o["ea0"] = (take(3 * n).reshape(3, n).copy() for _ in range(3))
     names = ["B1", "F1", "thermTorque", "thermField", "thermForce", "posCorr"]
-    steps = {k: [] for k in names + ["pairs", "B2", "pos", "mm", "ea", "obs"]}
+    steps = {k: [] for k in names + ["pairs", "B2", "pos", "mm", "ea", "obs", "dt0", "dtUsed"]}
     for _ in range(nsteps):
+        if adaptive:
+            steps["dt0"].append(take(1)[0])
         if dump_level >= 1:
             for k in names:
                 steps[k].append(take(3 * n).reshape(3, n).copy())
@@ -138,6 +143,8 @@ def parse_out(raw, n, nsteps, dump_level):
                 steps[k].append(take(3 * n).reshape(3, n).copy())
         if dump_level >= 0:
             steps["obs"].append(take(8).copy())
+        if adaptive:
+            steps["dtUsed"].append(take(1)[0])
     for k, v in steps.items():
         if v:
             o[k] = np.array(v)

@@ -28,12 +28,15 @@ VIS = 1e-3  # water, the BASELINE viscosity (the reference's Vogel formula gives
 
 
 def case(name, n, nsteps, rc_frac, seed, noise=True, coating=False, lognormal=False, overlap=False, dt=1e-12,
-         B0=0.01, rot=3, txt=False):
+         B0=0.01, rot=3, txt=False, solver=None, absTol=1e-4):
+    """solver None: fixed step (Heun, every step accepted); 0, 1, 2: the
+    reference's adaptive step control with that SOLVER, starting from dt."""
+    extra = {} if solver is None else dict(SOLVER=solver, absTol=absTol, deltaTinit=dt)
     ini = ref_io.ini_dict(npDim=round(n ** (1 / 3)) if round(n ** (1 / 3)) ** 3 == n else 4,
                           ENABLE_THERM_FIELD="true" if noise else "false",
                           ENABLE_THERM_TORQUE="true" if noise else "false",
                           ENABLE_THERM_FORCE="true" if noise else "false",
-                          ENABLE_COATING_POT="true" if coating else "false", magFluxDens=B0, seed=seed)
+                          ENABLE_COATING_POT="true" if coating else "false", magFluxDens=B0, seed=seed, **extra)
     d = O.derive(ini)
     rng = np.random.default_rng(seed)
     if lognormal:
@@ -57,7 +60,7 @@ def case(name, n, nsteps, rc_frac, seed, noise=True, coating=False, lognormal=Fa
         os.makedirs(txt_dir, exist_ok=True)
     ref = ref_io.run_ref(ini, n, nsteps, dt, alpha=alpha, rc=rc_frac * L, kc=kc, vis=VIS,
                          rmag=rMag if (lognormal or coating) else None, pos=pos.ravel(), mm=mm.ravel(),
-                         ea=ea.ravel(), txt_dir=txt_dir)
+                         ea=ea.ravel(), txt_dir=txt_dir, adaptive=solver is not None)
     assert abs(ref["lBox"] - L) <= 1e-15 * L, (ref["lBox"], L)
     out = dict(n=n, nsteps=nsteps, dt=dt, alpha=alpha, rc=rc_frac * L, kc=kc, vis=VIS, lBox=L, rMag=rMag,
                rHydr=ref["rHydr"], pos=pos, mm=mm, ea=ea, rCutSR=ref["rCutSR"])
@@ -65,6 +68,9 @@ def case(name, n, nsteps, rc_frac, seed, noise=True, coating=False, lognormal=Fa
               "pairs"):
         out["ref_" + k] = ref[k]
     out["ref_posF"], out["ref_mmF"], out["ref_eaF"] = ref["posF"], ref["mmF"], ref["eaF"]
+    if solver is not None:
+        out["solver"], out["absTol"] = solver, absTol
+        out["ref_dt0"], out["ref_dtUsed"] = ref["dt0"], ref["dtUsed"]
     np.savez_compressed(os.path.join(OUT, name + ".npz"), ini=json.dumps(ini), **out)
     print(name, "n", n, "L", L, "alpha*L", alpha * L, "kc", kc, "pairs", ref["pairs"])
 
@@ -96,6 +102,11 @@ if __name__ == "__main__":
         "n64_lognormal": lambda: case("n64_lognormal", 64, 2, 0.4, seed=14, noise=True, lognormal=True),
         "n64_overlap": lambda: case("n64_overlap", 64, 1, 0.45, seed=15, noise=False, overlap=True),
         "n64_outputs": lambda: case("n64_outputs", 64, 6, 0.4, seed=16, noise=True, lognormal=True, txt=True),
+        # adaptive step control (SOLVER 0, 1, 2), with rejections
+        "n64_adapt_he": lambda: case("n64_adapt_he", 64, 12, 0.45, seed=21, rot=4, B0=0.02, solver=0),
+        "n64_adapt_bs": lambda: case("n64_adapt_bs", 64, 12, 0.45, seed=22, rot=4, B0=0.02, solver=1),
+        "n64_adapt_dp": lambda: case("n64_adapt_dp", 64, 12, 0.45, seed=23, rot=4, B0=0.02, solver=2, dt=2e-12,
+                                     absTol=3e-5),
     }
     for name in (sys.argv[1:] or CASES):
         CASES[name]()

@@ -70,3 +70,38 @@ def test_philox_known_answer():
     assert abs(xs.mean()) < 0.01
     assert abs(xs.std() - 1) < 0.01
     del L, C
+
+
+ADAPTIVE_CASES = ["n64_adapt_he", "n64_adapt_bs", "n64_adapt_dp"]
+
+
+def xi_adaptive(ini, g, step):
+    """Unit normals of step `step` from the reference's thermal arrays, which
+    DefThermFluct scaled with that step's trial dt (simulation.cpp:563-603)."""
+    d = O.derive(ini)
+    sT, sB, sF = O.noise_scales(d, g["rMag"], g["rHydr"], float(g["ref_dt0"][step]), g["vis"])
+    return np.stack([g["ref_thermTorque"][step] / sT, g["ref_thermField"][step] / sB,
+                     g["ref_thermForce"][step] / sF])
+
+
+@pytest.mark.parametrize("name", ADAPTIVE_CASES)
+def test_oracle_matches_reference_adaptive(name):
+    """Heun-Euler, Bogacki-Shampine and Dormand-Prince with the reference's
+    step control (rejections included): the same trial and used steps, the
+    same states."""
+    ini, g = load_golden(name)
+    d = O.derive(ini)
+    orc = oracle_system(ini, g, overlap_mode=0)
+    dt = float(g["ref_dt0"][0])
+    for s in range(g["nsteps"]):
+        assert abs(dt - g["ref_dt0"][s]) <= 1e-9 * dt  # error estimates are differences of slopes
+        dt, used, att, obs = orc.step_adaptive(int(g["solver"]), dt, d["absTol"], d["deltaTmin"], d["deltaTmax"], 1,
+                                               xi_adaptive(ini, g, s))
+        assert abs(used - g["ref_dtUsed"][s]) <= 1e-9 * used
+        pos, mm, ea, t = orc.get_state()
+        assert np.max(np.abs(pos - g["ref_pos"][s])) <= 1e-12 * g["lBox"]
+        assert np.max(np.abs(mm - g["ref_mm"][s])) < 1e-11
+        assert np.max(np.abs(ea - g["ref_ea"][s])) < 1e-11
+        np.testing.assert_allclose(obs[:2], g["ref_obs"][s][:2], rtol=1e-11, atol=1e-15)
+    # the cases exercise rejections
+    assert np.any(g["ref_dtUsed"] != g["ref_dt0"])
