@@ -203,6 +203,24 @@ int md_set_noise(md_ctx* ctx, int mode, uint64_t seed);
  * [torque N x 3][field N x 3][force N x 3] column-major (the order of the
  * three Rand::normal draws of DefThermFluct); NULL otherwise. */
 int md_step(md_ctx* ctx, int64_t nsteps, double dt, const double* xi);
+/* RunSimulation's loop with the adaptive solvers of IntegrationRot
+ * (src/simulation.cpp:707-871; the configuration's SOLVER: 0 Heun-Euler 1(2),
+ * 1 Bogacki-Shampine 2(3), 2 Dormand-Prince 4(5)) and the step control
+ * AdjustTimeStep (src/simulation.cpp:912-951; absTol, deltaTmin, deltaTmax
+ * of the configuration), stage fields by CompDemagField.  Runs accepted
+ * steps while the time is <= t_end (the loop condition of RunSimulation),
+ * at most max_steps of them.  *dt: the trial step on entry (deltaTinit for
+ * the first step), the next trial step on exit.  The reference's behaviour is
+ * kept: deltaTmax is never applied (its clamp is overwritten), a retried
+ * attempt's first slope uses the field of the rejected attempt's last stage,
+ * and a rejection rescales the thermal field and torque by sqrt(new/old) but
+ * not the thermal force already in the interaction force.  A step rejected at
+ * deltaTmin, where the reference retries forever, returns MD_ERR_INVALID.
+ * xi: MD_NOISE_UPLOADED only, max_steps blocks of 9N unit normals as for
+ * md_step (scaled with each step's trial dt, like DefThermFluct).
+ * *steps_done: accepted steps; md_records holds one record per step. */
+int md_step_adaptive(md_ctx* ctx, int64_t max_steps, double t_end, double* dt, const double* xi,
+                     int64_t* steps_done);
 /* Per-step records {t, mz, MSDx, MSDy, MSDz, Pxy, Pxz, Pyz} (the vectors of
  * OutputVar_S, src/typedefs.h:129-137, filled by EvalTransCoeffs and
  * simulation.cpp:514-515) for steps [first, first + count) since the last

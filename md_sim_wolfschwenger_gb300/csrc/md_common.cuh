@@ -179,6 +179,21 @@ struct IntParams {
   StepFlags* flags;          // maxdisp is raised here
 };
 
+// One stage (or the accept step) of an adaptive Runge-Kutta attempt.
+struct RKStage {
+  IntParams p;              // p.Br / p.Bk: the field last evaluated; p.dt: the attempt's step
+  void* km[7];              // stage slopes of m, [3][n] T, original order
+  void* ke[7];              // stage slopes of n
+  void* cm;                 // stage coordinates (m), [3][n] T
+  void* ce;                 // stage coordinates (n)
+  double a[7];              // weights of k_0..k_s: next stage (stage kernel) / solution (accept)
+  double e[7];              // error weights (last stage)
+  int s;                    // stage index (0-based); accept: last weight index
+  int last;                 // stage: no next stage, form the error; accept: take (cm, ce)
+  double nf;                // factor on the thermal field and torque (rescaled on rejections)
+  unsigned long long* errmax;  // max over particles of the error norm (double bits)
+};
+
 struct ObsParams {
   int nblk_int;
   const double* obs_part;

@@ -943,6 +943,149 @@ int md_step(md_ctx* c, int64_t nsteps, double dt, const double* xi) {
   return read_err_word(c);
 }
 
+// Butcher rows of the reference's solvers (src/simulation.cpp:721-867):
+// weights of k_0..k_s for stage s + 1, error weights, solution weights.
+namespace {
+struct Tableau {
+  int stages;
+  double power;
+  double a[7][7];
+  double e[7];
+  double b[7];
+  int nb;         // solution weights b[0..nb)
+  bool last_is_solution;  // Bogacki-Shampine: the solution is the last stage's coordinates
+};
+
+const Tableau& tableau(int solver) {
+  static const Tableau he = {2, 1.0 / 2.0, {{1.0}}, {0.5, -0.5}, {0.5, 0.5}, 2, false};
+  static const Tableau bs = {4,
+                             1.0 / 3.0,
+                             {{1.0 / 2.0}, {0, 3.0 / 4.0}, {2.0 / 9.0, 1.0 / 3.0, 4.0 / 9.0}},
+                             {-5.0 / 72.0, 1.0 / 12.0, 1.0 / 9.0, -1.0 / 8.0},
+                             {},
+                             0,
+                             true};
+  static const Tableau dp = {7,
+                             1.0 / 5.0,
+                             {{1.0 / 5.0},
+                              {3.0 / 40.0, 9.0 / 40.0},
+                              {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0},
+                              {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0},
+                              {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0},
+                              {35.0 / 384.0, 0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0}},
+                             {71.0 / 57600.0, 0, -71.0 / 16695.0, 71.0 / 1920.0, -17253.0 / 339200.0, 22.0 / 525.0,
+                              -1.0 / 40.0},
+                             {35.0 / 384.0, 0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0},
+                             6,
+                             false};
+  return solver == 1 ? bs : (solver == 2 ? dp : he);
+}
+}  // namespace
+
+int md_step_adaptive(md_ctx* c, int64_t max_steps, double t_end, double* dt_io, const double* xi,
+                     int64_t* steps_done) {
+  int st = check_ready(c, true);
+  if (st) return st;
+  if (steps_done) *steps_done = 0;
+  if (max_steps < 0 || !dt_io || !(*dt_io > 0)) return set_err(c, MD_ERR_INVALID, "bad max_steps or dt");
+  if (c->noise == MD_NOISE_UPLOADED && !xi && max_steps > 0)
+    return set_err(c, MD_ERR_INVALID, "uploaded noise needs xi");
+  const int solver = (int)c->cfg.SOLVER;
+  if (solver < 0 || solver > 2) return set_err(c, MD_ERR_INVALID, "SOLVER must be 0, 1 or 2");
+  const Tableau& tb = tableau(solver);
+  const double absTol = c->cfg.absTol, dtMin = c->cfg.deltaTmin, dtMax = c->cfg.deltaTmax;
+  const size_t n3t = 3 * (size_t)c->n * tsz(c);
+  for (int q = 0; q < tb.stages; q++) {
+    if (!c->rk_km[q] && (st = dalloc(c, &c->rk_km[q], n3t))) return st;
+    if (!c->rk_ke[q] && (st = dalloc(c, &c->rk_ke[q], n3t))) return st;
+  }
+  if (!c->rk_cm && (st = dalloc(c, &c->rk_cm, n3t))) return st;
+  if (!c->rk_ce && (st = dalloc(c, &c->rk_ce, n3t))) return st;
+  if ((st = ensure_records(c, max_steps))) return st;
+  double t = 0;
+  int64_t stepno = 0;
+  if ((st = md_get_time(c, &t, &stepno))) return st;
+  RKStage q{};
+  for (int j = 0; j < 7; j++) {
+    q.km[j] = c->rk_km[j];
+    q.ke[j] = c->rk_ke[j];
+  }
+  q.cm = c->rk_cm;
+  q.ce = c->rk_ce;
+  q.errmax = &c->sc->errmax;
+  int64_t done = 0;
+  c->launches = 0;
+  while (done < max_steps && t <= t_end) {
+    const double dt0 = *dt_io;
+    if ((st = prepare_dt(c, dt0))) return st;
+    if (c->noise == MD_NOISE_UPLOADED)
+      CK(c, cudaMemcpyAsync(c->xi, xi + (size_t)done * 9 * c->n, 72 * (size_t)c->n, cudaMemcpyHostToDevice,
+                            c->stream));
+    c->launches += issue_interactions(c);
+    bool cond = true, noFailed = true, first = true;
+    double nf = 1.0, used = dt0;
+    while (cond) {
+      const double dt = *dt_io;
+      q.nf = nf;
+      for (int s = 0; s < tb.stages; s++) {
+        const bool start_field = s == 0 && first;  // later: the field last evaluated
+        q.p = int_params(c, dt, start_field ? c->Br : c->Br2, start_field ? c->Bk : c->Bk2);
+        q.s = s;
+        q.last = s == tb.stages - 1;
+        for (int j = 0; j < 7; j++) {
+          q.a[j] = q.last ? 0.0 : tb.a[s][j];
+          q.e[j] = tb.e[j];
+        }
+        if (q.last) CK(c, cudaMemsetAsync(&c->sc->errmax, 0, sizeof(unsigned long long), c->stream));
+        c->launches += launch_rk_stage(c->stream, q, fp64(c));
+        if (!q.last) c->launches += issue_field(c);
+      }
+      unsigned long long bits = 0;
+      CK(c, cudaMemcpyAsync(&bits, &c->sc->errmax, sizeof bits, cudaMemcpyDeviceToHost, c->stream));
+      CK(c, cudaStreamSynchronize(c->stream));
+      double emax;
+      std::memcpy(&emax, &bits, sizeof emax);
+      const double error = dt * emax;
+      used = dt;
+      // AdjustTimeStep (src/simulation.cpp:912-951), including its clamp:
+      // min(., deltaTmax) is overwritten by max(., deltaTmin)
+      double tnew;
+      if (error > absTol) {
+        if (noFailed) {
+          noFailed = false;
+          tnew = std::max(dtMin, dt * std::max(0.1, 0.9 * std::pow(absTol / error, tb.power)));
+        } else {
+          tnew = std::max(dtMin, dt * 0.5);
+        }
+        nf *= std::sqrt(tnew / dt);
+        if (tnew == dt) {
+          // the reference would retry the same step forever (deltaTmin reached)
+          return set_err(c, MD_ERR_INVALID, "step rejected at deltaTmin = %g s (error %g > absTol %g)", dt, error,
+                         absTol);
+        }
+      } else {
+        tnew = noFailed ? dt * std::min(std::max(0.9 * std::pow(absTol / error, tb.power), 0.2), 5.0) : dt;
+        cond = false;
+      }
+      *dt_io = std::min(tnew, dtMax);
+      *dt_io = std::max(tnew, dtMin);
+      first = false;
+    }
+    q.p = int_params(c, used, c->Br, c->Bk);
+    q.s = tb.nb - 1;
+    q.last = tb.last_is_solution ? 1 : 0;
+    for (int j = 0; j < 7; j++) q.a[j] = tb.b[j];
+    c->launches += launch_rk_accept(c->stream, q, fp64(c));
+    c->launches += launch_obs(c->stream, obs_params(c, used));
+    t += used;
+    done++;
+  }
+  CK(c, cudaGetLastError());
+  c->have_geometry = true;
+  if (steps_done) *steps_done = done;
+  return read_err_word(c);
+}
+
 int md_num_records(const md_ctx* cc, int64_t* count) {
   md_ctx* c = const_cast<md_ctx*>(cc);
   if (!c || !count) return MD_ERR_INVALID;

@@ -25,6 +25,7 @@ struct DevScalars {
   double musum[3];
   unsigned long long pairs;
   StepFlags flags;
+  unsigned long long errmax;  // adaptive solvers: error norm of the attempt (double bits)
 };
 
 }  // namespace md
@@ -79,6 +80,8 @@ struct md_ctx {
   // stage outputs (T)
   void *Br = nullptr, *Fr = nullptr, *ov = nullptr, *Bk = nullptr, *Fk = nullptr, *Br2 = nullptr, *Bk2 = nullptr;
   void *k1m = nullptr, *k1e = nullptr, *m2 = nullptr, *e2 = nullptr, *th = nullptr;
+  // adaptive solvers (allocated on first use): stage slopes and coordinates
+  void *rk_km[7] = {}, *rk_ke[7] = {}, *rk_cm = nullptr, *rk_ce = nullptr;
   double *Ppart = nullptr, *obs_part = nullptr;
   DevScalars* sc = nullptr;
   double* records = nullptr;

@@ -147,75 +147,55 @@ __device__ __forceinline__ void heun1(const IntParams& p, int bx) {
   ((T4*)p.s.mu)[r] = v;
 }
 
+// End of a step for particle i (sorted slot r): renormalised m and n
+// (simulation.cpp:869-870) from the solver's mn, en; translation with the
+// step-start force plus thermal force fth and the overlap push, the single
+// wrap (IntegrationTrans + ApplyBoundaryCondArr); unwrapped MSD, m_z and the
+// pressure partials into acc; squared displacement since the last list build.
 template <typename T>
-__device__ __forceinline__ void heun2(const IntParams& p, int bx) {
-  const int i = bx * kIntThreads + threadIdx.x;
+__device__ __forceinline__ void finish_particle(const IntParams& p, int i, int r, const T mn[3], const T en[3],
+                                                const T fth[3], double acc[7], double& disp2) {
   const int n = p.n;
-  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  double disp2 = 0;  // squared displacement since the last neighbour-list build
-  if (i < n) {
-    // pressure partials of the real-space pass (any order sums the same pairs)
-    acc[4] = p.Ppart[3 * i];
-    acc[5] = p.Ppart[3 * i + 1];
-    acc[6] = p.Ppart[3 * i + 2];
-    const int r = p.s.rank[i];
-    const T* th = (const T*)p.th;
-    T m[3], e[3], m2[3], e2[3], bd[3], tau[3], bth[3], k1m[3], k1e[3];
+  acc[4] = p.Ppart[3 * i];
+  acc[5] = p.Ppart[3 * i + 1];
+  acc[6] = p.Ppart[3 * i + 2];
+  const T nm = sqrt(mn[0] * mn[0] + mn[1] * mn[1] + mn[2] * mn[2]);
+  const T ne = sqrt(en[0] * en[0] + en[1] * en[1] + en[2] * en[2]);
+  const T* Fr = (const T*)p.Fr;
+  const T* Fk = (const T*)p.Fk;
+  const T* ov = (const T*)p.ov;
+  const double L = p.L, half = 0.5 * L, dtd = p.dt;
+  const T izt = (T)p.invZt[i];
+  bool bad = false;
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-      m[a] = (T)p.mm[a * n + i];
-      e[a] = (T)p.ea[a * n + i];
-      m2[a] = ((const T*)p.m2)[a * n + i];
-      e2[a] = ((const T*)p.e2)[a * n + i];
-      k1m[a] = ((const T*)p.k1m)[a * n + i];
-      k1e[a] = ((const T*)p.k1e)[a * n + i];
-      tau[a] = th[a * n + i];
-      bth[a] = th[(3 + a) * n + i];
+  for (int a = 0; a < 3; a++) {
+    const T mf = mn[a] / nm, ef = en[a] / ne;
+    p.mm[a * n + i] = (double)mf;
+    p.ea[a * n + i] = (double)ef;
+    const T f = (T)(((double)Fr[a * n + r] + (double)Fk[a * n + r]) * p.F_unit) + fth[a];
+    double x = p.pos[a * n + i] + (double)ov[a * n + r] * L + dtd * (double)(f * izt);
+    x -= L * (double)(x > half);
+    x += L * (double)(x < -half);
+    p.pos[a * n + i] = x;
+    if (p.xbuild) {
+      double db = x - p.xbuild[a * n + i];
+      db -= L * round(db / L);
+      disp2 += db * db;
     }
-    demag_si<T>(p, r, bd);
-    const T bz = (T)ext_field_z(p, *p.time);
-    T km[3], ke[3];
-    rk<T>(p, m2, e2, bd, bz, bth, tau, (T)p.velEa1[i], (T)p.velEa2[i], km, ke);
-    const T dt = (T)p.dt, h = (T)0.5;
-    T mn[3], en[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-      en[a] = e[a] + dt * (h * k1e[a] + h * ke[a]);
-      mn[a] = m[a] + dt * (h * k1m[a] + h * km[a]);
-    }
-    const T nm = sqrt(mn[0] * mn[0] + mn[1] * mn[1] + mn[2] * mn[2]);
-    const T ne = sqrt(en[0] * en[0] + en[1] * en[1] + en[2] * en[2]);
-    const T* Fr = (const T*)p.Fr;
-    const T* Fk = (const T*)p.Fk;
-    const T* ov = (const T*)p.ov;
-    const double L = p.L, half = 0.5 * L, dtd = p.dt;
-    const T izt = (T)p.invZt[i];
-    bool bad = false;
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-      const T mf = mn[a] / nm, ef = en[a] / ne;
-      p.mm[a * n + i] = (double)mf;
-      p.ea[a * n + i] = (double)ef;
-      const T f = (T)(((double)Fr[a * n + r] + (double)Fk[a * n + r]) * p.F_unit) + th[(6 + a) * n + i];
-      double x = p.pos[a * n + i] + (double)ov[a * n + r] * L + dtd * (double)(f * izt);
-      x -= L * (double)(x > half);
-      x += L * (double)(x < -half);
-      p.pos[a * n + i] = x;
-      if (p.xbuild) {
-        double db = x - p.xbuild[a * n + i];
-        db -= L * round(db / L);
-        disp2 += db * db;
-      }
-      double tp = p.truePos[a * n + i];
-      tp = x + round((tp - x) / L) * L;
-      p.truePos[a * n + i] = tp;
-      const double d = tp - p.posRef[a * n + i];
-      acc[a] = d * d;
-      bad |= !isfinite(x) || !isfinite((double)mf) || !isfinite((double)ef);
-    }
-    acc[3] = p.mm[2 * n + i];
-    if (bad) atomicOr(p.err, kErrNonFinite);
+    double tp = p.truePos[a * n + i];
+    tp = x + round((tp - x) / L) * L;
+    p.truePos[a * n + i] = tp;
+    const double d = tp - p.posRef[a * n + i];
+    acc[a] = d * d;
+    bad |= !isfinite(x) || !isfinite((double)mf) || !isfinite((double)ef);
   }
+  acc[3] = p.mm[2 * n + i];
+  if (bad) atomicOr(p.err, kErrNonFinite);
+}
+
+// Block sums of the step records and the largest displacement since the
+// last list build (every thread of the block calls this).
+__device__ __forceinline__ void step_block_sums(const IntParams& p, int bx, const double acc[7], double disp2) {
   if (p.flags) {
     float d = (float)(sqrt(disp2) / p.L);
 #pragma unroll
@@ -234,6 +214,44 @@ __device__ __forceinline__ void heun2(const IntParams& p, int bx) {
     for (int w = 0; w < kIntThreads / 32; w++) s += red[threadIdx.x][w];
     p.obs_part[7 * bx + threadIdx.x] = s;
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void heun2(const IntParams& p, int bx) {
+  const int i = bx * kIntThreads + threadIdx.x;
+  const int n = p.n;
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  double disp2 = 0;  // squared displacement since the last neighbour-list build
+  if (i < n) {
+    const int r = p.s.rank[i];
+    const T* th = (const T*)p.th;
+    T m[3], e[3], m2[3], e2[3], bd[3], tau[3], bth[3], k1m[3], k1e[3], fth[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      m[a] = (T)p.mm[a * n + i];
+      e[a] = (T)p.ea[a * n + i];
+      m2[a] = ((const T*)p.m2)[a * n + i];
+      e2[a] = ((const T*)p.e2)[a * n + i];
+      k1m[a] = ((const T*)p.k1m)[a * n + i];
+      k1e[a] = ((const T*)p.k1e)[a * n + i];
+      tau[a] = th[a * n + i];
+      bth[a] = th[(3 + a) * n + i];
+      fth[a] = th[(6 + a) * n + i];
+    }
+    demag_si<T>(p, r, bd);
+    const T bz = (T)ext_field_z(p, *p.time);
+    T km[3], ke[3];
+    rk<T>(p, m2, e2, bd, bz, bth, tau, (T)p.velEa1[i], (T)p.velEa2[i], km, ke);
+    const T dt = (T)p.dt, h = (T)0.5;
+    T mn[3], en[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      en[a] = e[a] + dt * (h * k1e[a] + h * ke[a]);
+      mn[a] = m[a] + dt * (h * k1m[a] + h * km[a]);
+    }
+    finish_particle<T>(p, i, r, mn, en, fth, acc, disp2);
+  }
+  step_block_sums(p, bx, acc, disp2);
 }
 
 __device__ __forceinline__ void obs(const ObsParams& p) {
@@ -337,6 +355,164 @@ int launch_real_part(cudaStream_t st, const IntParams& p, double* Bout, double* 
     k_real_part<double><<<(p.n + 255) / 256, 256, 0, st>>>(p, Bout, Fout);
   else
     k_real_part<float><<<(p.n + 255) / 256, 256, 0, st>>>(p, Bout, Fout);
+  return 1;
+}
+
+// ------------------------------------------------ adaptive Runge-Kutta
+// IntegrationRot with SOLVER = 0, 1, 2 and the reference's step control
+// (src/simulation.cpp:707-871): one kernel per stage s evaluates the slopes
+// k_s at the stage coordinates with the field last evaluated there, and
+// forms the next stage's coordinates (written into the sorted view for the
+// next field evaluation) or, at the last stage, the error norm
+// max_i |sum_j e_j km_j,i|.  The host runs the step control
+// (AdjustTimeStep) and launches the accept kernel with the step used.
+
+template <typename T>
+__device__ __forceinline__ void noise9(const IntParams& p, int i, T z[9]) {
+  const int n = p.n;
+  if (p.noise == 2) {
+    philox_normals9<T>(p.seed, (uint64_t)*p.stepno, (uint32_t)i, z);
+  } else if (p.noise == 1) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) z[q] = (T)p.xi[(q / 3) * 3 * n + (q % 3) * n + i];
+  } else {
+#pragma unroll
+    for (int q = 0; q < 9; q++) z[q] = 0;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kIntThreads) k_rk_stage(RKStage q) {
+  using T4 = typename V4<T>::t;
+  const IntParams& p = q.p;
+  const int i = blockIdx.x * kIntThreads + threadIdx.x;
+  const int n = p.n;
+  double err = 0.0;
+  if (i < n) {
+    const int r = p.s.rank[i];
+    T m[3], e[3], bd[3], z[9], tau[3], bth[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      m[a] = q.s == 0 ? (T)p.mm[a * n + i] : ((const T*)q.cm)[a * n + i];
+      e[a] = q.s == 0 ? (T)p.ea[a * n + i] : ((const T*)q.ce)[a * n + i];
+    }
+    demag_si<T>(p, r, bd);
+    noise9<T>(p, i, z);
+    const T sT = (T)(p.sT[i] * q.nf), sB = (T)(p.sB[i] * q.nf);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      tau[a] = sT * z[a];
+      bth[a] = sB * z[3 + a];
+    }
+    const T bz = (T)ext_field_z(p, *p.time);
+    T km[3], ke[3];
+    rk<T>(p, m, e, bd, bz, bth, tau, (T)p.velEa1[i], (T)p.velEa2[i], km, ke);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      ((T*)q.km[q.s])[a * n + i] = km[a];
+      ((T*)q.ke[q.s])[a * n + i] = ke[a];
+    }
+    if (!q.last) {
+      // next stage: y0 + dt sum_{j <= s} a_j k_j, formed in FP64 (the
+      // Dormand-Prince weights reach ~12 and cancel)
+      T nm[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        double sm = 0, se = 0;
+        for (int j = 0; j <= q.s; j++) {
+          if (q.a[j] == 0.0) continue;
+          const double kmj = j == q.s ? (double)km[a] : (double)((const T*)q.km[j])[a * n + i];
+          const double kej = j == q.s ? (double)ke[a] : (double)((const T*)q.ke[j])[a * n + i];
+          sm += q.a[j] * kmj;
+          se += q.a[j] * kej;
+        }
+        ((T*)q.ce)[a * n + i] = (T)(p.ea[a * n + i] + p.dt * se);
+        nm[a] = (T)(p.mm[a * n + i] + p.dt * sm);
+        ((T*)q.cm)[a * n + i] = nm[a];
+      }
+      const T mu = (T)p.magMom_u[i];
+      T4 v;
+      v.x = nm[0] * mu;
+      v.y = nm[1] * mu;
+      v.z = nm[2] * mu;
+      v.w = (T)p.rMag_u[i];
+      ((T4*)p.s.mu)[r] = v;
+    } else {
+      double ev[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        double sm = 0;
+        for (int j = 0; j <= q.s; j++) {
+          if (q.e[j] == 0.0) continue;
+          const double kmj = j == q.s ? (double)km[a] : (double)((const T*)q.km[j])[a * n + i];
+          sm += q.e[j] * kmj;
+        }
+        ev[a] = sm;
+      }
+      err = sqrt(ev[0] * ev[0] + ev[1] * ev[1] + ev[2] * ev[2]);
+    }
+  }
+  if (q.last) {
+    // non-negative doubles order like their bit patterns
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(kFull, err, o));
+    if ((threadIdx.x & 31) == 0 && err > 0.0)
+      atomicMax(q.errmax, (unsigned long long)__double_as_longlong(err));
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kIntThreads) k_rk_accept(RKStage q) {
+  const IntParams& p = q.p;
+  const int i = blockIdx.x * kIntThreads + threadIdx.x;
+  const int n = p.n;
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  double disp2 = 0;
+  if (i < n) {
+    const int r = p.s.rank[i];
+    T mn[3], en[3], z[9], fth[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      if (q.last) {  // Bogacki-Shampine: the last stage's coordinates
+        mn[a] = ((const T*)q.cm)[a * n + i];
+        en[a] = ((const T*)q.ce)[a * n + i];
+      } else {
+        double sm = 0, se = 0;
+        for (int j = 0; j <= q.s; j++) {
+          if (q.a[j] == 0.0) continue;
+          sm += q.a[j] * (double)((const T*)q.km[j])[a * n + i];
+          se += q.a[j] * (double)((const T*)q.ke[j])[a * n + i];
+        }
+        en[a] = (T)(p.ea[a * n + i] + p.dt * se);
+        mn[a] = (T)(p.mm[a * n + i] + p.dt * sm);
+      }
+    }
+    // the thermal force at the scale of the step's first trial (the
+    // reference rescales it on rejections only after it entered the force)
+    noise9<T>(p, i, z);
+    const T sF = (T)p.sF[i];
+#pragma unroll
+    for (int a = 0; a < 3; a++) fth[a] = sF * z[6 + a];
+    finish_particle<T>(p, i, r, mn, en, fth, acc, disp2);
+  }
+  step_block_sums(p, blockIdx.x, acc, disp2);
+}
+
+int launch_rk_stage(cudaStream_t st, const RKStage& q, bool fp64) {
+  const int g = (q.p.n + kIntThreads - 1) / kIntThreads;
+  if (fp64)
+    k_rk_stage<double><<<g, kIntThreads, 0, st>>>(q);
+  else
+    k_rk_stage<float><<<g, kIntThreads, 0, st>>>(q);
+  return 1;
+}
+
+int launch_rk_accept(cudaStream_t st, const RKStage& q, bool fp64) {
+  const int g = (q.p.n + kIntThreads - 1) / kIntThreads;
+  if (fp64)
+    k_rk_accept<double><<<g, kIntThreads, 0, st>>>(q);
+  else
+    k_rk_accept<float><<<g, kIntThreads, 0, st>>>(q);
   return 1;
 }
 

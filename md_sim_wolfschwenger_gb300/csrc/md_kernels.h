@@ -78,6 +78,9 @@ int launch_obs_packed(cudaStream_t st, const ObsParams* ps, int R);
 // B, F in SI (orig order, double) from the stage outputs; optional overlap push.
 // Real-space field and force alone of the last full evaluation (test hook).
 int launch_real_part(cudaStream_t st, const IntParams& p, double* Bout, double* Fout, bool fp64);
+// Adaptive Runge-Kutta stage / accept kernels (md_integrate.cu).
+int launch_rk_stage(cudaStream_t st, const RKStage& q, bool fp64);
+int launch_rk_accept(cudaStream_t st, const RKStage& q, bool fp64);
 int launch_combine(cudaStream_t st, const IntParams& p, double* Bout, double* Fout, int apply_overlap,
                    bool fp64);
 

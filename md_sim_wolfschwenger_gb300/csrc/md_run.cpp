@@ -10,10 +10,13 @@
 // MSDx/MSDy/MSDz.txt, mz.txt and t.txt, written with the reference's text
 // format (src/postprocessing.cpp, src/simulation.cpp:466-537).
 //
+// Time stepping: the configuration's SOLVER (0 Heun-Euler, 1
+// Bogacki-Shampine, 2 Dormand-Prince) with the reference's step control
+// (absTol, deltaTmin, deltaTmax), as the reference runs; --fixed-dt instead
+// takes every step with deltaTinit (Heun, every step accepted), the mode of
+// the benchmark configurations.
+//
 // Differences, stated on stdout when they apply:
-//   * the time step is fixed at deltaTinit (SOLVER = 0, Heun, with every step
-//     accepted); SOLVER = 1, 2 (adaptive Bogacki-Shampine / Dormand-Prince)
-//     are reported and run as fixed-step Heun;
 //   * thermal noise comes from the counter-based Philox generator (or is off,
 //     per the [gb300] noise key), not EigenRand's Mersenne Twister;
 //   * READ_FROM_FILE reads the last frame of coords_final.txt in the layout
@@ -43,12 +46,13 @@ struct Opts {
   int device = 0;
   int64_t chunk = 100000;    // steps between record read-backs
   bool quiet = false;
+  bool fixed_dt = false;     // every step with deltaTinit (Heun)
 };
 
 void usage() {
   std::printf(
       "usage: md_run [configuration.ini] [--out DIR] [--precision mixed|fp64] [--autotune K]\n"
-      "              [--device D] [--chunk STEPS] [--quiet]\n"
+      "              [--device D] [--chunk STEPS] [--fixed-dt] [--quiet]\n"
       "Runs MD_Sim_Wolfschwenger's simulation (InitSimulation + RunSimulation) with the time step on\n"
       "the GPU; the configuration defaults to ../configuration.ini like the reference.\n");
 }
@@ -134,6 +138,8 @@ int main(int argc, char** argv) {
       o.chunk = std::max<int64_t>(1, std::atoll(next("--chunk")));
     } else if (a == "--quiet") {
       o.quiet = true;
+    } else if (a == "--fixed-dt") {
+      o.fixed_dt = true;
     } else if (!a.empty() && a[0] == '-') {
       std::fprintf(stderr, "md_run: unknown option %s\n", a.c_str());
       usage();
@@ -148,9 +154,12 @@ int main(int argc, char** argv) {
   CALL(nullptr, md_config_load_ini(o.ini.c_str(), &cfg));
   const int prec = o.precision >= 0 ? o.precision : (int)cfg.precision;
   const int64_t n = md_config_numb_part(&cfg);
-  if (cfg.SOLVER != 0)
-    std::printf("note: SOLVER = %lld (adaptive) is run as Heun with the fixed step deltaTinit = %g s\n",
-                (long long)cfg.SOLVER, cfg.deltaTinit);
+  if (!o.fixed_dt && (cfg.SOLVER < 0 || cfg.SOLVER > 2)) {
+    std::fprintf(stderr, "md_run: SOLVER must be 0, 1 or 2\n");
+    return 1;
+  }
+  if (o.fixed_dt)
+    std::printf("note: fixed step deltaTinit = %g s (Heun, every step accepted)\n", cfg.deltaTinit);
   std::vector<double> rMag((size_t)n), rHydr((size_t)n), pos(3 * (size_t)n), mm(3 * (size_t)n), ea(3 * (size_t)n);
   double lBox = 0;
   CALL(nullptr, md_init_system(&cfg, n, (uint64_t)cfg.seed, rMag.data(), rHydr.data(), pos.data(), mm.data(),
@@ -187,53 +196,79 @@ int main(int argc, char** argv) {
   CALL(nullptr, md_write_data_txt(path_in(o, "data.txt").c_str(), &cfg, n, rMag.data(), rHydr.data(), lBox));
 
   // ------------------------------------------------------ RunSimulation
-  // The loop's time points and the coords frames, with the reference's own
-  // double arithmetic (tInt += deltaT; the frame test at the top of the
-  // loop body, written after the step, src/simulation.cpp:466-520).
-  const double dt = cfg.deltaTinit, tEnd = cfg.tEnd;
-  struct Frame {
-    int64_t step;
-    double t;
+  // The frame test sits at the top of the loop body and its frame is written
+  // after the step with the step's start time (src/simulation.cpp:466-520).
+  const double tEnd = cfg.tEnd;
+  const std::string coords = path_in(o, "coords.txt");
+  std::vector<double> rec;
+  auto pull_records = [&]() {
+    int64_t nr = 0;
+    CALL(ctx, md_num_records(ctx, &nr));
+    const size_t at = rec.size();
+    rec.resize(at + 8 * (size_t)nr);
+    CALL(ctx, md_records(ctx, 0, nr, rec.data() + at));
+    CALL(ctx, md_clear_records(ctx));
   };
-  std::vector<Frame> frames;
+  auto write_frame = [&](double label, int64_t count) {
+    CALL(ctx, md_state_download(ctx, pos.data(), mm.data(), ea.data()));
+    CALL(nullptr, md_write_coords_txt(coords.c_str(), n, pos.data(), mm.data(), ea.data(), label));
+    if (!o.quiet)
+      std::printf("actual time: %gs\nsimulation progress: %g%%\n", label, (double)count / cfg.npCoords * 100.0);
+  };
   int64_t steps = 0;
   double tInt = 0;
-  {
+  if (o.fixed_dt) {
+    // time points and frames with the reference's own double arithmetic
+    const double dt = cfg.deltaTinit;
+    struct Frame {
+      int64_t step;
+      double t;
+    };
+    std::vector<Frame> frames;
+    {
+      int64_t count = 0;
+      while (tInt <= tEnd) {
+        if (std::floor(tInt / tEnd * cfg.npCoords) == (double)count) {
+          frames.push_back({steps, tInt});
+          count++;
+        }
+        tInt += dt;
+        steps++;
+      }
+    }
+    rec.reserve(8 * (size_t)steps);
+    int64_t done = 0;
+    auto advance = [&](int64_t upto) {  // runs steps [done, upto)
+      while (done < upto) {
+        const int64_t k = std::min(o.chunk, upto - done);
+        CALL(ctx, md_step(ctx, k, dt, nullptr));
+        pull_records();
+        done += k;
+      }
+    };
+    for (size_t f = 0; f < frames.size(); f++) {
+      advance(frames[f].step + 1);
+      write_frame(frames[f].t, (int64_t)f);
+    }
+    advance(steps);
+  } else {
+    // adaptive: one accepted step at a time (the next time point is known
+    // only after the step control has run)
+    double dt = cfg.deltaTinit;
     int64_t count = 0;
     while (tInt <= tEnd) {
-      if (std::floor(tInt / tEnd * cfg.npCoords) == (double)count) {
-        frames.push_back({steps, tInt});
-        count++;
-      }
-      tInt += dt;
+      const bool frame = std::floor(tInt / tEnd * cfg.npCoords) == (double)count;
+      int64_t k = 0;
+      CALL(ctx, md_step_adaptive(ctx, 1, tEnd, &dt, nullptr, &k));
+      if (k != 1) break;
+      if (frame) write_frame(tInt, count++);
+      int64_t sdev = 0;
+      CALL(ctx, md_get_time(ctx, &tInt, &sdev));
       steps++;
+      if (steps % o.chunk == 0) pull_records();
     }
+    pull_records();
   }
-  std::vector<double> rec;
-  rec.reserve(8 * (size_t)steps);
-  int64_t done = 0;
-  auto advance = [&](int64_t upto) {  // runs steps [done, upto)
-    while (done < upto) {
-      const int64_t k = std::min(o.chunk, upto - done);
-      CALL(ctx, md_step(ctx, k, dt, nullptr));
-      int64_t nr = 0;
-      CALL(ctx, md_num_records(ctx, &nr));
-      const size_t at = rec.size();
-      rec.resize(at + 8 * (size_t)nr);
-      CALL(ctx, md_records(ctx, 0, nr, rec.data() + at));
-      CALL(ctx, md_clear_records(ctx));
-      done += k;
-    }
-  };
-  const std::string coords = path_in(o, "coords.txt");
-  for (size_t f = 0; f < frames.size(); f++) {
-    advance(frames[f].step + 1);
-    CALL(ctx, md_state_download(ctx, pos.data(), mm.data(), ea.data()));
-    CALL(nullptr, md_write_coords_txt(coords.c_str(), n, pos.data(), mm.data(), ea.data(), frames[f].t));
-    if (!o.quiet)
-      std::printf("actual time: %gs\nsimulation progress: %g%%\n", frames[f].t, f / cfg.npCoords * 100.0);
-  }
-  advance(steps);
   double tDev = 0;
   int64_t sDev = 0;
   CALL(ctx, md_get_time(ctx, &tDev, &sDev));

@@ -212,6 +212,22 @@ class Simulation:
             xp = _P(xi)
         self._ck(self.L.md_step(self.h, int(nsteps), dt, xp))
 
+    def step_adaptive(self, max_steps, dt, t_end=float("inf"), xi=None):
+        """Accepted steps of RunSimulation's loop with the configuration's
+        SOLVER (0 Heun-Euler, 1 Bogacki-Shampine, 2 Dormand-Prince) and the
+        reference's step control, while t <= t_end; returns (next trial dt,
+        steps done)."""
+        d = C.c_double(float(dt))
+        k = C.c_int64()
+        xp = None
+        if xi is not None:
+            xi = np.ascontiguousarray(xi, dtype=np.float64)
+            if xi.size != 9 * self.n * max_steps:
+                raise ValueError("xi must hold 9N normals per step")
+            xp = _P(xi)
+        self._ck(self.L.md_step_adaptive(self.h, int(max_steps), float(t_end), C.byref(d), xp, C.byref(k)))
+        return d.value, k.value
+
     def records(self, first=0, count=None):
         """Per-step {t, mz, MSDx, MSDy, MSDz, Pxy, Pxz, Pyz} rows."""
         n = C.c_int64()

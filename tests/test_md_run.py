@@ -1,7 +1,8 @@
 """The drop-in executable md_run (InitSimulation + RunSimulation of the
 reference, src/simulation.cpp:24-537, with the step on the GPU): command line
 and errors on CPU; on the GPU, the output files it writes equal those written
-from the same system stepped through the Python API, byte for byte."""
+from the same system stepped through the Python API, byte for byte, with the
+fixed step and with the adaptive solvers."""
 import os
 import subprocess
 
@@ -60,7 +61,7 @@ def test_outputs_equal_python_api_run(tmp_path):
     ref_io.write_ini(tmp_path / "configuration.ini", ini)
     run = tmp_path / "run"
     run.mkdir()
-    r = _run(["--precision", "mixed", "--chunk", "37", "--quiet"], run)
+    r = _run(["--precision", "mixed", "--chunk", "37", "--quiet", "--fixed-dt"], run)
     assert r.returncode == 0, r.stderr
     assert "simulation ended successfully" in r.stdout
     names = sorted(os.listdir(run))
@@ -101,3 +102,37 @@ def test_outputs_equal_python_api_run(tmp_path):
     last = _frames(ref / "final.txt")[0]
     np.testing.assert_array_equal(fr[-1][:, :9], last[:, :9])
     assert len(np.loadtxt(run / "mz.txt")) == steps
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver", [0, 2])
+def test_adaptive_outputs_equal_python_api_run(tmp_path, solver):
+    import md_sim_wolfschwenger_gb300 as m
+    from md_sim_wolfschwenger_gb300 import outputs
+    ini = ref_io.ini_dict(npDim=4, tMag=2e-11, tRelax=1e-11, deltaTinit=1e-12, magFluxDens=0.02, seed=9,
+                          SOLVER=solver, absTol=1e-4, volFrac=0.05)
+    ini["output_settings"]["npCoords"] = 5
+    ref_io.write_ini(tmp_path / "configuration.ini", ini)
+    run = tmp_path / "run"
+    run.mkdir()
+    r = _run(["--precision", "fp64", "--quiet"], run)
+    assert r.returncode == 0, r.stderr
+    cfg = m.Configuration.from_ini(tmp_path / "configuration.ini")
+    n = cfg.numb_part()
+    rMag, rHydr, pos, mm, ea, L = m.init_system(cfg, n, 9)
+    sim = m.Simulation(cfg, n, m.MD_PREC_FP64, rMag=rMag, rHydr=rHydr)
+    sim.set_state(pos, mm, ea)
+    a, rc, kc, _, _ = sim.ewald_params()
+    sim.set_ewald(a, rc, kc)
+    sim.set_noise(m.MD_NOISE_PHILOX, 9)
+    _, steps = sim.step_adaptive(100000, cfg.c.deltaTinit, t_end=cfg.c.tEnd)
+    rec = sim.records()
+    t_end = sim.get_time()[0]
+    sim.close()
+    assert steps >= 3 and len(np.atleast_1d(np.loadtxt(run / "t.txt"))) == steps
+    ref = tmp_path / "api"
+    ref.mkdir()
+    outputs.export_records(str(ref), rec, t_end, steps)
+    for nm in ("dtMean.txt", "Pxy.txt", "MSDx.txt", "MSDz.txt", "mz.txt", "t.txt"):
+        assert (run / nm).read_bytes() == (ref / nm).read_bytes(), nm
+    assert np.all(np.diff(rec[:, 0]) > 0)
