@@ -589,13 +589,13 @@ def run_ours(args):
                            frac=(ach / hbm_peak) if hbm_peak else None)
         segs[k] = ent
     dom = max((k for k in segs if k in work), key=lambda k: segs[k]["ms"])
-    traffic = None
+    traffic = None  # from the ncu capture of this workload, when there is one
     try:
         for ln in open(os.path.join(ROOT, "profiles", "traffic.txt")):
             f = ln.split()
-            if len(f) == 2 and f[0] == dom and not ln.startswith("#"):
-                traffic = float(f[1])
-    except OSError:
+            if len(f) == 4 and not ln.startswith("#") and f[0] == args.workload and int(f[1]) == n and f[2] == dom:
+                traffic = float(f[3])
+    except (OSError, ValueError):
         pass
     d = segs[dom]
     roofline = {"kernel": dom, "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"], "unit": d["unit"],

@@ -48,6 +48,8 @@
 //
 // Roofline: FP32/SFU issue bound.  Algorithmic FLOPs per unordered in-range
 // pair (counted from the reference formula): 113 full, 58 field only.
+#include <algorithm>
+
 #include "md_common.cuh"
 #include "md_kernels.h"
 
@@ -84,12 +86,12 @@ __device__ __forceinline__ void pair_terms(const RealParams& p, T dx, T dy, T dz
   a.np++;
   T ir0, r0;
   if constexpr (std::is_same<T, float>::value) {
-    // r correctly rounded from the (once-rounded) exact r^2, 1/r to ~1 ulp:
-    // the pair terms go as r^-4 .. r^-7, so r's rounding is the largest
+    // 1/r to ~1 ulp (rsqrt + one Newton step) from the once-rounded exact
+    // r^2: the pair terms go as r^-4 .. r^-7, so r's rounding is the largest
     // FP32 error source near contact
-    r0 = __fsqrt_rn(r2);
     ir0 = rsqrtf(r2);
     ir0 = ir0 * fmaf(-0.5f * r2 * ir0, ir0, 1.5f);
+    r0 = r2 * ir0;
   } else {
     ir0 = rsqrt(r2);
     r0 = r2 * ir0;
@@ -494,9 +496,12 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
 
 // ------------------------------------------------------------ entry points
 
+// Grid-stride over the particle blocks: most steps do not rebuild, and a
+// grid of a few blocks per SM then costs one flag read per block.
 template <typename T, bool FILL>
-__global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build(RealParams p) {
-  nbr_build<T, FILL>(p, blockIdx.x);
+__global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build(RealParams p, int nblk) {
+  if (!p.flags->rebuild) return;
+  for (int bx = blockIdx.x; bx < nblk; bx += gridDim.x) nbr_build<T, FILL>(p, bx);
 }
 __global__ void __launch_bounds__(1024) k_nbr_scan(RealParams p) { nbr_scan(p); }
 template <typename T, bool FULL, bool COAT>
@@ -526,17 +531,24 @@ __global__ void __launch_bounds__(kRealWarps * 32, COAT ? 2 : 4) k_real_packed(c
 int real_blocks(int n) { return (n + kRealWarps - 1) / kRealWarps; }
 
 int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64) {
-  dim3 grid(real_blocks(p.n)), block(kRealWarps * 32);
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
+  }
+  const int nblk = real_blocks(p.n);
+  dim3 grid(std::min(nblk, 8 * nsm)), block(kRealWarps * 32);
   if (fp64)
-    k_nbr_build<double, false><<<grid, block, 0, st>>>(p);
+    k_nbr_build<double, false><<<grid, block, 0, st>>>(p, nblk);
   else
-    k_nbr_build<float, false><<<grid, block, 0, st>>>(p);
+    k_nbr_build<float, false><<<grid, block, 0, st>>>(p, nblk);
   (void)flags;
   k_nbr_scan<<<1, 1024, 0, st>>>(p);
   if (fp64)
-    k_nbr_build<double, true><<<grid, block, 0, st>>>(p);
+    k_nbr_build<double, true><<<grid, block, 0, st>>>(p, nblk);
   else
-    k_nbr_build<float, true><<<grid, block, 0, st>>>(p);
+    k_nbr_build<float, true><<<grid, block, 0, st>>>(p, nblk);
   return 3;
 }
 
