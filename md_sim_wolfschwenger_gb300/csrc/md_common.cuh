@@ -86,7 +86,6 @@ struct RealParams {
   CellGrid grid;
   double alpha, rc;      // box units
   double rc2, rc2_test;  // exact and (slightly larger) candidate cutoff
-  unsigned long long rc2_fix;  // rc^2 in units of (L 2^-32)^2: exact in-range test on the mixed path
   double c2a;            // 2 alpha / sqrt(pi)
   double al2, al4;       // alpha^2, alpha^4
   double cont_eps;       // 1e-10 m / L (contact offset, interaction.cpp:120)

@@ -117,7 +117,6 @@ RealParams real_params(md_ctx* c, void* B, void* F, void* ov) {
   p.alpha = a;
   p.rc = rcb;
   p.rc2 = rcb * rcb;
-  p.rc2_fix = (unsigned long long)std::ldexp(rcb * rcb, 64);  // rcb <= 1/2: below 2^62
   const double rt = rcb * (1.0 + 1e-6) + 2e-7;
   p.rc2_test = rt * rt;
   p.c2a = 2.0 * a * g.irPi;
@@ -770,10 +769,12 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
     CK(c, cudaMemcpy(c->cell_start, h, sizeof h, cudaMemcpyHostToDevice));
   }
   const size_t nk = (size_t)c->klist.nk, nseg = c->klist.seg.size();
-  if (nk + 2 > c->ksize_cap || nseg + 2 > c->ksize_cap) {
+  const size_t nks = (size_t)c->klist.nk_scat, nrseg = c->klist.rseg.size();
+  const size_t need = std::max(std::max(nk, nseg), std::max(nks, nrseg)) + 2;
+  if (need > c->ksize_cap) {
     void* old[] = {c->kseg, c->koff, c->ek, c->eS, c->Sfull, c->rseg, c->rowpos, c->chunks};
     for (void* p : old) dfree(c, p);
-    const size_t cap = std::max(nk, nseg) + 2;
+    const size_t cap = need;
     int st;
     if ((st = dalloc(c, &c->kseg, sizeof(KSeg) * cap))) return st;
     if ((st = dalloc(c, &c->koff, sizeof(int) * cap))) return st;
@@ -811,8 +812,10 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
   CK(c, cudaMemcpy(c->kseg, c->klist.seg.data(), sizeof(KSeg) * nseg, cudaMemcpyHostToDevice));
   CK(c, cudaMemcpy(c->koff, c->klist.koff.data(), sizeof(int) * nseg, cudaMemcpyHostToDevice));
   CK(c, cudaMemcpy(c->ek, c->klist.ek.data(), sizeof(double) * nk, cudaMemcpyHostToDevice));
-  CK(c, cudaMemcpy(c->rseg, c->klist.rseg.data(), sizeof(KSeg) * nseg, cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->rseg, c->klist.rseg.data(), sizeof(KSeg) * nrseg, cudaMemcpyHostToDevice));
   CK(c, cudaMemcpy(c->rowpos, c->klist.rowpos.data(), sizeof(int) * nk, cudaMemcpyHostToDevice));
+  // the padding entries of the scatter layout are never written: zero
+  CK(c, cudaMemset(c->eS, 0, 2 * tsz(c) * nks));
   CK(c, cudaMemcpy(c->chunks, c->klist.chunks.data(), sizeof(int) * c->klist.chunks.size(), cudaMemcpyHostToDevice));
   {
     // neighbour-list capacity: uniform-density estimate + margin (grown on overflow)

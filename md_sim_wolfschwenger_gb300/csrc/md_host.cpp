@@ -484,8 +484,11 @@ double choose_rc(const md_config& c, const EwaldModel& m, int64_t n, double* alp
 KList build_klist(int kc, double w) {
   KList L;
   const int kc2 = kc * kc;
-  std::vector<md::KSeg> segs;
-  std::vector<int> reals;
+  // rows of the half space: (ny, nz) with nx in [x0, x1]
+  struct Row {
+    int ny, nz, x0, x1;
+  };
+  std::vector<Row> rows;
   for (int nz = 0; nz <= kc; nz++)
     for (int ny = -kc; ny <= kc; ny++) {
       if (nz == 0 && ny < 0) continue;
@@ -496,54 +499,67 @@ KList build_klist(int kc, double w) {
       while (m * m > rem) m--;
       int x0 = (nz == 0 && ny == 0) ? 1 : -m, x1 = m;
       if (x1 < x0) continue;
-      int len = x1 - x0 + 1;
-      int ns = (len + 15) / 16;
-      int base = len / ns, extra = len % ns, x = x0;
+      rows.push_back({ny, nz, x0, x1});
+    }
+  // rows split evenly into pieces of at most `maxlen`, padded to multiples of 4
+  auto split = [&](int maxlen, std::vector<md::KSeg>* segs, std::vector<int>* reals) {
+    for (const Row& r : rows) {
+      const int len = r.x1 - r.x0 + 1, ns = (len + maxlen - 1) / maxlen;
+      const int base = len / ns, extra = len % ns;
+      int x = r.x0;
       for (int s = 0; s < ns; s++) {
-        int l = base + (s < extra ? 1 : 0);
-        md::KSeg sg;
-        sg.nx0 = x;
-        sg.ny = ny;
-        sg.nz = nz;
-        sg.len = (l + 3) & ~3;
-        segs.push_back(sg);
-        reals.push_back(l);
+        const int l = base + (s < extra ? 1 : 0);
+        segs->push_back(md::KSeg{x, r.ny, r.nz, (l + 3) & ~3});
+        reals->push_back(l);
         x += l;
       }
     }
+  };
+  // structure factor: segments of <= 16, sorted by length (uniform warps)
+  std::vector<md::KSeg> segs;
+  std::vector<int> reals;
+  split(16, &segs, &reals);
   std::vector<int> order(segs.size());
   for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return segs[a].len > segs[b].len; });
-  // row order (generation order): k offsets and chunks of <= kKChunk k's
-  std::vector<int> rkoff(segs.size());
-  int roff = 0;
-  L.rseg = segs;
-  L.chunks.clear();
-  int chunk_k = 0;
-  for (size_t s = 0; s < segs.size(); s++) {
-    if (s == 0 || chunk_k + segs[s].len > md::kKChunk) {
+  // scatter: whole rows (<= kScatSeg), row order, chunks of <= kKChunk k's
+  std::vector<int> sreals;
+  split(md::kScatSeg, &L.rseg, &sreals);
+  std::map<std::pair<int, int>, int> row_first;  // (ny, nz) -> first scatter segment
+  std::vector<int> soff(L.rseg.size());
+  int roff = 0, chunk_k = 0;
+  for (size_t s = 0; s < L.rseg.size(); s++) {
+    if (s == 0 || chunk_k + L.rseg[s].len > md::kKChunk) {
       L.chunks.push_back((int)s);
       L.chunks.push_back(roff);
       chunk_k = 0;
     }
-    rkoff[s] = roff;
-    roff += segs[s].len;
-    chunk_k += segs[s].len;
+    soff[s] = roff;
+    roff += L.rseg[s].len;
+    chunk_k += L.rseg[s].len;
+    row_first.emplace(std::make_pair(L.rseg[s].ny, L.rseg[s].nz), (int)s);
   }
   L.nchk = (int)L.chunks.size() / 2;
-  L.chunks.push_back((int)segs.size());
+  L.chunks.push_back((int)L.rseg.size());
   L.chunks.push_back(roff);
+  L.nk_scat = roff;
+  // position of k = (nx, ny, nz) in the scatter layout
+  auto scat_pos = [&](int nx, int ny, int nz) {
+    int s = row_first.at(std::make_pair(ny, nz));
+    while (nx >= L.rseg[s].nx0 + sreals[s]) s++;
+    return soff[s] + (nx - L.rseg[s].nx0);
+  };
   L.rowpos.clear();
   int off = 0;
   for (int idx : order) {
     const md::KSeg& sg = segs[idx];
     L.seg.push_back(sg);
     L.koff.push_back(off);
-    for (int t = 0; t < sg.len; t++) L.rowpos.push_back(rkoff[idx] + t);
     for (int t = 0; t < sg.len; t++) {
-      int nx = sg.nx0 + t;
-      bool real = t < reals[idx];
-      double n2 = (double)nx * nx + (double)sg.ny * sg.ny + (double)sg.nz * sg.nz;
+      const int nx = sg.nx0 + t;
+      const bool real = t < reals[idx];
+      L.rowpos.push_back(real ? scat_pos(nx, sg.ny, sg.nz) : -1);
+      const double n2 = (double)nx * nx + (double)sg.ny * sg.ny + (double)sg.nz * sg.nz;
       L.ek.push_back(real ? 2.0 * std::exp(-w * n2) / n2 : 0.0);
       L.kx.push_back(nx);
       L.ky.push_back(sg.ny);

@@ -57,10 +57,13 @@ struct KList {
   std::vector<md::KSeg> seg;   // length-sorted (structure factor)
   std::vector<int> koff;
   std::vector<double> ek;
-  std::vector<md::KSeg> rseg;  // row order (scatter)
-  std::vector<int> rowpos;     // sorted k -> row-order k
+  // scatter layout: whole k rows (split evenly above kScatSeg), each padded
+  // to a multiple of 4, in row order
+  std::vector<md::KSeg> rseg;
+  std::vector<int> rowpos;     // sorted padded k -> scatter-layout k (-1: padding)
   std::vector<int> chunks;     // pairs (first row segment, first row k), nchk + 1 pairs
   int nchk = 0;
+  int nk_scat = 0;             // length of the scatter layout
   std::vector<int> kx, ky, kz;  // per padded k (padding k's are marked by kreal = 0)
   std::vector<char> kreal;
   int nk = 0, nk_real = 0;

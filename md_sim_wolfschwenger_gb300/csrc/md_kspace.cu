@@ -24,8 +24,10 @@
 // uniform), particles staged through shared-memory tiles of 64; FP32 sums over
 // a chunk of <= 512 particles, FP64 across chunks (k_sk_reduce), which also
 // applies e(n) and writes e*S in row order for the scatter.
-// Scatter (k_kscatter): threads = (particle, partition); the k rows are split
-// into chunks staged in shared memory and dealt round-robin to 4 partitions
+// Scatter (k_kscatter): threads = (particle, partition); whole k rows (its own
+// layout: one segment per row up to 64 k's, so the per-segment work of phase
+// setup and sums is paid once per row) are grouped into chunks staged in
+// shared memory and dealt round-robin to 4 partitions
 // of threads that share the particle's tables; FP32 per segment, blocks of 8
 // segments added with Kahan compensation (mixed path); the partitions are
 // summed in a fixed order.
@@ -229,7 +231,8 @@ __device__ __forceinline__ void sk_reduce(const KParams& p, int bx) {
     T2 o;
     o.x = (T)(e * a);
     o.y = (T)(e * b);
-    ((T2*)p.eS)[p.rowpos[kk]] = o;
+    const int pos = p.rowpos[kk];
+    if (pos >= 0) ((T2*)p.eS)[pos] = o;
   }
   if (bx == 0 && threadIdx.x < 3) {
     double s = 0;
@@ -312,43 +315,41 @@ __device__ __forceinline__ void kscatter(const KParams& p, int bx, int kcmax) {
       if (sg.nx0 < 0) X.y = -X.y;
       T pr, pi;
       cmul<T>(X.x, X.y, yzr, yzi, pr, pi);
-      // k = (nx0 + u, ny, nz), u = 0..len-1.  With G_u = Re(conj(eS) phase)
-      // and H_u = Im(conj(eS) phase), the field needs sum G_u n_u and the
-      // force sum H_u (n_u . mu) n_u; both follow from the moments
-      // sum u^p G_u (p <= 1) and sum u^p H_u (p <= 2), whose weights u, u^2
-      // are constants of the unrolled loop.
-      T g0 = 0, g1 = 0, h0 = 0, h1 = 0, h2 = 0;
+      // k = (nx0 + u, ny, nz), u = 0..len-1: the field takes G n with
+      // G = Re(conj(eS) phase), the force H (n . mu) n with H = Im(conj(eS)
+      // phase); n_x and n . mu advance by 1 and mu_x per k
+      T nxf = (T)sg.nx0;
+      T w = 0;
+      if constexpr (FULL) w = nxf * mu.x + (T)sg.ny * mu.y + (T)sg.nz * mu.z;
+      T gx = 0, gs = 0, hx = 0, hs = 0;
       const T2* es_seg = es_s + ko;
 #pragma unroll
-      for (int q = 0; q < kSegMax; q += 4) {
+      for (int q = 0; q < kScatSeg; q += 4) {
         if (q >= sg.len) break;
 #pragma unroll
         for (int u = 0; u < 4; u++) {
           const T2 es = es_seg[q + u];
-          const T uf = (T)(q + u);
           const T g = es.x * pr + es.y * pi;
-          g0 += g;
-          g1 += uf * g;
+          gx += g * nxf;
+          gs += g;
           if constexpr (FULL) {
-            const T h = es.x * pi - es.y * pr;
-            h0 += h;
-            h1 += uf * h;
-            h2 += (uf * uf) * h;
+            const T h = (es.x * pi - es.y * pr) * w;
+            hx += h * nxf;
+            hs += h;
+            w += mu.x;
           }
           const T npr = pr * E.x - pi * E.y;
           pi = pr * E.y + pi * E.x;
           pr = npr;
+          nxf += (T)1;
         }
       }
       ko += sg.len;
-      const T nx0 = (T)sg.nx0;
-      bb[0] += nx0 * g0 + g1;
-      bb[1] += g0 * (T)sg.ny;
-      bb[2] += g0 * (T)sg.nz;
+      bb[0] += gx;
+      bb[1] += gs * (T)sg.ny;
+      bb[2] += gs * (T)sg.nz;
       if constexpr (FULL) {
-        const T w0 = nx0 * mu.x + (T)sg.ny * mu.y + (T)sg.nz * mu.z;
-        const T hs = w0 * h0 + mu.x * h1;
-        fb[0] += w0 * nx0 * h0 + (w0 + mu.x * nx0) * h1 + mu.x * h2;
+        fb[0] += hx;
         fb[1] += hs * (T)sg.ny;
         fb[2] += hs * (T)sg.nz;
       }

@@ -86,11 +86,7 @@ __device__ __forceinline__ void pair_terms(const RealParams& p, T dx, T dy, T dz
   a.np++;
   T ir0, r0;
   if constexpr (std::is_same<T, float>::value) {
-    // 1/r to ~1 ulp (rsqrt + one Newton step) from the once-rounded exact
-    // r^2: the pair terms go as r^-4 .. r^-7, so r's rounding is the largest
-    // FP32 error source near contact
     ir0 = rsqrtf(r2);
-    ir0 = ir0 * fmaf(-0.5f * r2 * ir0, ir0, 1.5f);
     r0 = r2 * ir0;
   } else {
     ir0 = rsqrt(r2);
@@ -375,22 +371,17 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
   Acc<T> a;
   const T4 mi = ((const T4*)p.s.mu)[k];
   const Self<T> me = load_self<T, COAT>(p, k);
+  const float rc2_fix = (float)(p.rc2 * 18446744073709551616.0);  // (rc / (L 2^-32))^2
 
   // pair terms with the neighbour's loaded coordinates and moment (mixed path)
   auto eval_loaded = [&](const int4& sj, const T4& mj) {
     if constexpr (F32) {
-      // wrapping 32-bit differences are the exact minimum image; r^2 in
-      // 64-bit integers is exact, so the cutoff test is exact and r^2 is
-      // rounded once
-      const int dxi = sj.x - me.si.x, dyi = sj.y - me.si.y, dzi = sj.z - me.si.z;
-      const unsigned long long R2 = (unsigned long long)((long long)dxi * dxi) +
-                                    (unsigned long long)((long long)dyi * dyi) +
-                                    (unsigned long long)((long long)dzi * dzi);
-      if (R2 < p.rc2_fix) {
+      // wrapping 32-bit differences are the exact minimum image
+      const float dxf = (float)(sj.x - me.si.x), dyf = (float)(sj.y - me.si.y), dzf = (float)(sj.z - me.si.z);
+      if (dxf * dxf + dyf * dyf + dzf * dzf < rc2_fix) {
         const float sc = 2.3283064365386963e-10f;  // 2^-32
-        const float dx = (float)dxi * sc, dy = (float)dyi * sc, dz = (float)dzi * sc;
-        const float r2 = __ull2float_rn(R2) * 5.421010862427522e-20f;  // 2^-64
-        pair_terms<T, FULL, COAT>(p, dx, dy, dz, r2, mi, mj, me.oi, COAT ? sj.w : 0, a);
+        const float dx = dxf * sc, dy = dyf * sc, dz = dzf * sc;
+        pair_terms<T, FULL, COAT>(p, dx, dy, dz, dx * dx + dy * dy + dz * dz, mi, mj, me.oi, COAT ? sj.w : 0, a);
       }
     }
   };
@@ -398,7 +389,13 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
   auto eval = [&](int j) {
     const T4 mj = ((const T4*)p.s.mu)[j];
     if constexpr (F32) {
-      eval_loaded(p.s.xi[j], mj);
+      const int4 sj = p.s.xi[j];
+      const float dxf = (float)(sj.x - me.si.x), dyf = (float)(sj.y - me.si.y), dzf = (float)(sj.z - me.si.z);
+      if (dxf * dxf + dyf * dyf + dzf * dzf < rc2_fix) {
+        const float sc = 2.3283064365386963e-10f;
+        const float dx = dxf * sc, dy = dyf * sc, dz = dzf * sc;
+        pair_terms<T, FULL, COAT>(p, dx, dy, dz, dx * dx + dy * dy + dz * dz, mi, mj, me.oi, COAT ? sj.w : 0, a);
+      }
     } else {
       const double4_32a dj = p.s.xd[j];
       double dx = dj.x - me.di.x, dy = dj.y - me.di.y, dz = dj.z - me.di.z;

@@ -18,6 +18,9 @@ struct KSeg {
 
 // k vectors per shared-memory chunk of the k-space scatter.
 constexpr int kKChunk = 512;
+// Longest k-row segment of the scatter (rows longer than this are split
+// evenly); the structure factor uses segments of at most 16.
+constexpr int kScatSeg = 64;
 // Thread partitions of the k-space scatter: each particle's k range is split
 // over this many threads (by chunk), reduced in a fixed order.
 constexpr int kScatterParts = 4;
