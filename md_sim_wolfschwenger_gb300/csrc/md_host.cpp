@@ -391,16 +391,23 @@ double fun_rez_error(const md_config& c, const EwaldModel& m, double alpha, doub
 // bisection to full precision.  kc: the root on the decaying side of
 // FunRezError after its maximum (interaction.cpp:219-249), kc >= 2.
 bool ewald_for_rc(const md_config& c, const EwaldModel& m, double rc, double* alpha, double* kc_raw) {
-  double lo = 0, hi = 0, prev = 1e-4 / rc;
-  if (!(fun_real_error(c, m, prev, rc) > 0)) return false;
-  for (int i = 1; i <= 4000; i++) {
-    double a = 1e-4 / rc * std::pow(10.0, 6.0 * i / 4000.0);
-    if (fun_real_error(c, m, a, rc) < 0) {
-      lo = prev;
-      hi = a;
-      break;
+  // first sign change on the grid a_i = 1e-4 / rc 10^(6 i / 4000): located on
+  // every 10th grid point, then among the 10 points before it (the error
+  // function is smooth on the 3.5 % span of ten grid points)
+  auto grid = [&](int i) { return 1e-4 / rc * std::pow(10.0, 6.0 * i / 4000.0); };
+  double lo = 0, hi = 0;
+  if (!(fun_real_error(c, m, grid(0), rc) > 0)) return false;
+  for (int j = 10; j <= 4000 + 9 && hi == 0; j += 10) {
+    const int jj = std::min(j, 4000);
+    if (fun_real_error(c, m, grid(jj), rc) < 0) {
+      for (int i = jj - 9 > 1 ? jj - 9 : 1; i <= jj; i++)
+        if (fun_real_error(c, m, grid(i), rc) < 0) {
+          lo = grid(i - 1);
+          hi = grid(i);
+          break;
+        }
     }
-    prev = a;
+    if (jj == 4000) break;
   }
   if (hi == 0) return false;
   for (int it = 0; it < 200 && hi - lo > 1e-15 * hi; it++) {

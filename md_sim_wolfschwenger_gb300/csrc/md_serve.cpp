@@ -8,7 +8,9 @@
 //   1. while the current packed round runs on the GPU, admit arrived
 //      requests in arrival order: build the system on the host, create its
 //      context, upload the state, choose the Ewald parameters -- as long as
-//      the admitted systems stay inside the memory budget and batch slots;
+//      the admitted systems stay inside the memory budget and batch slots.
+//      The host-side systems of the next arrived requests (sizes, placement,
+//      Ewald parameters) are prepared ahead on worker threads;
 //   2. wait for the round; systems that have run all their steps are read
 //      back (final m_z, state checksum), leave the batch and free memory;
 //   3. the newly admitted systems join the batch (it re-packs its launches)
@@ -18,8 +20,11 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <future>
+#include <map>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/md_gb300.h"
@@ -183,6 +188,18 @@ int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, co
   auto now = [&] { return std::chrono::duration<double>(Clock::now() - t0).count(); };
   std::vector<Live> live, staged;
   HostSys pend;  // the next request's host system, kept while it waits for memory
+  // host systems prepared ahead on worker threads, by request index
+  using Prep = std::pair<int, HostSys>;
+  std::map<int64_t, std::future<Prep>> ahead;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nahead = std::min<size_t>(16, std::max<size_t>(1, hw / 2));
+  auto prepare_async = [&](int64_t qi) {
+    ahead.emplace(qi, std::async(std::launch::async, [base, reqs, qi]() {
+      Prep r;
+      r.first = prepare_host(*base, reqs[qi], qi, &r.second);
+      return r;
+    }));
+  };
   size_t next = 0;
   int64_t completed = 0;
   double used = 0;
@@ -206,6 +223,11 @@ int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, co
   while (completed < nreq && !fatal) {
     // 1. admission (overlaps the round in flight)
     const double ta = now();
+    for (size_t k = next; k < order.size() && k < next + nahead; k++) {
+      const int64_t qi = order[k];
+      if (opts->realtime && reqs[qi].arrival > now()) break;
+      if ((int64_t)qi != pend.req && !ahead.count(qi)) prepare_async(qi);
+    }
     while (next < order.size() && (int64_t)(live.size() + staged.size()) < opts->max_systems) {
       const int64_t qi = order[next];
       const md_request& q = reqs[qi];
@@ -220,7 +242,16 @@ int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, co
       };
       if (pend.req != qi) {
         pend = HostSys();
-        const int hs = prepare_host(*base, q, qi, &pend);
+        int hs;
+        auto it = ahead.find(qi);
+        if (it != ahead.end()) {
+          Prep r = it->second.get();
+          ahead.erase(it);
+          hs = r.first;
+          pend = std::move(r.second);
+        } else {
+          hs = prepare_host(*base, q, qi, &pend);
+        }
         if (hs) {
           reject(hs);
           continue;
