@@ -415,11 +415,16 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
     const int* lst = p.nbr + p.nbr_off[k];
     const int cnt = p.nbr_off[k + 1] - p.nbr_off[k];
     if constexpr (F32) {
-      // two batches of 32 entries per iteration: all gathers issued first
+      // two batches of 32 entries per iteration, all gathers issued first;
+      // the list indices of the next iteration are loaded one ahead, so a
+      // gather waits on one memory round trip instead of two
+      int ja_n = lane < cnt ? lst[lane] : k, jb_n = 32 + lane < cnt ? lst[32 + lane] : k;
       for (int t0 = 0; t0 < cnt; t0 += 64) {
         const int ta = t0 + lane, tb = t0 + 32 + lane;
         const bool va = ta < cnt, vb = tb < cnt;
-        const int ja = va ? lst[ta] : k, jb = vb ? lst[tb] : k;
+        const int ja = ja_n, jb = jb_n;
+        ja_n = ta + 64 < cnt ? lst[ta + 64] : k;
+        jb_n = tb + 64 < cnt ? lst[tb + 64] : k;
         const int4 sa = p.s.xi[ja], sb = p.s.xi[jb];
         const T4 ma = ((const T4*)p.s.mu)[ja], mb = ((const T4*)p.s.mu)[jb];
         if (va) eval_loaded(sa, ma);
