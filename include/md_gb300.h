@@ -394,6 +394,18 @@ typedef struct md_serve_stats {
 int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, const md_serve_opts* opts,
                  md_request_result* results, md_serve_stats* stats);
 
+/* ------------------------------------------------------ post-processing */
+/* Radial distribution function of the current positions, as the reference's
+ * analysis script computes it per frame (mFiles/radial_dist_fun.m:19-66):
+ * pairs i < j at their minimum-image distance, distances below 2 r_mag0
+ * clamped to 2 r_mag0 (the script uses rMag of the first particle), pairs
+ * closer than `range` (m; the script: 8 r_mag0) counted in `bins` equal bins
+ * (<= 8192), g[k] = count[k] L^3 / (2 pi dr^3 N^2) / (k + 1/2)^2.  With
+ * include_last = 0 the pairs with the last particle are left out, as the
+ * script's loop bound does; 1 counts all pairs.  counts (may be NULL) gets
+ * the integer pair counts. */
+int md_rdf(md_ctx* ctx, int64_t bins, double range, double r_mag0, int include_last, double* g, uint64_t* counts);
+
 /* ------------------------------------------------------ output files */
 /* The reference's text outputs, written from host arrays with the bytes its
  * Eigen stream output produces (6 significant digits, columns aligned to the

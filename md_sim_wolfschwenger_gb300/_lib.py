@@ -151,6 +151,7 @@ def lib():
         "md_write_coords_txt": (C.c_int, [C.c_char_p, I64, P, P, P, C.c_double]),
         "md_write_data_txt": (C.c_int, [C.c_char_p, C.POINTER(MdConfig), I64, P, P, C.c_double]),
         "md_export_records_txt": (C.c_int, [C.c_char_p, P, I64, C.c_double, I64]),
+        "md_rdf": (C.c_int, [V, I64, C.c_double, C.c_double, C.c_int, P, C.POINTER(C.c_uint64)]),
         "md_noalloc_scratch_bytes": (C.c_size_t, []),
         "md_structure_factor_noalloc": (C.c_int, [V, V, I64, C.c_double, I64, C.c_double, V, PI64, V]),
     }

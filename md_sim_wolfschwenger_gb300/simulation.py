@@ -260,6 +260,17 @@ class Simulation:
         self._ck(self.L.md_debug_structure_factor(self.h, C.byref(nk), _P(out)))
         return out
 
+    def rdf(self, bins=500, range_mag=8.0, r_mag0=None, include_last=False):
+        """g(r) of the current frame on the device (mFiles/radial_dist_fun.m):
+        returns (x in units of 2 r_mag0 at the bin centres, g, counts)."""
+        r0 = float(self._rMag[0] if r_mag0 is None else r_mag0)
+        g = np.empty(int(bins))
+        cnt = np.empty(int(bins), dtype=np.uint64)
+        self._ck(self.L.md_rdf(self.h, int(bins), range_mag * r0, r0, int(bool(include_last)), _P(g),
+                               cnt.ctypes.data_as(C.POINTER(C.c_uint64))))
+        x = (np.arange(bins) + 0.5) * (range_mag * r0 / bins) / (2 * r0)
+        return x, g, cnt
+
     def debug_real_part(self):
         """Real-space (B, F) alone of the last CompInteractions, (3, N) SI."""
         B, F = np.empty((3, self.n)), np.empty((3, self.n))
