@@ -454,12 +454,17 @@ void predicted_errors(const md_config& c, const EwaldModel& m, double alpha, dou
 // Instruction-count model of one step (two field evaluations): per neighbour
 // ~75 for the candidate tests and ~155 for the pair maths; per (k, particle)
 // ~44 (structure factor twice, full and field-only scatter).
+// Relative cost of one step for cutoff rc (box units) and kc: per particle,
+// the ordered pairs within rc (field + force and field-only passes over the
+// Verlet list, which is rebuilt only every many steps) and the k vectors of
+// the half space (structure factor twice, scatter twice).  The weights are
+// the measured per-unit times on GB300 (9.5 ps per ordered pair, 2.5 ps per
+// (k, particle) at N = 32768).
 double model_cost(double rc_box, int64_t kc, int64_t n) {
   const double pi = 3.141592653589793;
   const double nr = (double)n * 4.0 / 3.0 * pi * rc_box * rc_box * rc_box;
   const double nk = 2.0 * pi / 3.0 * (double)kc * kc * kc;
-  const double cand = rc_box > 0.4 ? 30.0 * n : 75.0 * 2.5 * nr;
-  return (double)n * (cand + 155.0 * nr + 44.0 * nk);
+  return (double)n * (9.5 * nr + 2.5 * nk);
 }
 
 double choose_rc(const md_config& c, const EwaldModel& m, int64_t n, double* alpha_out, int64_t* kc_out) {
