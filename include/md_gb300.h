@@ -150,6 +150,18 @@ int md_set_box(md_ctx* ctx, double lBox);
  * positions like InitSimulation (simulation.cpp:108-109) when reset != 0. */
 int md_state_upload(md_ctx* ctx, const double* pos, const double* mm, const double* ea, int reset);
 int md_state_download(md_ctx* ctx, double* pos, double* mm, double* ea);
+/* Checkpoint / resume (the reference's READ_FROM_FILE path reads columns
+ * its own writer does not produce, src/simulation.cpp:357-382 vs
+ * src/postprocessing.cpp:84-97; this one restores everything): a binary file
+ * with the radii, box, Ewald parameters, noise mode and seed, time and step
+ * counter, and the positions, moments, easy axes, unwrapped positions and MSD
+ * reference positions.  Loading needs a context of the same particle count
+ * and precision (created with the same configuration); a run continued from
+ * the file equals the saving run continued, step for step (both rebuild
+ * their cell order and neighbour list at the next step).  Per-step records
+ * are not part of the file. */
+int md_checkpoint_save(md_ctx* ctx, const char* path);
+int md_checkpoint_load(md_ctx* ctx, const char* path);
 /* Integration time and step counter (RunSimulation's tInt / steps). */
 int md_set_time(md_ctx* ctx, double t, int64_t step);
 int md_get_time(const md_ctx* ctx, double* t, int64_t* step);

@@ -107,6 +107,8 @@ def lib():
         "md_state_upload": (C.c_int, [V, P, P, P, C.c_int]),
         "md_state_download": (C.c_int, [V, P, P, P]),
         "md_set_time": (C.c_int, [V, C.c_double, I64]),
+        "md_checkpoint_save": (C.c_int, [V, C.c_char_p]),
+        "md_checkpoint_load": (C.c_int, [V, C.c_char_p]),
         "md_get_time": (C.c_int, [V, P, PI64]),
         "md_ewald_params": (C.c_int, [V, C.c_double, P, P, PI64, P, P]),
         "md_set_ewald": (C.c_int, [V, C.c_double, C.c_double, I64]),

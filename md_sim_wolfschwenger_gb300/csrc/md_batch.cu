@@ -368,6 +368,7 @@ int md_batch_remove(md_batch* b, int64_t id) {
 }
 
 int md_batch_launch(md_batch* b, int64_t max_steps, int64_t* steps) {
+  NvtxRange nv("md_batch_launch");
   if (!b || max_steps < 0) return set_err(nullptr, MD_ERR_INVALID, "bad arguments");
   if (b->running) return set_err(nullptr, MD_ERR_INVALID, "batch round in flight (md_batch_wait first)");
   int64_t k = max_steps;

@@ -656,6 +656,7 @@ int md_state_download(md_ctx* c, double* pos, double* mm, double* ea) {
 
 int md_set_time(md_ctx* c, double t, int64_t step) {
   if (!c) return set_err(c, MD_ERR_INVALID, "null context");
+  CK(c, cudaStreamSynchronize(c->stream));
   DevScalars h;
   CK(c, cudaMemcpy(&h, c->sc, sizeof h, cudaMemcpyDeviceToHost));
   h.time = t;
@@ -832,6 +833,7 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
 }
 
 int md_compute_interactions(md_ctx* c, double* B, double* F, double* P3) {
+  NvtxRange nv("md_compute_interactions");
   int st = check_ready(c, true);
   if (st) return st;
   if ((st = force_rebuild(c))) return st;
@@ -857,6 +859,7 @@ int md_compute_interactions(md_ctx* c, double* B, double* F, double* P3) {
 }
 
 int md_compute_field(md_ctx* c, const double* mm, double* B) {
+  NvtxRange nv("md_compute_field");
   int st = check_ready(c, true);
   if (st) return st;
   if (!mm) return set_err(c, MD_ERR_INVALID, "null moment directions");
@@ -916,6 +919,7 @@ int prepare_dt(md_ctx* c, double dt) {
 extern "C" {
 
 int md_step(md_ctx* c, int64_t nsteps, double dt, const double* xi) {
+  NvtxRange nv("md_step");
   int st = check_ready(c, true);
   if (st) return st;
   if (nsteps < 0 || !(dt > 0)) return set_err(c, MD_ERR_INVALID, "bad nsteps or dt");
@@ -987,6 +991,7 @@ const Tableau& tableau(int solver) {
 
 int md_step_adaptive(md_ctx* c, int64_t max_steps, double t_end, double* dt_io, const double* xi,
                      int64_t* steps_done) {
+  NvtxRange nv("md_step_adaptive");
   int st = check_ready(c, true);
   if (st) return st;
   if (steps_done) *steps_done = 0;
@@ -1087,6 +1092,73 @@ int md_step_adaptive(md_ctx* c, int64_t max_steps, double t_end, double* dt_io, 
   c->have_geometry = true;
   if (steps_done) *steps_done = done;
   return read_err_word(c);
+}
+
+// ------------------------------------------------------------ checkpoints
+// Binary snapshot of a context: "MDCKPT01", then int64 n, precision, kc,
+// noise mode, seed, step; double box length, alpha, rc, time; rMag[n],
+// rHydr[n]; pos, mm, ea, truePos, posRef as N x 3 column-major FP64.
+
+namespace {
+const char kCkptMagic[8] = {'M', 'D', 'C', 'K', 'P', 'T', '0', '1'};
+}
+
+int md_checkpoint_save(md_ctx* c, const char* path) {
+  int st = check_ready(c, true);
+  if (st) return st;
+  if (!path) return set_err(c, MD_ERR_INVALID, "null path");
+  CK(c, cudaStreamSynchronize(c->stream));
+  const size_t n = (size_t)c->n, B = 24 * n;
+  std::vector<double> arr(15 * n);
+  double* dev[5] = {c->pos, c->mm, c->ea, c->truePos, c->posRef};
+  for (int q = 0; q < 5; q++) CK(c, cudaMemcpy(arr.data() + 3 * n * q, dev[q], B, cudaMemcpyDeviceToHost));
+  double t = 0;
+  int64_t step = 0;
+  if ((st = md_get_time(c, &t, &step))) return st;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return set_err(c, MD_ERR_INVALID, "cannot open %s for writing", path);
+  const int64_t hi[6] = {c->n, c->prec, c->kc, c->noise, (int64_t)c->seed, step};
+  const double hd[4] = {c->L, c->alpha, c->rc, t};
+  bool ok = std::fwrite(kCkptMagic, 1, 8, f) == 8 && std::fwrite(hi, 8, 6, f) == 6 && std::fwrite(hd, 8, 4, f) == 4 &&
+            std::fwrite(c->props.rMag.data(), 8, n, f) == n && std::fwrite(c->props.rHydr.data(), 8, n, f) == n &&
+            std::fwrite(arr.data(), 8, 15 * n, f) == 15 * n;
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) return set_err(c, MD_ERR_INVALID, "write to %s failed", path);
+  // the saving run rebuilds its cell order and list at the next step, as a
+  // run restored from this file does, so both continue identically
+  return force_rebuild(c);
+}
+
+int md_checkpoint_load(md_ctx* c, const char* path) {
+  if (!c || !path) return set_err(c, MD_ERR_INVALID, "null argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_err(c, MD_ERR_INVALID, "cannot open %s", path);
+  char magic[8];
+  int64_t hi[6];
+  double hd[4];
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kCkptMagic, 8) == 0 &&
+            std::fread(hi, 8, 6, f) == 6 && std::fread(hd, 8, 4, f) == 4;
+  if (!ok || hi[0] != c->n || hi[1] != c->prec) {
+    std::fclose(f);
+    return set_err(c, MD_ERR_INVALID, "%s is not a checkpoint of %lld particles in this precision", path,
+                   (long long)c->n);
+  }
+  const size_t n = (size_t)c->n, B = 24 * n;
+  std::vector<double> rMag(n), rHydr(n), arr(15 * n);
+  ok = std::fread(rMag.data(), 8, n, f) == n && std::fread(rHydr.data(), 8, n, f) == n &&
+       std::fread(arr.data(), 8, 15 * n, f) == 15 * n;
+  std::fclose(f);
+  if (!ok) return set_err(c, MD_ERR_INVALID, "%s is truncated", path);
+  int st;
+  if ((st = md_set_particles(c, rMag.data(), rHydr.data()))) return st;
+  if ((st = md_set_box(c, hd[0]))) return st;
+  if ((st = md_set_ewald(c, hd[1], hd[2], hi[2]))) return st;
+  if ((st = md_state_upload(c, arr.data(), arr.data() + 3 * n, arr.data() + 6 * n, 0))) return st;
+  CK(c, cudaMemcpy(c->truePos, arr.data() + 9 * n, B, cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->posRef, arr.data() + 12 * n, B, cudaMemcpyHostToDevice));
+  if ((st = md_set_noise(c, (int)hi[3], (uint64_t)hi[4]))) return st;
+  if ((st = md_set_time(c, hd[3], hi[5]))) return st;
+  return force_rebuild(c);
 }
 
 int md_num_records(const md_ctx* cc, int64_t* count) {

@@ -3,6 +3,7 @@
 // helpers shared by md_ctx.cu (one system) and md_batch.cu (packed systems).
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <string>
@@ -31,6 +32,15 @@ struct DevScalars {
 }  // namespace md
 
 using namespace md;
+
+// Named ranges for timeline tools (NVTX v3, header only; no-ops unless a
+// tool is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 struct md_ctx {
   md_config cfg{};

@@ -47,12 +47,15 @@ struct Opts {
   int64_t chunk = 100000;    // steps between record read-backs
   bool quiet = false;
   bool fixed_dt = false;     // every step with deltaTinit (Heun)
+  std::string resume;        // checkpoint to continue from (md_checkpoint_load)
+  std::string checkpoint;    // checkpoint written at the end (md_checkpoint_save)
 };
 
 void usage() {
   std::printf(
       "usage: md_run [configuration.ini] [--out DIR] [--precision mixed|fp64] [--autotune K]\n"
-      "              [--device D] [--chunk STEPS] [--fixed-dt] [--quiet]\n"
+      "              [--device D] [--chunk STEPS] [--fixed-dt] [--resume FILE] [--checkpoint FILE]\n"
+      "              [--quiet]\n"
       "Runs MD_Sim_Wolfschwenger's simulation (InitSimulation + RunSimulation) with the time step on\n"
       "the GPU; the configuration defaults to ../configuration.ini like the reference.\n");
 }
@@ -140,6 +143,10 @@ int main(int argc, char** argv) {
       o.quiet = true;
     } else if (a == "--fixed-dt") {
       o.fixed_dt = true;
+    } else if (a == "--resume") {
+      o.resume = next("--resume");
+    } else if (a == "--checkpoint") {
+      o.checkpoint = next("--checkpoint");
     } else if (!a.empty() && a[0] == '-') {
       std::fprintf(stderr, "md_run: unknown option %s\n", a.c_str());
       usage();
@@ -193,6 +200,17 @@ int main(int argc, char** argv) {
               "%.3g (relative to contact)\n",
               alpha, rc, rc / lBox, (long long)kc, errF, errT);
   CALL(ctx, md_set_noise(ctx, (int)cfg.noise, (uint64_t)cfg.seed));
+  double t_start = 0;  // time of the first step (later than 0 when resuming)
+  if (!o.resume.empty()) {
+    // continue a run: radii, box, Ewald parameters, state, time and noise
+    // counter from the checkpoint; the loop below runs on until tEnd
+    CALL(ctx, md_checkpoint_load(ctx, o.resume.c_str()));
+    CALL(ctx, md_get_box(ctx, &lBox));
+    int64_t s0 = 0;
+    CALL(ctx, md_get_time(ctx, &t_start, &s0));
+    std::printf("resumed from %s at t = %g s (step %lld), with its Ewald parameters\n", o.resume.c_str(), t_start,
+                (long long)s0);
+  }
   CALL(nullptr, md_write_data_txt(path_in(o, "data.txt").c_str(), &cfg, n, rMag.data(), rHydr.data(), lBox));
 
   // ------------------------------------------------------ RunSimulation
@@ -216,7 +234,9 @@ int main(int argc, char** argv) {
       std::printf("actual time: %gs\nsimulation progress: %g%%\n", label, (double)count / cfg.npCoords * 100.0);
   };
   int64_t steps = 0;
-  double tInt = 0;
+  double tInt = t_start;
+  // frames already written before a resumed run's start
+  const int64_t count0 = t_start > 0 ? (int64_t)std::floor(t_start / tEnd * cfg.npCoords) + 1 : 0;
   if (o.fixed_dt) {
     // time points and frames with the reference's own double arithmetic
     const double dt = cfg.deltaTinit;
@@ -226,7 +246,7 @@ int main(int argc, char** argv) {
     };
     std::vector<Frame> frames;
     {
-      int64_t count = 0;
+      int64_t count = count0;
       while (tInt <= tEnd) {
         if (std::floor(tInt / tEnd * cfg.npCoords) == (double)count) {
           frames.push_back({steps, tInt});
@@ -255,7 +275,7 @@ int main(int argc, char** argv) {
     // adaptive: one accepted step at a time (the next time point is known
     // only after the step control has run)
     double dt = cfg.deltaTinit;
-    int64_t count = 0;
+    int64_t count = count0;
     while (tInt <= tEnd) {
       const bool frame = std::floor(tInt / tEnd * cfg.npCoords) == (double)count;
       int64_t k = 0;
@@ -279,6 +299,7 @@ int main(int argc, char** argv) {
   if (tDev != tInt || sDev != steps)
     std::printf("note: device time %.17g after %lld steps, host %.17g after %lld\n", tDev, (long long)sDev, tInt,
                 (long long)steps);
+  if (!o.checkpoint.empty()) CALL(ctx, md_checkpoint_save(ctx, o.checkpoint.c_str()));
   md_ctx_destroy(ctx);
   std::printf("simulation ended successfully\n");
   return 0;

@@ -30,6 +30,7 @@
 #include "../../include/md_gb300.h"
 #include "md_err.h"
 #include "md_host.h"
+#include <nvtx3/nvToolsExt.h>
 
 namespace {
 
@@ -165,6 +166,10 @@ int md_init_system(const md_config* cfg, int64_t n, uint64_t seed, double* rMag,
 
 int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, const md_serve_opts* opts,
                  md_request_result* results, md_serve_stats* stats) {
+  nvtxRangePushA("md_serve_run");
+  struct Pop {
+    ~Pop() { nvtxRangePop(); }
+  } pop;
   if (!base || (!reqs && nreq) || nreq < 0 || !opts || (!results && nreq))
     return set_err(nullptr, MD_ERR_INVALID, "null argument");
   if (opts->max_systems < 1 || opts->round_steps < 1 || !(opts->hbm_budget > 0))
@@ -222,6 +227,7 @@ int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, co
 
   while (completed < nreq && !fatal) {
     // 1. admission (overlaps the round in flight)
+    nvtxRangePushA("admission");
     const double ta = now();
     for (size_t k = next; k < order.size() && k < next + nahead; k++) {
       const int64_t qi = order[k];
@@ -281,6 +287,7 @@ int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, co
       next++;
     }
     S.admit_ms += 1e3 * (now() - ta);
+    nvtxRangePop();
     // 2. the round in flight
     if (in_flight) {
       const int ws = md_batch_wait(b);

@@ -11,6 +11,7 @@ arrays (x block, y block, z block).
 from __future__ import annotations
 
 import ctypes as C
+import os
 import re
 
 import numpy as np
@@ -155,6 +156,14 @@ class Simulation:
         a = out if out is not None else [np.empty((3, self.n)) for _ in range(3)]
         self._ck(self.L.md_state_download(self.h, *(_P(x) for x in a)))
         return tuple(a)
+
+    def checkpoint_save(self, path):
+        """Binary snapshot of the state (see md_checkpoint_save)."""
+        self._ck(self.L.md_checkpoint_save(self.h, os.fsencode(str(path))))
+
+    def checkpoint_load(self, path):
+        """Restores a snapshot into this context (same N and precision)."""
+        self._ck(self.L.md_checkpoint_load(self.h, os.fsencode(str(path))))
 
     def set_time(self, t, step=0):
         self._ck(self.L.md_set_time(self.h, t, step))

@@ -136,3 +136,43 @@ def test_adaptive_outputs_equal_python_api_run(tmp_path, solver):
     for nm in ("dtMean.txt", "Pxy.txt", "MSDx.txt", "MSDz.txt", "mz.txt", "t.txt"):
         assert (run / nm).read_bytes() == (ref / nm).read_bytes(), nm
     assert np.all(np.diff(rec[:, 0]) > 0)
+
+
+def _ckpt_state(path, n):
+    raw = np.fromfile(path, dtype=np.uint8)
+    assert bytes(raw[:8]) == b"MDCKPT01"
+    vals = raw[8 + 6 * 8 + 4 * 8:].view(np.float64)
+    return vals[2 * n:2 * n + 9 * n].reshape(3, 3, n), raw[8:8 + 48].view(np.int64)
+
+
+@pytest.mark.gpu
+def test_resume_from_checkpoint_continues_the_run(tmp_path):
+    # no applied field: the field program (on while t < tMag) would differ
+    # between the two configurations, which end at different times
+    ini = ref_io.ini_dict(npDim=4, tMag=6e-11, tRelax=0.0, deltaTinit=1e-12, magFluxDens=0.0, seed=3,
+                          volFrac=0.05)
+    ini["output_settings"]["npCoords"] = 4
+    full = tmp_path / "full"
+    full.mkdir()
+    ref_io.write_ini(full / "configuration.ini", ini)
+    (full / "run").mkdir()
+    r = _run(["--precision", "fp64", "--quiet", "--fixed-dt", "--checkpoint", str(full / "end.ckpt")], full / "run")
+    assert r.returncode == 0, r.stderr
+    half = tmp_path / "half"
+    half.mkdir()
+    ini_h = ref_io.ini_dict(npDim=4, tMag=3e-11, tRelax=0.0, deltaTinit=1e-12, magFluxDens=0.0, seed=3,
+                            volFrac=0.05)
+    ini_h["output_settings"]["npCoords"] = 4
+    ref_io.write_ini(half / "configuration.ini", ini_h)
+    (half / "run").mkdir()
+    r = _run(["--precision", "fp64", "--quiet", "--fixed-dt", "--checkpoint", str(half / "mid.ckpt")], half / "run")
+    assert r.returncode == 0, r.stderr
+    r = _run([str(full / "configuration.ini"), "--precision", "fp64", "--quiet", "--fixed-dt", "--resume",
+              str(half / "mid.ckpt"), "--checkpoint", str(half / "end.ckpt")], half / "run")
+    assert r.returncode == 0, r.stderr
+    assert "resumed from" in r.stdout
+    a, ha = _ckpt_state(full / "end.ckpt", 64)
+    b, hb = _ckpt_state(half / "end.ckpt", 64)
+    assert ha[5] == hb[5]  # same number of steps
+    np.testing.assert_allclose(b[1:], a[1:], rtol=0, atol=1e-11)          # moments, easy axes
+    np.testing.assert_allclose(b[0], a[0], rtol=0, atol=1e-12 * np.abs(a[0]).max())
