@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
 
 # Section -> key -> value, in the order of src/configuration.ini.  Values are
-# the BASELINE "config 1" physics (20 nm magnetite cores, 5 nm shell, 10 mT);
+# the monodisperse physics (20 nm magnetite cores, 5 nm shell, 10 mT);
 # the physical constants are the reference's own (src/configuration.ini:69-79).
 DEFAULT_INI = {
     "initial_configuration": {"INIT_CONFIG_ROT": 2, "INIT_CONFIG_TRANS": 1, "READ_FROM_FILE": "false"},

@@ -24,7 +24,7 @@ import oracle as O  # noqa: E402
 import ref_io  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-VIS = 1e-3  # water, the BASELINE viscosity (the reference's Vogel formula gives 8.5e-4 at 300 K)
+VIS = 1e-3  # water at room temperature, 1 mPa s (the reference's Vogel formula gives 8.5e-4 at 300 K)
 
 
 def case(name, n, nsteps, rc_frac, seed, noise=True, coating=False, lognormal=False, overlap=False, dt=1e-12,

@@ -94,7 +94,8 @@ def torque(mm, B, magMom):
 
 
 def random_system(n, seed, rc_frac=0.3, phi=0.05, lognormal=False, noise=False, B0=0.01, min_gap=0.0):
-    """Seeded system with the BASELINE physics (config 1 unless overridden)."""
+    """Seeded system: monodisperse 20 nm magnetite cores with a 5 nm shell in a
+    10 mT field unless overridden."""
     ini = ref_io.ini_dict(volFrac=phi, magFluxDens=B0, ENABLE_THERM_FIELD="true" if noise else "false",
                           ENABLE_THERM_TORQUE="true" if noise else "false",
                           ENABLE_THERM_FORCE="true" if noise else "false", seed=seed)

@@ -186,7 +186,7 @@ def test_noise_off_trajectory_vs_oracle(prec):
 
 
 def test_momentum_and_translation_invariance_full_size():
-    """Size-independent properties at the BASELINE single-instance size
+    """Size-independent properties at the largest single-system size
     (N = 32768, phi = 0.10): the interaction forces sum to zero, a rigid
     shift of all particles leaves B and F unchanged, and the mixed path
     agrees with the FP64 path within the 1e-5 contact-normalised budget."""
@@ -210,7 +210,7 @@ def test_momentum_and_translation_invariance_full_size():
 
 
 def random_system_fast(n, seed, phi, B0):
-    """Jittered lattice (no overlaps) for large N; BASELINE config-2 physics
+    """Jittered lattice (no overlaps) for large N; polydisperse physics
     (log-normal cores, median 20 nm diameter, sigma 0.2, 5 nm shell)."""
     import ref_io
     ini = ref_io.ini_dict(volFrac=phi, magFluxDens=B0, ENABLE_THERM_FIELD="false", ENABLE_THERM_TORQUE="false",
