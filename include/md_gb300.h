@@ -56,6 +56,13 @@ enum {
   MD_NOISE_PHILOX = 2    /* counter-based Philox4x32-10 on the device        */
 };
 
+/* Reciprocal-space engine of the mixed path (md_set_kspace_engine). */
+enum {
+  MD_KSPACE_AUTO = 0, /* tensor cores when kc allows, else the FP32 kernels   */
+  MD_KSPACE_SIMT = 1, /* FP32 CUDA-core kernels (row segments, phase recurrences) */
+  MD_KSPACE_TC = 2    /* tensor cores (3-pass TF32 matrix products over k rows) */
+};
+
 /* External field program (DefExtField, src/simulation.cpp:546-556). */
 enum {
   MD_FIELD_STEP = 0,  /* B = magFluxDens e_z for t < tMag, else 0 (reference) */
@@ -184,6 +191,15 @@ int md_ewald_params_host(const md_config* cfg, int64_t n, const double* rMag, co
 /* Sets the Ewald parameters (Params_S alpha, rCutLR, nCutLR) and derives
  * the constants of InitEwaldConst (src/interaction.cpp:353-374). */
 int md_set_ewald(md_ctx* ctx, double alpha, double rc, int64_t kc);
+/* Chooses how the mixed path evaluates CompDipInteractEwaldF /
+ * CompDipFieldEwaldF (src/interaction.cpp:429-514, 588-672): MD_KSPACE_*.
+ * Both engines compute the same sums.  MD_KSPACE_TC returns
+ * MD_ERR_UNSUPPORTED on the FP64 path or when kc is too large for the
+ * tensor-core kernels' shared memory (kc <= 25).  Applies to the current
+ * and later Ewald parameters. */
+int md_set_kspace_engine(md_ctx* ctx, int engine);
+/* *tensor_cores = 1 when the current Ewald parameters use the tensor cores. */
+int md_kspace_engine_active(const md_ctx* ctx, int* tensor_cores);
 /* Times candidate cut-offs on the device and sets the fastest that meets
  * the error model; the GPU counterpart of the timing sweep of
  * CompEwaldParams (src/interaction.cpp:185-296). */

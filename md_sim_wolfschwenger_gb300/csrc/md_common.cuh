@@ -137,6 +137,22 @@ struct KParams {
   SortedView s;
   void* B;   // [3][n] T sorted
   void* F;   // [3][n] T sorted (FULL only)
+  // Tensor-core engine (mixed path): k rows r = (ny, nz), each with nx in
+  // [-kc, kc] (column q = nx + kc; k's outside the sphere or the half space
+  // have kmap -1 and a zero operand).
+  int tc_rows;           // R
+  int tc_mt;             // structure-factor M tiles of 64 rows (x U, V)
+  int tc_ns;             // structure-factor N: 2 (2kc + 1) rounded up to 16
+  int tc_kp;             // scatter K: 2 (2kc + 1) rounded up to 8
+  int tc_rt;             // rows per 64-column scatter tile: 10 (field + force) or 16
+  int tc_nt;             // scatter tiles: ceil(R / tc_rt)
+  int tc_nst;            // scatter pipeline stages (2 or 3)
+  int tc_chunk, tc_nchunk;  // structure-factor particle chunks (multiple of 16)
+  const int2* tc_row;    // [R] (ny, nz)
+  const int* tc_kmap;    // [R][2kc + 1] sorted k index, or -1
+  float* tc_part;        // [nchunk][mt][ns][128] FP32 chunk partials (column-major tiles)
+  float* tc_w;           // scatter operand image [nt][hi, lo][64][kp] (this evaluation's layout)
+  int* err;              // device error word (kErrTcWait on a wait that gave up)
 };
 
 // ----------------------------------------------------- integrator
@@ -278,6 +294,6 @@ __device__ __forceinline__ void cmul(T ar, T ai, T br, T bi, T& cr, T& ci) {
 }
 
 // Device error word bits.
-enum : int { kErrNonFinite = 1, kErrQueue = 2 };
+enum : int { kErrNonFinite = 1, kErrQueue = 2, kErrTcWait = 4 };
 
 }  // namespace md

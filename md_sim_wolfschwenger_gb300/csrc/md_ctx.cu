@@ -213,6 +213,20 @@ KParams k_params(md_ctx* c, void* B, void* F) {
   p.s = sorted_view(c);
   p.B = B;
   p.F = F;
+  p.tc_rows = c->tc_rows;
+  p.tc_mt = c->tcs.mt;
+  p.tc_ns = c->tcs.ns;
+  p.tc_kp = c->tcs.kp;
+  p.tc_rt = F ? c->tcs.rt_full : c->tcs.rt_field;
+  p.tc_nt = F ? c->tcs.nt_full : c->tcs.nt_field;
+  p.tc_nst = c->tcs.nst;
+  p.tc_chunk = c->tcs.chunk;
+  p.tc_nchunk = c->tcs.nchunk;
+  p.tc_row = c->tc_row;
+  p.tc_kmap = c->tc_kmap;
+  p.tc_part = c->tc_part;
+  p.tc_w = F ? c->tc_wfull : c->tc_wfield;
+  p.err = &c->sc->err;
   return p;
 }
 
@@ -403,11 +417,65 @@ int read_err_word(md_ctx* c) {
   if (e) {
     CK(c, cudaMemsetAsync(&c->sc->err, 0, sizeof(int), c->stream));
     if (e & kErrNonFinite) return set_err(c, MD_ERR_NONFINITE, "non-finite position or orientation after the step");
+    if (e & kErrTcWait) return set_err(c, MD_ERR_CUDA, "tensor-core k space: a pipeline wait gave up");
   }
   return check_overflow(c);
 }
 
 // ============================================================== C ABI
+
+// Tensor-core k space: the k rows (ny, nz) of the half-space k list, ordered
+// by nz then ny, the k index of each (row, nx), and the buffers of the
+// launches (md_ktc.cu).  Off (tc_rows = 0) on the FP64 path, when the
+// engine is MD_KSPACE_SIMT, or when kc is beyond the kernels' shared memory.
+static int setup_tc(md_ctx* c) {
+  c->tc_rows = 0;
+  if (fp64(c) || c->kengine == MD_KSPACE_SIMT || !md::kspace_tc_supported((int)c->kc)) return MD_OK;
+  const int kc = (int)c->kc, Q = 2 * kc + 1, nk = c->klist.nk;
+  std::map<std::pair<int, int>, int> rowid;  // (nz, ny) -> row
+  for (int k = 0; k < nk; k++)
+    if (c->klist.kreal[k]) rowid[{c->klist.kz[k], c->klist.ky[k]}] = 0;
+  std::vector<int2> rows;
+  for (auto& e : rowid) {
+    e.second = (int)rows.size();
+    rows.push_back(make_int2(e.first.second, e.first.first));
+  }
+  const int R = (int)rows.size();
+  if (R == 0) return MD_OK;
+  std::vector<int> kmap((size_t)R * Q, -1);
+  for (int k = 0; k < nk; k++)
+    if (c->klist.kreal[k]) kmap[(size_t)rowid[{c->klist.kz[k], c->klist.ky[k]}] * Q + c->klist.kx[k] + kc] = k;
+  int nsm = 148;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+  const md::TcShape t = md::kspace_tc_shape(kc, (int)c->n, R, nsm);
+  void* old[] = {c->tc_row, c->tc_kmap, c->tc_part, c->tc_wfull, c->tc_wfield};
+  for (void* q : old) dfree(c, q);
+  c->tc_row = nullptr;
+  c->tc_kmap = nullptr;
+  c->tc_part = nullptr;
+  c->tc_wfull = c->tc_wfield = nullptr;
+  const size_t wfull = md::kspace_tc_image_floats(kc, t.nt_full), wfield = md::kspace_tc_image_floats(kc, t.nt_field);
+  int st;
+  if ((st = dalloc(c, &c->tc_row, sizeof(int2) * (size_t)R))) return st;
+  if ((st = dalloc(c, &c->tc_kmap, sizeof(int) * kmap.size()))) return st;
+  if ((st = dalloc(c, &c->tc_part, sizeof(float) * (size_t)t.nchunk * t.mt * t.ns * 128))) return st;
+  if ((st = dalloc(c, &c->tc_wfull, sizeof(float) * wfull))) return st;
+  if ((st = dalloc(c, &c->tc_wfield, sizeof(float) * wfield))) return st;
+  if (t.nchunk > c->musum_cap) {
+    dfree(c, c->musum_part);
+    c->musum_part = nullptr;
+    if ((st = dalloc(c, &c->musum_part, 24 * (size_t)t.nchunk))) return st;
+    c->musum_cap = t.nchunk;
+  }
+  CK(c, cudaMemcpy(c->tc_row, rows.data(), sizeof(int2) * (size_t)R, cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->tc_kmap, kmap.data(), sizeof(int) * kmap.size(), cudaMemcpyHostToDevice));
+  // operand entries of k's outside the sphere or the half space stay zero
+  CK(c, cudaMemset(c->tc_wfull, 0, sizeof(float) * wfull));
+  CK(c, cudaMemset(c->tc_wfield, 0, sizeof(float) * wfield));
+  c->tcs = t;
+  c->tc_rows = R;
+  return MD_OK;
+}
 
 extern "C" {
 
@@ -818,6 +886,7 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
   // the padding entries of the scatter layout are never written: zero
   CK(c, cudaMemset(c->eS, 0, 2 * tsz(c) * nks));
   CK(c, cudaMemcpy(c->chunks, c->klist.chunks.data(), sizeof(int) * c->klist.chunks.size(), cudaMemcpyHostToDevice));
+  if (int st = setup_tc(c)) return st;
   {
     // neighbour-list capacity: uniform-density estimate + margin (grown on overflow)
     const double rlb = rc / c->L * (1.0 + c->skin_frac);
@@ -829,6 +898,25 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
   if (int st = force_rebuild(c)) return st;
   c->have_ewald = true;
   c->have_geometry = false;
+  return MD_OK;
+}
+
+int md_set_kspace_engine(md_ctx* c, int engine) {
+  if (!c || engine < MD_KSPACE_AUTO || engine > MD_KSPACE_TC) return set_err(c, MD_ERR_INVALID, "bad k-space engine");
+  if (engine == MD_KSPACE_TC && fp64(c))
+    return set_err(c, MD_ERR_UNSUPPORTED, "the tensor-core k space is part of the mixed path");
+  if (engine == MD_KSPACE_TC && c->have_ewald && !md::kspace_tc_supported((int)c->kc))
+    return set_err(c, MD_ERR_UNSUPPORTED, "kc too large for the tensor-core k space");
+  invalidate_graph(c);
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->kengine = engine;
+  if (c->have_ewald) return setup_tc(c);
+  return MD_OK;
+}
+
+int md_kspace_engine_active(const md_ctx* c, int* tensor_cores) {
+  if (!c || !tensor_cores) return MD_ERR_INVALID;
+  *tensor_cores = c->tc_rows > 0 ? 1 : 0;
   return MD_OK;
 }
 

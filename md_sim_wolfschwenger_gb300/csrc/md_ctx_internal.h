@@ -13,6 +13,7 @@
 #include "md_common.cuh"
 #include "md_err.h"
 #include "md_host.h"
+#include "md_kernels.h"
 
 namespace md {
 
@@ -111,6 +112,15 @@ struct md_ctx {
   size_t ptab_cap = 0;
   size_t ksize_cap = 0, spart_cap = 0;
   int musum_cap = 0;
+  // tensor-core k space (mixed path; md_ktc.cu): engine choice, k rows and
+  // their buffers (tc_rows = 0 while the engine is off)
+  int kengine = MD_KSPACE_AUTO;
+  int tc_rows = 0;
+  TcShape tcs{};
+  int2* tc_row = nullptr;
+  int* tc_kmap = nullptr;
+  float* tc_part = nullptr;
+  float *tc_wfull = nullptr, *tc_wfield = nullptr;
   // Verlet list (sorted indices) within rc + skin
   int *nbr = nullptr, *nbr_cnt = nullptr, *nbr_off = nullptr;
   long long nbr_cap = 0;

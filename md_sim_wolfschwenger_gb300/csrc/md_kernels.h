@@ -58,6 +58,18 @@ int launch_kspace(cudaStream_t st, const KParams& p, bool full, bool fp64, cudaE
 // scatter block (scatter_particles(kcmax)).
 int launch_kspace_packed(cudaStream_t st, const KParams* ps, const Packed& sk, const Packed& red, const Packed& sc,
                          bool full, int kcmax, int np);
+// Tensor-core k space (mixed path, md_ktc.cu): same sums, as matrix
+// products over k rows.  Shape of the launches for kc, N particles, R k rows.
+struct TcShape {
+  int ns, kp, mt, nst;          // structure-factor N, scatter K, M tiles, scatter stages
+  int nt_full, nt_field;        // scatter tiles (field + force, field only)
+  int rt_full, rt_field;        // k rows per scatter tile
+  int chunk, nchunk;            // structure-factor particle chunks
+};
+bool kspace_tc_supported(int kc);
+TcShape kspace_tc_shape(int kc, int n, int rows, int nsm);
+size_t kspace_tc_image_floats(int kc, int nt);  // scatter operand image of nt tiles
+int launch_kspace_tc(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* ev = nullptr);
 // Per-particle phase tables (once per step; positions are frozen across the
 // two Heun stages).
 int launch_phase_tables(cudaStream_t st, const KParams& p, bool fp64);

@@ -521,6 +521,7 @@ static int kspace_t(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* e
 }
 
 int launch_kspace(cudaStream_t st, const KParams& p, bool full, bool fp64, cudaEvent_t* ev) {
+  if (!fp64 && p.tc_rows > 0) return launch_kspace_tc(st, p, full, ev);
   return fp64 ? kspace_t<double>(st, p, full, ev) : kspace_t<float>(st, p, full, ev);
 }
 

@@ -186,6 +186,17 @@ class Simulation:
         self._ck(self.L.md_set_ewald(self.h, float(alpha), float(rc), int(kc)))
         self.ewald = (float(alpha), float(rc), int(kc))
 
+    def set_kspace_engine(self, engine):
+        """Reciprocal-space engine of the mixed path: "auto", "simt" or "tc"."""
+        code = {"auto": 0, "simt": 1, "tc": 2}[engine]
+        self._ck(self.L.md_set_kspace_engine(self.h, code))
+
+    def kspace_tensor_cores(self):
+        """True when the current Ewald parameters run the k space on the tensor cores."""
+        v = C.c_int()
+        self._ck(self.L.md_kspace_engine_active(self.h, C.byref(v)))
+        return bool(v.value)
+
     def autotune_ewald(self, ncand=5):
         a, r, k, ms = C.c_double(), C.c_double(), C.c_int64(), C.c_double()
         self._ck(self.L.md_autotune_ewald(self.h, ncand, C.byref(a), C.byref(r), C.byref(k), C.byref(ms)))
