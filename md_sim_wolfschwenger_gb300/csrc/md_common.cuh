@@ -152,6 +152,10 @@ struct KParams {
   const int* tc_kmap;    // [R][2kc + 1] sorted k index, or -1
   float* tc_part;        // [nchunk][mt][ns][128] FP32 chunk partials (column-major tiles)
   float* tc_w;           // scatter operand image [nt][hi, lo][64][kp] (this evaluation's layout)
+  float* tc_bimg;        // per step: X operand tiles per 16 particles [n/16][hi, lo][ns][32]
+  float2* tc_tblk;       // per step: Y, Z of each 16 particles [n/16][2][kc + 1][17]
+  int tc_scat_smem;      // dynamic shared memory of the scatter launch
+  int tc_sfa, tc_sfb;    // structure-factor ring slots (generated, copied)
   int* err;              // device error word (kErrTcWait on a wait that gave up)
 };
 

@@ -226,6 +226,11 @@ KParams k_params(md_ctx* c, void* B, void* F) {
   p.tc_kmap = c->tc_kmap;
   p.tc_part = c->tc_part;
   p.tc_w = F ? c->tc_wfull : c->tc_wfield;
+  p.tc_bimg = c->tc_bimg;
+  p.tc_tblk = c->tc_tblk;
+  p.tc_scat_smem = c->tcs.scat_smem;
+  p.tc_sfa = c->tcs.sfa;
+  p.tc_sfb = c->tcs.sfb;
   p.err = &c->sc->err;
   return p;
 }
@@ -424,6 +429,11 @@ int read_err_word(md_ctx* c) {
 
 // ============================================================== C ABI
 
+// Largest kc the context's k space runs on the tensor cores (0: none).
+static int tc_kc_bound(const md_ctx* c) {
+  return (fp64(c) || c->kengine == MD_KSPACE_SIMT) ? 0 : md::kspace_tc_max_kc();
+}
+
 // Tensor-core k space: the k rows (ny, nz) of the half-space k list, ordered
 // by nz then ny, the k index of each (row, nx), and the buffers of the
 // launches (md_ktc.cu).  Off (tc_rows = 0) on the FP64 path, when the
@@ -448,12 +458,14 @@ static int setup_tc(md_ctx* c) {
   int nsm = 148;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
   const md::TcShape t = md::kspace_tc_shape(kc, (int)c->n, R, nsm);
-  void* old[] = {c->tc_row, c->tc_kmap, c->tc_part, c->tc_wfull, c->tc_wfield};
+  void* old[] = {c->tc_row, c->tc_kmap, c->tc_part, c->tc_wfull, c->tc_wfield, c->tc_bimg, c->tc_tblk};
   for (void* q : old) dfree(c, q);
   c->tc_row = nullptr;
   c->tc_kmap = nullptr;
   c->tc_part = nullptr;
   c->tc_wfull = c->tc_wfield = nullptr;
+  c->tc_bimg = nullptr;
+  c->tc_tblk = nullptr;
   const size_t wfull = md::kspace_tc_image_floats(kc, t.nt_full), wfield = md::kspace_tc_image_floats(kc, t.nt_field);
   int st;
   if ((st = dalloc(c, &c->tc_row, sizeof(int2) * (size_t)R))) return st;
@@ -461,6 +473,8 @@ static int setup_tc(md_ctx* c) {
   if ((st = dalloc(c, &c->tc_part, sizeof(float) * (size_t)t.nchunk * t.mt * t.ns * 128))) return st;
   if ((st = dalloc(c, &c->tc_wfull, sizeof(float) * wfull))) return st;
   if ((st = dalloc(c, &c->tc_wfield, sizeof(float) * wfield))) return st;
+  if ((st = dalloc(c, &c->tc_bimg, sizeof(float) * md::kspace_tc_bimg_floats(kc, t.nsb)))) return st;
+  if ((st = dalloc(c, &c->tc_tblk, sizeof(float2) * md::kspace_tc_tblk_entries(kc, t.nsb)))) return st;
   if (t.nchunk > c->musum_cap) {
     dfree(c, c->musum_part);
     c->musum_part = nullptr;
@@ -750,7 +764,7 @@ int md_ewald_params(md_ctx* c, double rc, double* alpha, double* rc_out, int64_t
   double a = 0, kraw = 0;
   int64_t k = 0;
   if (rc <= 0) {
-    rc = mdh::choose_rc(c->cfg, m, c->n, &a, &k);
+    rc = mdh::choose_rc(c->cfg, m, c->n, &a, &k, tc_kc_bound(c));
     kraw = (double)k;
   } else {
     if (rc > 0.5 * c->L * (1 + 1e-12)) return set_err(c, MD_ERR_INVALID, "rc must not exceed L/2");
@@ -776,7 +790,7 @@ int md_ewald_params_host(const md_config* cfg, int64_t n, const double* rMag, co
   double a = 0, kraw = 0;
   int64_t k = 0;
   if (rc <= 0) {
-    rc = mdh::choose_rc(*cfg, m, n, &a, &k);
+    rc = mdh::choose_rc(*cfg, m, n, &a, &k, cfg->precision == MD_PREC_MIXED ? md::kspace_tc_max_kc() : 0);
   } else {
     if (rc > 0.5 * p.lBox * (1 + 1e-12)) return set_err(nullptr, MD_ERR_INVALID, "rc must not exceed L/2");
     if (!mdh::ewald_for_rc(*cfg, m, rc, &a, &kraw))
@@ -910,6 +924,8 @@ int md_set_kspace_engine(md_ctx* c, int engine) {
   invalidate_graph(c);
   CK(c, cudaStreamSynchronize(c->stream));
   c->kengine = engine;
+  // the per-step operand images of a newly chosen engine come with the next full evaluation
+  c->have_geometry = false;
   if (c->have_ewald) return setup_tc(c);
   return MD_OK;
 }
@@ -1434,7 +1450,7 @@ int md_autotune_ewald(md_ctx* c, int ncand, double* alpha_out, double* rc_out, i
   mdh::EwaldModel m = mdh::ewald_model(c->cfg, c->props);
   double a0;
   int64_t k0;
-  const double rc0 = mdh::choose_rc(c->cfg, m, c->n, &a0, &k0) / c->L;
+  const double rc0 = mdh::choose_rc(c->cfg, m, c->n, &a0, &k0, tc_kc_bound(c)) / c->L;
   cudaEvent_t e0, e1;
   CK(c, cudaEventCreate(&e0));
   CK(c, cudaEventCreate(&e1));

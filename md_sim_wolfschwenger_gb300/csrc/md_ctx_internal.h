@@ -121,6 +121,8 @@ struct md_ctx {
   int* tc_kmap = nullptr;
   float* tc_part = nullptr;
   float *tc_wfull = nullptr, *tc_wfield = nullptr;
+  float* tc_bimg = nullptr;
+  float2* tc_tblk = nullptr;
   // Verlet list (sorted indices) within rc + skin
   int *nbr = nullptr, *nbr_cnt = nullptr, *nbr_off = nullptr;
   long long nbr_cap = 0;

@@ -458,16 +458,18 @@ void predicted_errors(const md_config& c, const EwaldModel& m, double alpha, dou
 // the ordered pairs within rc (field + force and field-only passes over the
 // Verlet list, which is rebuilt only every many steps) and the k vectors of
 // the half space (structure factor twice, scatter twice).  The weights are
-// the measured per-unit times on GB300 (9.5 ps per ordered pair, 2.5 ps per
-// (k, particle) at N = 32768).
-double model_cost(double rc_box, int64_t kc, int64_t n) {
+// the measured per-unit times on GB300 at N = 32768: 9.5 ps per ordered
+// pair; per (k, particle) 2.5 ps on the FP32 CUDA-core k-space kernels and
+// 1.7 ps on the tensor-core ones (used for kc <= kc_tc).
+double model_cost(double rc_box, int64_t kc, int64_t n, int kc_tc) {
   const double pi = 3.141592653589793;
   const double nr = (double)n * 4.0 / 3.0 * pi * rc_box * rc_box * rc_box;
   const double nk = 2.0 * pi / 3.0 * (double)kc * kc * kc;
-  return (double)n * (9.5 * nr + 2.5 * nk);
+  return (double)n * (9.5 * nr + (kc <= kc_tc ? 1.7 : 2.5) * nk);
 }
 
-double choose_rc(const md_config& c, const EwaldModel& m, int64_t n, double* alpha_out, int64_t* kc_out) {
+double choose_rc(const md_config& c, const EwaldModel& m, int64_t n, double* alpha_out, int64_t* kc_out,
+                 int kc_tc) {
   // every candidate rc = 0.08 L .. 0.5 L in steps of 0.005 L (the cost is not
   // unimodal in rc, so no candidate is skipped)
   double best = 1e300, best_rc = 0.5;
@@ -477,7 +479,7 @@ double choose_rc(const md_config& c, const EwaldModel& m, int64_t n, double* alp
     if (!ewald_for_rc(c, m, x * m.L, &a, &k)) continue;
     const int64_t kc = (int64_t)std::floor(k + 0.5);
     if (kc > 64) continue;
-    const double cost = model_cost(x, kc, n);
+    const double cost = model_cost(x, kc, n, kc_tc);
     if (cost < best) {
       best = cost;
       best_rc = x;

@@ -49,8 +49,9 @@ bool ewald_for_rc(const md_config& c, const EwaldModel& m, double rc, double* al
 void predicted_errors(const md_config& c, const EwaldModel& m, double alpha, double rc, double kc,
                       double* errF, double* errT);
 // Cost-model choice of rc (box fraction in [0.08, 0.5]) for n particles.
-double choose_rc(const md_config& c, const EwaldModel& m, int64_t n, double* alpha, int64_t* kc);
-double model_cost(double rc_box, int64_t kc, int64_t n);
+// kc_tc: largest kc the tensor-core k space takes (0: none).
+double choose_rc(const md_config& c, const EwaldModel& m, int64_t n, double* alpha, int64_t* kc, int kc_tc);
+double model_cost(double rc_box, int64_t kc, int64_t n, int kc_tc);
 
 // ------------------------------------------------------ k-vector list
 struct KList {

@@ -65,10 +65,18 @@ struct TcShape {
   int nt_full, nt_field;        // scatter tiles (field + force, field only)
   int rt_full, rt_field;        // k rows per scatter tile
   int chunk, nchunk;            // structure-factor particle chunks
+  int nsb;                      // blocks of 16 particles (per-step operand images)
+  int sfa, sfb;                 // structure-factor ring slots (generated, copied)
+  int scat_smem;                // dynamic shared memory of the scatter
 };
 bool kspace_tc_supported(int kc);
+int kspace_tc_max_kc();  // largest supported kc
 TcShape kspace_tc_shape(int kc, int n, int rows, int nsm);
 size_t kspace_tc_image_floats(int kc, int nt);  // scatter operand image of nt tiles
+size_t kspace_tc_bimg_floats(int kc, int nsb);   // per-step X operand tiles
+size_t kspace_tc_tblk_entries(int kc, int nsb);  // per-step Y, Z blocks (float2)
+// Per-step operand images (after the phase tables), then per evaluation.
+int launch_kspace_tc_prep(cudaStream_t st, const KParams& p);
 int launch_kspace_tc(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* ev = nullptr);
 // Per-particle phase tables (once per step; positions are frozen across the
 // two Heun stages).

@@ -530,6 +530,7 @@ int launch_phase_tables(cudaStream_t st, const KParams& p, bool fp64) {
     k_phase_tables<double><<<phase_blocks(p.n), kPhaseThreads, 0, st>>>(p);
   else
     k_phase_tables<float><<<phase_blocks(p.n), kPhaseThreads, 0, st>>>(p);
+  if (!fp64 && p.tc_rows > 0) return 1 + launch_kspace_tc_prep(st, p);
   return 1;
 }
 

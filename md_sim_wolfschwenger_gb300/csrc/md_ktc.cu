@@ -22,26 +22,37 @@
 // Precision: each FP32 operand is split into TF32 hi + lo and the products
 // are hi*hi + hi*lo + lo*hi (three kind::tf32 MMAs into one FP32
 // accumulator), ~22 significant bits per product like FP32 arithmetic.  The
-// structure factor accumulates chunks of <= 1024 particles in the tensor
+// structure factor accumulates chunks of <= 2048 particles in the tensor
 // core's FP32 and sums the chunks in FP64 in a fixed order; the scatter sums
 // over the nx of a row in the MMA (<= 2 kc + 1 terms), over the rows of a
 // tile in FP32 and over tiles with compensated FP32 sums.  All sums have a
 // fixed order: results are deterministic.
 //
 // Kernels:
-//   k_sf_tc      grid (M tiles, chunks), 256 threads: generates U, V (A) and
-//                X (B) operands of 16 particles per stage in shared memory
-//                (two stages: the next is generated while the tensor cores
-//                multiply the current one), one thread issues the MMAs;
-//                D (128 x NS FP32) lives in tensor memory and is written to
-//                chunk partials at the end.
+//   k_tc_prep    once per step (positions are frozen across the step's
+//                evaluations): the X operand tiles (hi, lo) of every 16
+//                particles in the shared-memory layout of the structure
+//                factor, and their Y, Z phases in blocks.
+//   k_sf_tc      grid (M tiles, chunks); 16 warps generate the U, V operand
+//                of 16 particles per stage into a ring of shared-memory
+//                slots, one warp bulk-copies each stage's X tiles, tables and
+//                moments into a second ring, 4 warps issue the MMAs (stages
+//                dealt round-robin, one accumulator each, added in a fixed
+//                order at the end); mbarriers hand stages between the roles
+//                and tcgen05.commit releases the slots.
 //   k_sf_tc_reduce  FP64 sum of the chunk partials, S(n) = C_U + nx C_V,
 //                e(n) S(n), and the scatter's W operand image (hi, lo) in
 //                the shared-memory layout the scatter copies in bulk.
-//   k_kscat_tc   128 particles per block: the particles' X phases (A) stay in
-//                shared memory, W tiles of 64 columns stream in by bulk copy
-//                (2-3 stages), two tensor-memory accumulators alternate so
-//                the epilogue of one tile overlaps the MMAs of the next.
+//   k_kscat_tc   128 particles per block, their X phases (the A operand, hi
+//                and lo) in tensor memory; W tiles of 128 columns stream in
+//                by bulk copy (2-3 stages); two issuing warps alternate tiles
+//                into two tensor-memory accumulators, and 8 epilogue warps
+//                turn each accumulator into per-row terms of B and F.
+//
+// Pipeline latency, not arithmetic, bounds these kernels on GB300: a stage
+// is released by tcgen05.commit -> mbarrier, and that round trip (~1-2 us,
+// measured with the stage work removed) is long against the ~0.3 us of MMA
+// work per 16-particle stage; the rings hide it only partly.
 #include "md_common.cuh"
 #include "md_kernels.h"
 #include "md_tc.cuh"
@@ -52,65 +63,147 @@ namespace md {
 
 constexpr int kSfSC = 16;            // particles per structure-factor stage
 constexpr int kSfSK = 2 * kSfSC;     // K elements per stage
-constexpr int kSfThreads = 256;
-constexpr int kTcMaxKc = 25;         // shared-memory bound of the scatter (two stages)
-constexpr int kSfTabPer = (3 * (kTcMaxKc + 1) * kSfSC + kSfThreads - 1) / kSfThreads;  // table entries per thread
+constexpr int kSfGenWarps = 16;      // structure factor: operand generators (64 rows x U, V)
+constexpr int kSfIssuers = 4;        // structure factor: MMA-issuing warps (one accumulator each)
+constexpr int kSfThreads = 32 * (kSfGenWarps + 1 + kSfIssuers);  // + copy producer + issuers
+constexpr int kSfMaxSlots = 4;       // deepest operand rings
+constexpr int kTabPad = kSfSC + 1;   // Y, Z block row stride (bank spread)
+constexpr int kTcMaxKc = 25;         // operand bounds: A of the scatter in 256 tensor-memory columns
 constexpr int kScEpiWarps = 8;       // scatter: 2 warps per tensor-memory lane quarter (tile halves)
-constexpr int kScThreads = 32 * (kScEpiWarps + 1);  // + one producer warp (bulk copies, MMAs)
+constexpr int kScThreads = 32 * (kScEpiWarps + 3);  // + copy producer + two MMA issuers
 constexpr int kScParticles = 128;    // particles per scatter block (tensor-memory lanes)
-constexpr int kScCols = 64;          // scatter tile: 64 output columns
+constexpr int kScCols = 128;         // scatter tile: 128 output columns (MMA N)
 constexpr int kScMaxStages = 3;
 constexpr size_t kSmemLimit = 227 * 1024 - 5 * 1024;  // dynamic shared memory per block (static <= 4 KB)
 
-// Scatter tile: 64 real columns in two halves of 16 complex columns; a
-// half holds RH k rows x P complex columns Q_0 .. Q_{P-1} (+ padding), so
-// each half is one 32-column tensor-memory load of an epilogue warp.
+// Scatter tile: 128 real columns in two halves of 32 complex columns; a
+// half holds RH k rows x P complex columns Q_0 .. Q_{P-1} (+ padding), one
+// 64-column tensor-memory load of an epilogue warp.
 template <bool FULL>
 struct ScatLayout {
   static constexpr int P = FULL ? 3 : 2;       // Q_p per row
-  static constexpr int RH = FULL ? 5 : 8;      // rows per half tile
+  static constexpr int RH = FULL ? 10 : 16;    // rows per half tile
   static constexpr int RT = 2 * RH;            // rows per tile
   // complex column of Q_p of the tile's row sl
-  __host__ __device__ static constexpr int ccol(int sl, int pp) { return (sl / RH) * 16 + (sl % RH) * P + pp; }
+  __host__ __device__ static constexpr int ccol(int sl, int pp) { return (sl / RH) * 32 + (sl % RH) * P + pp; }
 };
 
 static int tc_ns(int kc) { return (2 * (2 * kc + 1) + 15) / 16 * 16; }
 static int tc_kp(int kc) { return (2 * (2 * kc + 1) + 7) / 8 * 8; }
 
-static size_t sf_smem(int kc) {
+// Structure-factor shared memory: a ring of na generated U, V operand slots
+// (hi, lo) and a ring of nb copied-in slots (X tiles hi, lo | Y, Z block |
+// moments), so the bulk copies run nb - 1 stages ahead and the generators
+// na - 1 stages ahead of the MMAs.
+struct SfLayout {
+  int na, nb, a, b, t, m, bt, bytes;
+  __host__ __device__ SfLayout(int ns, int k1, int na_, int nb_)
+      : na(na_), nb(nb_), a(128 * kSfSK * 4), b(ns * kSfSK * 4), t(2 * k1 * kTabPad * 8), m(kSfSC * 16),
+        bt(2 * b + t + m), bytes(na_ * 2 * a + nb_ * bt) {}
+  __host__ __device__ int aslot(int s) const { return (s % na) * 2 * a; }
+  __host__ __device__ int btslot(int s) const { return na * 2 * a + (s % nb) * bt; }
+};
+// deepest rings that fit: (4, 4), (4, 3), (3, 3), (2, 3)
+static SfLayout sf_layout(int kc) {
   const int ns = tc_ns(kc), k1 = kc + 1;
-  const size_t stage = 2 * (size_t)128 * kSfSK * 4 + 2 * (size_t)ns * kSfSK * 4;
-  return 2 * stage + (size_t)kSfSC * (3 * k1 + 1) * 8 + (size_t)kSfSC * 16;
+  const int opts[4][2] = {{4, 4}, {4, 3}, {3, 3}, {2, 3}};
+  for (const auto& o : opts) {
+    SfLayout l(ns, k1, o[0], o[1]);
+    if ((size_t)l.bytes <= kSmemLimit) return l;
+  }
+  return SfLayout(ns, k1, 2, 2);
 }
-static size_t scat_smem(int kc, int nst) {
+static size_t sf_smem(int kc) { return (size_t)sf_layout(kc).bytes; }
+static size_t scat_smem(int kc, int nst, int rows) {
   const int kp = tc_kp(kc);
-  return 2 * (size_t)128 * kp * 4 + (size_t)nst * 2 * kScCols * kp * 4;
+  return (size_t)nst * 2 * kScCols * kp * 4 + ((size_t)rows * 8 + 15) / 16 * 16;
+}
+
+// ------------------------------------------------------ per-step operands
+
+// Block per 16 particles: X operand rows 2q = (Re X, -Im X), 2q + 1 =
+// (Im X, Re X) per particle (q = nx + kc; zero beyond 2 kc and beyond n) as
+// hi, lo TF32 tiles [ns][32]; Y(|ny|), Z(nz) of the 16 particles.
+__global__ void __launch_bounds__(256) k_tc_prep(KParams p) {
+  const int sb = blockIdx.x;
+  const int NS = p.tc_ns, kc = p.kc, K1 = kc + 1, n = p.n;
+  const int j0 = sb * kSfSC;
+  const float2* gtab = (const float2*)p.tab;
+  unsigned char* bimg = (unsigned char*)(p.tc_bimg + (size_t)sb * 2 * NS * kSfSK);
+  for (int e = threadIdx.x; e < NS * (kSfSK / 4); e += blockDim.x) {
+    // 8 rows x 8 particle pairs per 64 threads: whole 128-byte core-matrix rows
+    const int nrow = (e & 7) + 8 * (e >> 6), c = (e >> 3) & 7;
+    const int q = nrow >> 1, par = nrow & 1;
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    if (q <= 2 * kc) {
+      const int nx = q - kc, ax = nx < 0 ? -nx : nx;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int j = j0 + 2 * c + h;
+        if (j < n) {
+          const float2 X = gtab[(size_t)ax * n + j];
+          const float xr = X.x, xi = nx < 0 ? -X.y : X.y;
+          v[2 * h] = par ? xi : xr;
+          v[2 * h + 1] = par ? xr : -xi;
+        }
+      }
+    }
+    float4 h4, l4;
+    tf32_split(v[0], h4.x, l4.x);
+    tf32_split(v[1], h4.y, l4.y);
+    tf32_split(v[2], h4.z, l4.z);
+    tf32_split(v[3], h4.w, l4.w);
+    *(float4*)(bimg + cm_off(nrow, 4 * c, kSfSK)) = h4;
+    *(float4*)(bimg + NS * kSfSK * 4 + cm_off(nrow, 4 * c, kSfSK)) = l4;
+  }
+  float2* tb = p.tc_tblk + (size_t)sb * 2 * K1 * kTabPad;
+  for (int e = threadIdx.x; e < 2 * K1 * kTabPad; e += blockDim.x) {
+    const int row = e / kTabPad, jj = e - row * kTabPad;  // row = axis (Y, Z) * K1 + |n|
+    const int j = j0 + jj;
+    tb[e] = (jj < kSfSC && j < n) ? gtab[(size_t)(K1 + row) * n + j] : make_float2(0.f, 0.f);
+  }
 }
 
 // ------------------------------------------------------ structure factor
 
+// Roles (warps): 0-15 generate the U, V operand of a stage into a
+// generated-operand slot; 16 bulk-copies X tiles, Y, Z blocks and moments
+// into copied-operand slots; 17 .. 16 + kSfIssuers issue the MMAs, issuer i
+// taking the stages s = i (mod kSfIssuers) into its own accumulator (several
+// issuing threads keep the tensor cores busy with these N <= 112 MMAs); the
+// accumulators are added in a fixed order at the end.
 __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ __align__(8) uint64_t full_bt[kSfMaxSlots];   // X tiles, tables, moments landed
+  __shared__ __align__(8) uint64_t bt_empty[kSfMaxSlots];  // MMAs that read the copied slot are complete
+  __shared__ __align__(8) uint64_t full_a[kSfMaxSlots];    // U, V operand written (all generator warps)
+  __shared__ __align__(8) uint64_t a_empty[kSfMaxSlots];   // MMAs that read the generated slot are complete
+  __shared__ __align__(8) uint64_t dfull[kSfIssuers];      // all MMAs of issuer i complete
   __shared__ uint32_t tslot;
-  __shared__ double red[3][kSfThreads / 32];
+  __shared__ volatile int abort_flag;
+  __shared__ double red[3][kSfGenWarps];
   const int mtile = blockIdx.x, chunk = blockIdx.y;
   const int NS = p.tc_ns, kc = p.kc, K1 = kc + 1, n = p.n;
-  const int abytes = 128 * kSfSK * 4, bbytes = NS * kSfSK * 4, sbytes = 2 * abytes + 2 * bbytes;
-  const int tstride = 3 * K1 + 1;
-  float2* tabs = (float2*)(smem + 2 * sbytes);              // [kSfSC][3 K1 + 1]: X, Y, Z
-  float4* mus = (float4*)(tabs + kSfSC * tstride);          // [kSfSC]
+  const SfLayout L(NS, K1, p.tc_sfa, p.tc_sfb);
+  const int kSfA = L.na, kSfB = L.nb;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int p0 = chunk * p.tc_chunk, p1 = min(n, p0 + p.tc_chunk);
   const int nstage = p1 > p0 ? (p1 - p0 + kSfSC - 1) / kSfSC : 0;
-  const uint32_t ncols = NS <= 32 ? 32 : (NS <= 64 ? 64 : (NS <= 128 ? 128 : 256));
-  const float2* gtab = (const float2*)p.tab;
-  const float4* gmu = (const float4*)p.s.mu;
+  const uint32_t acols = NS <= 64 ? 64 : 128;  // columns per accumulator
+  const uint32_t ncols = kSfIssuers * acols <= 256 ? 256 : 512;
 
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int q = 0; q < kSfB; q++) {
+      mbar_init(&full_bt[q], 1);
+      mbar_init(&bt_empty[q], 1);
+    }
+    for (int q = 0; q < kSfA; q++) {
+      mbar_init(&full_a[q], kSfGenWarps);
+      mbar_init(&a_empty[q], 1);
+    }
+    for (int q = 0; q < kSfIssuers; q++) mbar_init(&dfull[q], 1);
     mbar_init_fence();
+    abort_flag = 0;
   }
   if (warp == 0) tmem_alloc(&tslot, ncols);
   tc_fence_before();
@@ -118,63 +211,107 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
   tc_fence_after();
   const uint32_t tmem = tslot;
 
-  // A generator: row 8 warp + (lane & 7) of this M tile (U at m = row, V at
-  // m = 64 + row), particle pairs c = (lane >> 3) + 4 u
-  const int arow = 8 * warp + (lane & 7);
-  const int rg = mtile * 64 + arow;
-  const bool rvalid = rg < p.tc_rows;
-  const int2 rr = rvalid ? p.tc_row[rg] : make_int2(0, 0);
-  const int ny = rr.x, nz = rr.y, ay = ny < 0 ? -ny : ny;
-  const float nyf = (float)ny, nzf = (float)nz;
-  const uint32_t idesc = tc_idesc_tf32(128, NS);
-  const uint32_t sbo = kSfSK * 32;
-  bool ok = true;   // this thread's waits all succeeded
-  int ncom = 0;     // (thread 0) stages whose MMAs were issued
-
-  // this thread's share of a stage's tables, loaded one stage ahead
-  float2 tpre[kSfTabPer];
-  float4 mpre = make_float4(0.f, 0.f, 0.f, 0.f);
-  auto load_tables = [&](int s) {
-    const int j0 = p0 + s * kSfSC;
-#pragma unroll
-    for (int u = 0; u < kSfTabPer; u++) {
-      const int e = tid + u * kSfThreads;
-      const int row = e / kSfSC, j = e - row * kSfSC;  // row = axis * K1 + |n|
-      tpre[u] = (row < 3 * K1 && j0 + j < p1) ? gtab[(size_t)row * n + j0 + j] : make_float2(0.f, 0.f);
+  if (warp == kSfGenWarps) {
+    // copy producer
+    if (lane == 0) {
+      auto issue_copy = [&](int s) {
+        unsigned char* st = smem + L.btslot(s);
+        uint64_t* bar = &full_bt[s % kSfB];
+        const int j0 = p0 + s * kSfSC, sb = j0 / kSfSC;
+        const uint32_t mb = (uint32_t)(min(kSfSC, p1 - j0) * 16);
+        mbar_expect_tx(bar, (uint32_t)(2 * L.b + L.t) + mb);
+        bulk_g2s(st, p.tc_bimg + (size_t)sb * 2 * NS * kSfSK, 2 * L.b, bar);
+        bulk_g2s(st + 2 * L.b, p.tc_tblk + (size_t)sb * 2 * K1 * kTabPad, L.t, bar);
+        bulk_g2s(st + 2 * L.b + L.t, (const float4*)p.s.mu + j0, mb, bar);
+      };
+      bool ok = true;
+      int issued = 0;
+      for (int s = 0; s < kSfB && s < nstage; s++) {
+        issue_copy(s);
+        issued = s + 1;
+      }
+      for (int s = 0; s + kSfB < nstage && ok; s++) {
+        // the copied slot of stage s takes stage s + kSfB once stage s's MMAs are done
+        ok = mbar_wait_abort(&bt_empty[s % kSfB], (s / kSfB) & 1, &abort_flag);
+        if (!ok) break;
+        issue_copy(s + kSfB);
+        issued = s + kSfB + 1;
+      }
+      if (!ok) {
+        abort_flag = 1;
+        atomicOr(p.err, kErrTcWait);
+      }
+      // no copy may still be in flight at the exit: the last copy of each slot has landed
+      for (int u = issued - kSfB > 0 ? issued - kSfB : 0; u < issued; u++)
+        mbar_wait(&full_bt[u % kSfB], (u / kSfB) & 1);
     }
-    if (tid < kSfSC) mpre = j0 + tid < p1 ? gmu[j0 + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
-  };
-  if (nstage > 0) load_tables(0);
-
-  for (int s = 0; s < nstage; s++) {
-    unsigned char* st = smem + (s & 1) * sbytes;
-    // the MMAs that last read this stage buffer (stage s - 2) are complete
-    if (s >= 2 && ok) ok = mbar_wait(&bar[s & 1], ((s - 2) >> 1) & 1);
+  } else if (warp > kSfGenWarps) {
+    // MMA issuer is: stages is, is + kSfIssuers, ...
+    const int is = warp - kSfGenWarps - 1;
+    if (lane == 0) {
+      const uint32_t idesc = tc_idesc_tf32(128, NS);
+      const uint32_t sbo = kSfSK * 32;
+      const uint32_t d = tmem + (uint32_t)is * acols;
+      bool ok = true, any = false;
+      for (int s = is; s < nstage && ok; s += kSfIssuers) {
+        ok = mbar_wait_abort(&full_a[s % kSfA], (s / kSfA) & 1, &abort_flag);
+        if (!ok) break;
+        tc_fence_after();
+        // descriptors of the slots' tiles; k step ks starts 256 B (16 address units) further
+        const uint64_t dah = tc_desc(smem_u32(smem + L.aslot(s)), 128, sbo), dal = dah + (uint64_t)(L.a >> 4);
+        const uint64_t dbh = tc_desc(smem_u32(smem + L.btslot(s)), 128, sbo), dbl = dbh + (uint64_t)(L.b >> 4);
 #pragma unroll
-    for (int u = 0; u < kSfTabPer; u++) {
-      const int e = tid + u * kSfThreads;
-      const int row = e / kSfSC, j = e - row * kSfSC;
-      if (row < 3 * K1) tabs[j * tstride + row] = tpre[u];
+        for (int ks = 0; ks < kSfSK / 8; ks++) {
+          const uint64_t o = 16 * ks;
+          tc_mma_tf32(d, dah + o, dbh + o, idesc, any || ks > 0);
+          tc_mma_tf32(d, dah + o, dbl + o, idesc, true);
+          tc_mma_tf32(d, dal + o, dbh + o, idesc, true);
+        }
+        any = true;
+        tc_commit(smem_u32(&bt_empty[s % kSfB]));
+        tc_commit(smem_u32(&a_empty[s % kSfA]));
+      }
+      if (!ok) {
+        abort_flag = 1;
+        atomicOr(p.err, kErrTcWait);
+      }
+      tc_commit(smem_u32(&dfull[is]));  // tracks every MMA this issuer started
     }
-    if (tid < kSfSC) mus[tid] = mpre;
-    __syncthreads();
-    if (s + 1 < nstage) load_tables(s + 1);  // in flight during this stage's generation
-    unsigned char* ahi = st;
-    unsigned char* alo = st + abytes;
-    unsigned char* bhi = st + 2 * abytes;
-    unsigned char* blo = st + 2 * abytes + bbytes;
-#pragma unroll
-    for (int u = 0; u < 2; u++) {
-      const int c = (lane >> 3) + 4 * u;  // particles 2c, 2c + 1 -> k = 4c .. 4c + 3
+  } else {
+    // generator: row 8 (warp & 7) + (lane & 7) of this M tile (U at m = row,
+    // V at m = 64 + row), particle pair c = (lane >> 3) + 4 (warp >> 3)
+    const int arow = 8 * (warp & 7) + (lane & 7);
+    const int c = (lane >> 3) + 4 * (warp >> 3);  // particles 2c, 2c + 1 -> k = 4c .. 4c + 3
+    const int rg = mtile * 64 + arow;
+    const bool rvalid = rg < p.tc_rows;
+    const int2 rr = rvalid ? p.tc_row[rg] : make_int2(0, 0);
+    const int ny = rr.x, nz = rr.y, ay = ny < 0 ? -ny : ny;
+    const float nyf = (float)ny, nzf = (float)nz;
+    for (int s = 0; s < nstage; s++) {
+      bool w = mbar_wait_abort(&full_bt[s % kSfB], (s / kSfB) & 1, &abort_flag);
+      if (w && s >= kSfA) w = mbar_wait_abort(&a_empty[s % kSfA], ((s - kSfA) / kSfA) & 1, &abort_flag);
+      w = __all_sync(kFull, w);
+      if (!w) {
+        if (lane == 0) {
+          abort_flag = 1;
+          atomicOr(p.err, kErrTcWait);
+        }
+        break;
+      }
+      unsigned char* sa = smem + L.aslot(s);
+      const unsigned char* sbt = smem + L.btslot(s);
+      const float2* tb = (const float2*)(sbt + 2 * L.b);
+      const float4* mus = (const float4*)(sbt + 2 * L.b + L.t);
+      const int nval = p1 - (p0 + s * kSfSC);
       float U[4] = {0.f, 0.f, 0.f, 0.f}, V[4] = {0.f, 0.f, 0.f, 0.f};
-      if (rvalid) {
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const float2* tb = tabs + (2 * c + h) * tstride;
-          float2 Y = tb[K1 + ay];
+      for (int h = 0; h < 2; h++) {
+        const int j = 2 * c + h;
+        if (rvalid && j < nval) {
+          float2 Y = tb[ay * kTabPad + j];
           if (ny < 0) Y.y = -Y.y;
-          const float2 Z = tb[2 * K1 + nz];
-          const float4 mu = mus[2 * c + h];
+          const float2 Z = tb[(K1 + nz) * kTabPad + j];
+          const float4 mu = mus[j];
           const float pr = Y.x * Z.x - Y.y * Z.y, pi = Y.x * Z.y + Y.y * Z.x;
           const float cf = nyf * mu.y + nzf * mu.z;
           U[2 * h] = cf * pr;
@@ -188,89 +325,63 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
       tf32_split(U[1], h4.y, l4.y);
       tf32_split(U[2], h4.z, l4.z);
       tf32_split(U[3], h4.w, l4.w);
-      *(float4*)(ahi + cm_off(arow, 4 * c, kSfSK)) = h4;
-      *(float4*)(alo + cm_off(arow, 4 * c, kSfSK)) = l4;
+      *(float4*)(sa + cm_off(arow, 4 * c, kSfSK)) = h4;
+      *(float4*)(sa + L.a + cm_off(arow, 4 * c, kSfSK)) = l4;
       tf32_split(V[0], h4.x, l4.x);
       tf32_split(V[1], h4.y, l4.y);
       tf32_split(V[2], h4.z, l4.z);
       tf32_split(V[3], h4.w, l4.w);
-      *(float4*)(ahi + cm_off(64 + arow, 4 * c, kSfSK)) = h4;
-      *(float4*)(alo + cm_off(64 + arow, 4 * c, kSfSK)) = l4;
-    }
-    // B rows: 2q = (Re X, -Im X), 2q + 1 = (Im X, Re X) per particle, X = X(q - kc)
-    for (int e = tid; e < NS * (kSfSK / 4); e += kSfThreads) {
-      // a warp writes 8 rows x 4 particle pairs: whole 128-byte core-matrix rows
-      const int nrow = (e & 7) + 8 * (e >> 6), c = ((e >> 3) & 3) + 4 * ((e >> 5) & 1);
-      const int q = nrow >> 1, par = nrow & 1;
-      float v[4] = {0.f, 0.f, 0.f, 0.f};
-      if (q <= 2 * kc) {
-        const int nx = q - kc, ax = nx < 0 ? -nx : nx;
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const float2 X = tabs[(2 * c + h) * tstride + ax];
-          const float xr = X.x, xi = nx < 0 ? -X.y : X.y;
-          v[2 * h] = par ? xi : xr;
-          v[2 * h + 1] = par ? xr : -xi;
-        }
-      }
-      float4 h4, l4;
-      tf32_split(v[0], h4.x, l4.x);
-      tf32_split(v[1], h4.y, l4.y);
-      tf32_split(v[2], h4.z, l4.z);
-      tf32_split(v[3], h4.w, l4.w);
-      *(float4*)(bhi + cm_off(nrow, 4 * c, kSfSK)) = h4;
-      *(float4*)(blo + cm_off(nrow, 4 * c, kSfSK)) = l4;
-    }
-    fence_async_smem();
-    __syncthreads();
-    if (tid == 0 && ok) {
-      tc_fence_after();
-      const uint32_t ah = smem_u32(ahi), al = smem_u32(alo), bh = smem_u32(bhi), bl = smem_u32(blo);
-#pragma unroll
-      for (int ks = 0; ks < kSfSK / 8; ks++) {
-        const uint32_t o = ks * 256;
-        tc_mma_tf32(tmem, tc_desc(ah + o, 128, sbo), tc_desc(bh + o, 128, sbo), idesc, s > 0 || ks > 0);
-        tc_mma_tf32(tmem, tc_desc(ah + o, 128, sbo), tc_desc(bl + o, 128, sbo), idesc, true);
-        tc_mma_tf32(tmem, tc_desc(al + o, 128, sbo), tc_desc(bh + o, 128, sbo), idesc, true);
-      }
-      tc_commit(smem_u32(&bar[s & 1]));
-      ncom = s + 1;
+      *(float4*)(sa + cm_off(64 + arow, 4 * c, kSfSK)) = h4;
+      *(float4*)(sa + L.a + cm_off(64 + arow, 4 * c, kSfSK)) = l4;
+      fence_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&full_a[s % kSfA]);
     }
   }
-  // the last commit tracks every MMA of this block
-  bool fin = ok && nstage > 0;
-  if (fin) fin = mbar_wait(&bar[(nstage - 1) & 1], ((nstage - 1) >> 1) & 1);
-  // after a failed wait: the MMAs that were issued finish before the exit
-  if (tid == 0 && ncom > 0 && ncom < nstage) mbar_wait(&bar[(ncom - 1) & 1], ((ncom - 1) >> 1) & 1);
-  ok = fin || nstage == 0;
-  if (!ok && lane == 0) atomicOr(p.err, kErrTcWait);
-  tc_fence_after();
-  {
-    // warp w: tensor-memory lanes 32 (w & 3) .., column half w >> 2
+  tc_fence_before();
+  __syncthreads();
+  if (warp < 8) {
+    // every issuer's MMAs are complete (each issuer committed once at its end)
+    bool w = true;
+    for (int q = 0; q < kSfIssuers; q++) w = w && mbar_wait_abort(&dfull[q], 0, &abort_flag);
+    w = __all_sync(kFull, w);
+    tc_fence_after();
+    const bool good = w && !abort_flag && nstage > 0;
+    // warp w: tensor-memory lanes 32 (w & 3) .., column half w >> 2; the
+    // accumulators of the issuers that had stages, added in order
     const int m = 32 * (warp & 3) + lane;
     const int c0 = (warp >> 2) * (NS / 2);
+    const int nis = min(nstage, kSfIssuers);
     float* out = p.tc_part + (size_t)(chunk * p.tc_mt + mtile) * NS * 128;
     for (int cc = c0; cc < c0 + NS / 2; cc += 8) {
-      float v[8];
-      tmem_ld8(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + cc, v);
-      tmem_wait_ld();
+      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int q = 0; q < nis; q++) {
+        float v[8];
+        tmem_ld8(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)q * acols + cc, v);
+        tmem_wait_ld();
 #pragma unroll
-      for (int u = 0; u < 8; u++) out[(size_t)(cc + u) * 128 + m] = (fin) ? v[u] : 0.f;
+        for (int u = 0; u < 8; u++) acc[u] += v[u];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) out[(size_t)(cc + u) * 128 + m] = good ? acc[u] : 0.f;
     }
+    if (!w && lane == 0) atomicOr(p.err, kErrTcWait);
   }
   if (mtile == 0) {
     // FP64 moment sum of this chunk (surface term)
+    const float4* gmu = (const float4*)p.s.mu;
     double m0 = 0, m1 = 0, m2 = 0;
-    for (int q = p0 + tid; q < p1; q += kSfThreads) {
-      const float4 mu = gmu[q];
-      m0 += (double)mu.x;
-      m1 += (double)mu.y;
-      m2 += (double)mu.z;
-    }
+    if (warp < kSfGenWarps)
+      for (int q = p0 + tid; q < p1; q += 32 * kSfGenWarps) {
+        const float4 mu = gmu[q];
+        m0 += (double)mu.x;
+        m1 += (double)mu.y;
+        m2 += (double)mu.z;
+      }
     m0 = warp_sum(m0);
     m1 = warp_sum(m1);
     m2 = warp_sum(m2);
-    if (lane == 0) {
+    if (lane == 0 && warp < kSfGenWarps) {
       red[0][warp] = m0;
       red[1][warp] = m1;
       red[2][warp] = m2;
@@ -278,7 +389,7 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
     __syncthreads();
     if (tid < 3) {
       double s = 0;
-      for (int w = 0; w < kSfThreads / 32; w++) s += red[tid][w];
+      for (int w = 0; w < kSfGenWarps; w++) s += red[tid][w];
       p.musum_part[3 * chunk + tid] = s;
     }
   }
@@ -296,12 +407,12 @@ __device__ __forceinline__ void w_put(float* img, int kp, int row, int k, float 
   img[kScCols * kp + o] = l;
 }
 
-// Block per (M tile, column q): 64 rows x 4 groups of chunks, the groups
+// Block per (M tile, column q): 64 rows x 8 groups of chunks, the groups
 // combined in a fixed order.
 template <bool FULL>
-__global__ void __launch_bounds__(256) k_sf_tc_reduce(KParams p) {
+__global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
   using L = ScatLayout<FULL>;
-  __shared__ double red[4][4][64];
+  __shared__ double red[8][4][64];
   const int Q = 2 * p.kc + 1;
   const int mtile = blockIdx.x / Q, q = blockIdx.x - mtile * Q;
   const int rl = threadIdx.x & 63, grp = threadIdx.x >> 6;
@@ -314,7 +425,8 @@ __global__ void __launch_bounds__(256) k_sf_tc_reduce(KParams p) {
   const size_t cstride = (size_t)p.tc_mt * NS * 128;
   const float* b = p.tc_part + (size_t)mtile * NS * 128;
   double ur = 0, ui = 0, vr = 0, vi = 0;
-  for (int c = grp; c < p.tc_nchunk; c += 4) {
+  #pragma unroll 4
+  for (int c = grp; c < p.tc_nchunk; c += 8) {
     const float* bc = b + (size_t)c * cstride;
     ur += (double)bc[(2 * q) * 128 + rl];
     ui += (double)bc[(2 * q + 1) * 128 + rl];
@@ -327,10 +439,14 @@ __global__ void __launch_bounds__(256) k_sf_tc_reduce(KParams p) {
   red[grp][3][rl] = vi;
   __syncthreads();
   if (grp != 0) return;
-  ur = ((red[0][0][rl] + red[1][0][rl]) + red[2][0][rl]) + red[3][0][rl];
-  ui = ((red[0][1][rl] + red[1][1][rl]) + red[2][1][rl]) + red[3][1][rl];
-  vr = ((red[0][2][rl] + red[1][2][rl]) + red[2][2][rl]) + red[3][2][rl];
-  vi = ((red[0][3][rl] + red[1][3][rl]) + red[2][3][rl]) + red[3][3][rl];
+  ur = ui = vr = vi = 0;
+#pragma unroll
+  for (int g8 = 0; g8 < 8; g8++) {
+    ur += red[g8][0][rl];
+    ui += red[g8][1][rl];
+    vr += red[g8][2][rl];
+    vi += red[g8][3][rl];
+  }
   const int r = mtile * 64 + rl;
   if (r >= p.tc_rows) return;
   const int kk = p.tc_kmap[r * Q + q];
@@ -359,50 +475,61 @@ __global__ void __launch_bounds__(256) k_sf_tc_reduce(KParams p) {
 
 // ---------------------------------------------------------------- scatter
 
-// Warps 0-7: epilogue (warp w reads tensor-memory lanes 32 (w & 3) .. for
-// its particles and the half w >> 2 of each tile); warp 8, one lane:
-// producer (bulk copies of W tiles into NST stages, MMAs into two
-// alternating accumulators).  An epilogue warp releases an accumulator as
-// soon as it has loaded it, so the MMAs of the next tiles overlap the
-// arithmetic of this one.
+// Roles (warps): 0-7 epilogue (warp w owns the tensor-memory lanes
+// 32 (w & 3) .. = its particles and the half w >> 2 of each tile), 8 copy
+// producer (bulk copies of W tiles into NST stages), 9 and 10 MMA issuers
+// (tiles alternate between them, each into its own 128-column accumulator;
+// two issuing threads keep the tensor cores busy with these small MMAs).
+// The particles' X phases (the A operand, hi and lo) sit in tensor memory
+// (columns [0, 2 kp)), the accumulators at columns 256 and 384.  An
+// epilogue warp releases an accumulator as soon as it has loaded it.
 template <bool FULL>
 __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
   using L = ScatLayout<FULL>;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t full_bar[kScMaxStages];  // W tile landed in a stage
-  __shared__ __align__(8) uint64_t mma_bar[2];              // accumulator d complete
-  __shared__ __align__(8) uint64_t free_bar[2];             // accumulator d loaded by all epilogue warps
+  __shared__ __align__(8) uint64_t sfree_bar[kScMaxStages]; // the MMAs that read the stage are done
+  __shared__ __align__(8) uint64_t dfull_bar[2];            // accumulator of issuer i complete
+  __shared__ __align__(8) uint64_t dfree_bar[2];            // accumulator of issuer i loaded by the epilogue
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
   __shared__ float part[6][kScParticles];                   // second tile halves' sums
   const int kp = p.tc_kp, kc = p.kc, K1 = kc + 1, n = p.n, R = p.tc_rows, NT = p.tc_nt, NST = p.tc_nst;
-  const int abytes = kScParticles * kp * 4;
   const int tbytes = 2 * kScCols * kp * 4;
-  unsigned char* a_hi = smem;
-  unsigned char* a_lo = smem + abytes;
-  unsigned char* stage0 = smem + 2 * abytes;
+  unsigned char* stage0 = smem;
+  int2* rows_s = (int2*)(stage0 + NST * tbytes);  // [R] (ny, nz)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool producer = warp == kScEpiWarps;
+  const bool epi = warp < kScEpiWarps;
   const int quarter = warp & 3, half = (warp >> 2) & 1;
   const int pl = 32 * quarter + lane;  // particle of this epilogue thread = tensor-memory lane
   const int i = blockIdx.x * kScParticles + pl;
-  const bool act = !producer && i < n;
+  const bool act = epi && i < n;
   const int ii = i < n ? i : n - 1;
   const float2* gtab = (const float2*)p.tab;
+  for (int r = tid; r < R; r += kScThreads) rows_s[r] = p.tc_row[r];
 
   if (tid == 0) {
-    for (int q = 0; q < kScMaxStages; q++) mbar_init(&full_bar[q], 1);
+    for (int q = 0; q < kScMaxStages; q++) {
+      mbar_init(&full_bar[q], 1);
+      mbar_init(&sfree_bar[q], 1);
+    }
     for (int q = 0; q < 2; q++) {
-      mbar_init(&mma_bar[q], 1);
-      mbar_init(&free_bar[q], kScEpiWarps);
+      mbar_init(&dfull_bar[q], 1);
+      mbar_init(&dfree_bar[q], kScEpiWarps);
     }
     mbar_init_fence();
     abort_flag = 0;
   }
-  if (warp == 0) tmem_alloc(&tslot, 2 * kScCols);
-  if (!producer) {
-    // A row of this particle: X(nx), nx = q - kc, at k = 2q (Re), 2q + 1 (Im);
-    // the two warps of a particle write half of the row each
+  if (warp == 0) tmem_alloc(&tslot, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tslot;
+  if (epi) {
+    // A row of this particle into its tensor-memory lane: X(nx), nx = q - kc,
+    // at k = 2q (Re), 2q + 1 (Im); hi at column k, lo at kp + k; the two
+    // warps of a lane quarter write half of the row each
+    const uint32_t lrow = tmem + ((uint32_t)(32 * quarter) << 16);
     for (int c = half * (kp / 8); c < (half + 1) * (kp / 8); c++) {
       float v[4];
 #pragma unroll
@@ -418,69 +545,79 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
         v[2 * h] = xr;
         v[2 * h + 1] = xi;
       }
-      float4 h4, l4;
-      tf32_split(v[0], h4.x, l4.x);
-      tf32_split(v[1], h4.y, l4.y);
-      tf32_split(v[2], h4.z, l4.z);
-      tf32_split(v[3], h4.w, l4.w);
-      *(float4*)(a_hi + cm_off(pl, 4 * c, kp)) = h4;
-      *(float4*)(a_lo + cm_off(pl, 4 * c, kp)) = l4;
+      float hi[4], lo[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) tf32_split(v[u], hi[u], lo[u]);
+      tmem_st4(lrow + 4 * c, hi);
+      tmem_st4(lrow + kp + 4 * c, lo);
     }
+    tmem_wait_st();
   }
-  fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  const uint32_t tmem = tslot;
   float b[3] = {0.f, 0.f, 0.f}, cb[3] = {0.f, 0.f, 0.f}, f[3] = {0.f, 0.f, 0.f}, cfr[3] = {0.f, 0.f, 0.f};
+  const uint32_t dcol[2] = {256u, 384u};
 
-  if (producer) {
+  if (warp == kScEpiWarps) {
+    // copy producer
     if (lane == 0) {
-      const uint32_t idesc = tc_idesc_tf32(128, kScCols);
-      const uint32_t sbo = kp * 32;
-      const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
       bool ok = true;
-      int issued = 0, consumed = 0, ncom = 0;
+      int issued = 0;
       for (int u = 0; u < NST && u < NT; u++) {
         mbar_expect_tx(&full_bar[u], tbytes);
         bulk_g2s(stage0 + u * tbytes, p.tc_w + (size_t)u * (tbytes / 4), tbytes, &full_bar[u]);
         issued = u + 1;
       }
-      for (int t = 0; t < NT && ok; t++) {
-        ok = mbar_wait_abort(&full_bar[t % NST], (t / NST) & 1, &abort_flag);
+      for (int t = 0; t + NST < NT && ok; t++) {
+        // the stage of tile t takes tile t + NST once tile t's MMAs are done
+        ok = mbar_wait_abort(&sfree_bar[t % NST], (t / NST) & 1, &abort_flag);
         if (!ok) break;
-        consumed = t + 1;
-        // accumulator t & 1 was loaded by the epilogue of tile t - 2
-        if (t >= 2) ok = mbar_wait_abort(&free_bar[t & 1], ((t - 2) >> 1) & 1, &abort_flag);
-        if (!ok) break;
-        tc_fence_after();
-        const uint32_t bh = smem_u32(stage0 + (t % NST) * tbytes), bl = bh + kScCols * kp * 4;
-        const uint32_t d = tmem + (uint32_t)((t & 1) * kScCols);
-        for (int ks = 0; ks < kp / 8; ks++) {
-          const uint32_t o = ks * 256;
-          tc_mma_tf32(d, tc_desc(ah + o, 128, sbo), tc_desc(bh + o, 128, sbo), idesc, ks > 0);
-          tc_mma_tf32(d, tc_desc(ah + o, 128, sbo), tc_desc(bl + o, 128, sbo), idesc, true);
-          tc_mma_tf32(d, tc_desc(al + o, 128, sbo), tc_desc(bh + o, 128, sbo), idesc, true);
-        }
-        tc_commit(smem_u32(&mma_bar[t & 1]));
-        ncom = t + 1;
-        // the stage of tile t - 1 is free once its MMAs are done: next tile in
-        const int u = t - 1 + NST;
-        if (t >= 1 && u < NT) {
-          ok = mbar_wait_abort(&mma_bar[(t - 1) & 1], ((t - 1) >> 1) & 1, &abort_flag);
-          if (!ok) break;
-          mbar_expect_tx(&full_bar[u % NST], tbytes);
-          bulk_g2s(stage0 + (u % NST) * tbytes, p.tc_w + (size_t)u * (tbytes / 4), tbytes, &full_bar[u % NST]);
-          issued = u + 1;
-        }
+        const int u = t + NST;
+        mbar_expect_tx(&full_bar[u % NST], tbytes);
+        bulk_g2s(stage0 + (u % NST) * tbytes, p.tc_w + (size_t)u * (tbytes / 4), tbytes, &full_bar[u % NST]);
+        issued = u + 1;
       }
       if (!ok) {
         abort_flag = 1;
         atomicOr(p.err, kErrTcWait);
       }
-      // nothing of this block may still be in flight when it exits
-      for (int u = consumed; u < issued; u++) mbar_wait(&full_bar[u % NST], (u / NST) & 1);
-      if (ncom > 0) mbar_wait(&mma_bar[(ncom - 1) & 1], ((ncom - 1) >> 1) & 1);
+      // no copy may still be in flight at the exit: the last copy of each stage has landed
+      for (int u = issued - NST > 0 ? issued - NST : 0; u < issued; u++)
+        mbar_wait(&full_bar[u % NST], (u / NST) & 1);
+    }
+  } else if (warp > kScEpiWarps) {
+    // MMA issuer 0 or 1: tiles t = is, is + 2, ...
+    const int is = warp - kScEpiWarps - 1;
+    if (lane == 0) {
+      const uint32_t idesc = tc_idesc_tf32(128, kScCols);
+      const uint32_t sbo = kp * 32;
+      const uint32_t d = tmem + dcol[is];
+      bool ok = true;
+      int k = 0, last = -1;
+      for (int t = is; t < NT && ok; t += 2, k++) {
+        ok = mbar_wait_abort(&full_bar[t % NST], (t / NST) & 1, &abort_flag);
+        if (ok && k >= 1) ok = mbar_wait_abort(&dfree_bar[is], (k - 1) & 1, &abort_flag);
+        if (!ok) break;
+        tc_fence_after();
+        const uint64_t dbh = tc_desc(smem_u32(stage0 + (t % NST) * tbytes), 128, sbo);
+        const uint64_t dbl = dbh + (uint64_t)((kScCols * kp * 4) >> 4);
+#pragma unroll 2
+        for (int ks = 0; ks < kp / 8; ks++) {
+          const uint64_t o = 16 * ks;
+          tc_mma_tf32_ta(d, tmem + 8 * ks, dbh + o, idesc, ks > 0);
+          tc_mma_tf32_ta(d, tmem + 8 * ks, dbl + o, idesc, true);
+          tc_mma_tf32_ta(d, tmem + kp + 8 * ks, dbh + o, idesc, true);
+        }
+        tc_commit(smem_u32(&dfull_bar[is]));
+        tc_commit(smem_u32(&sfree_bar[t % NST]));
+        last = k;
+      }
+      if (!ok) {
+        abort_flag = 1;
+        atomicOr(p.err, kErrTcWait);
+      }
+      if (last >= 0) mbar_wait(&dfull_bar[is], last & 1);  // this issuer's MMAs are done
     }
   } else {
     const float4 mu = act ? ((const float4*)p.s.mu)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -489,8 +626,28 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
       c = (t - s) - y;
       s = t;
     };
+    // P = Y(ny) Z(nz) of this particle for the rows of its half of tile t
+    auto fetch = [&](int t, float2* P) {
+#pragma unroll
+      for (int sh = 0; sh < L::RH; sh++) {
+        const int r = t * L::RT + half * L::RH + sh;
+        P[sh] = make_float2(0.f, 0.f);
+        if (r < R) {
+          const int2 rr = rows_s[r];
+          float2 y = gtab[(size_t)(K1 + (rr.x < 0 ? -rr.x : rr.x)) * n + ii];
+          if (rr.x < 0) y.y = -y.y;
+          const float2 z = gtab[(size_t)(2 * K1 + rr.y) * n + ii];
+          P[sh] = make_float2(y.x * z.x - y.y * z.y, y.x * z.y + y.y * z.x);
+        }
+      }
+    };
+    float2 Pc[L::RH];
+    if (NT > 0) fetch(0, Pc);
     for (int t = 0; t < NT; t++) {
-      bool w = mbar_wait_abort(&mma_bar[t & 1], (t >> 1) & 1, &abort_flag);
+      const int is = t & 1, k = t >> 1;
+      float2 Pn[L::RH];
+      if (t + 1 < NT) fetch(t + 1, Pn);  // in flight during this tile's wait and arithmetic
+      bool w = mbar_wait_abort(&dfull_bar[is], k & 1, &abort_flag);
       w = __all_sync(kFull, w);
       if (!w) {
         if (lane == 0) {
@@ -500,29 +657,22 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
         break;
       }
       tc_fence_after();
-      float v[32];
-      tmem_ld32(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)((t & 1) * kScCols + 32 * half), v);
+      float v[64];
+      const uint32_t ta = tmem + ((uint32_t)(32 * quarter) << 16) + dcol[is] + (uint32_t)(64 * half);
+      tmem_ld32(ta, v);
+      tmem_ld32(ta + 32, v + 32);
       tmem_wait_ld();
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&free_bar[t & 1]);
+      if (lane == 0) mbar_arrive(&dfree_bar[is]);
       float tb0 = 0.f, tb1 = 0.f, tb2 = 0.f, tf0 = 0.f, tf1 = 0.f, tf2 = 0.f;
-      int cur_nz = -1;
-      float2 Z = make_float2(0.f, 0.f);
 #pragma unroll
       for (int sh = 0; sh < L::RH; sh++) {
         const int r = t * L::RT + half * L::RH + sh;
         if (r < R) {
-          const int2 rr = p.tc_row[r];
-          const int ny = rr.x, nz = rr.y;
-          float2 Y = gtab[(size_t)(K1 + (ny < 0 ? -ny : ny)) * n + ii];
-          if (ny < 0) Y.y = -Y.y;
-          if (nz != cur_nz) {
-            Z = gtab[(size_t)(2 * K1 + nz) * n + ii];
-            cur_nz = nz;
-          }
-          const float pr = Y.x * Z.x - Y.y * Z.y, pi = Y.x * Z.y + Y.y * Z.x;
-          const float nyf = (float)ny, nzf = (float)nz;
+          const int2 rr = rows_s[r];
+          const float pr = Pc[sh].x, pi = Pc[sh].y;
+          const float nyf = (float)rr.x, nzf = (float)rr.y;
           const float* qv = v + 2 * L::P * sh;
           const float re0 = pr * qv[0] - pi * qv[1];
           const float re1 = pr * qv[2] - pi * qv[3];
@@ -548,6 +698,8 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
         kahan(f[1], cfr[1], tf1);
         kahan(f[2], cfr[2], tf2);
       }
+#pragma unroll
+      for (int sh = 0; sh < L::RH; sh++) Pc[sh] = Pn[sh];
     }
     if (half == 1) {
 #pragma unroll
@@ -574,13 +726,23 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
       F[2 * n + i] = cfo * ((f[2] - cfr[2]) + part[5][pl]);
     }
   }
-  if (warp == 0) tmem_free(tmem, 2 * kScCols);
+  if (warp == 0) tmem_free(tmem, 512);
 }
 
 // ------------------------------------------------------------ host side
 
+static int rows_bound(int kc) { return (kc + 1) * (2 * kc + 1); }
+
 bool kspace_tc_supported(int kc) {
-  return kc >= 1 && kc <= kTcMaxKc && sf_smem(kc) <= kSmemLimit && scat_smem(kc, 2) <= kSmemLimit && tc_ns(kc) <= 256;
+  return kc >= 1 && kc <= kTcMaxKc && sf_smem(kc) <= kSmemLimit && scat_smem(kc, 2, rows_bound(kc)) <= kSmemLimit &&
+         tc_ns(kc) <= 256;
+}
+
+int kspace_tc_max_kc() {
+  int k = 0;
+  for (int q = 1; q <= kTcMaxKc; q++)
+    if (kspace_tc_supported(q)) k = q;
+  return k;
 }
 
 TcShape kspace_tc_shape(int kc, int n, int rows, int nsm) {
@@ -588,17 +750,22 @@ TcShape kspace_tc_shape(int kc, int n, int rows, int nsm) {
   s.ns = tc_ns(kc);
   s.kp = tc_kp(kc);
   s.mt = (rows + 63) / 64;
-  s.nst = scat_smem(kc, 3) <= kSmemLimit ? 3 : 2;
+  s.nst = scat_smem(kc, 3, rows) <= kSmemLimit ? 3 : 2;
+  s.scat_smem = (int)scat_smem(kc, s.nst, rows);
   s.nt_full = (rows + ScatLayout<true>::RT - 1) / ScatLayout<true>::RT;
   s.nt_field = (rows + ScatLayout<false>::RT - 1) / ScatLayout<false>::RT;
   s.rt_full = ScatLayout<true>::RT;
   s.rt_field = ScatLayout<false>::RT;
-  // structure-factor grid: M tiles x chunks of <= 1024 particles, the chunk
+  s.nsb = (n + kSfSC - 1) / kSfSC;
+  const SfLayout sl = sf_layout(kc);
+  s.sfa = sl.na;
+  s.sfb = sl.nb;
+  // structure-factor grid: M tiles x chunks of <= 2048 particles, the chunk
   // count filling whole waves of resident blocks
-  int res = (int)((228 * 1024) / (sf_smem(kc) + 1024 + 2048));
+  int res = (int)((228 * 1024) / (sf_smem(kc) + 4096));
   res = std::max(1, std::min(res, 2));
   const long slots = (long)nsm * res;
-  const long nch_min = std::max(1L, ((long)n + 1023) / 1024);
+  const long nch_min = std::max(1L, ((long)n + 2047) / 2048);
   const long waves = std::max(1L, ((long)s.mt * nch_min + slots - 1) / slots);
   long nch = std::max(nch_min, waves * slots / (long)std::max(1, s.mt));
   nch = std::min<long>(nch, std::max(1L, ((long)n + kSfSC - 1) / kSfSC));
@@ -608,6 +775,13 @@ TcShape kspace_tc_shape(int kc, int n, int rows, int nsm) {
 }
 
 size_t kspace_tc_image_floats(int kc, int nt) { return (size_t)nt * 2 * kScCols * tc_kp(kc); }
+size_t kspace_tc_bimg_floats(int kc, int nsb) { return (size_t)nsb * 2 * tc_ns(kc) * kSfSK; }
+size_t kspace_tc_tblk_entries(int kc, int nsb) { return (size_t)nsb * 2 * (kc + 1) * kTabPad; }
+
+int launch_kspace_tc_prep(cudaStream_t st, const KParams& p) {
+  k_tc_prep<<<(p.n + kSfSC - 1) / kSfSC, 256, 0, st>>>(p);
+  return 1;
+}
 
 int launch_kspace_tc(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* ev) {
   const size_t sm1 = sf_smem(p.kc);
@@ -616,11 +790,11 @@ int launch_kspace_tc(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* 
   if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
   const int nred = p.tc_mt * (2 * p.kc + 1);
   if (full)
-    k_sf_tc_reduce<true><<<nred, 256, 0, st>>>(p);
+    k_sf_tc_reduce<true><<<nred, 512, 0, st>>>(p);
   else
-    k_sf_tc_reduce<false><<<nred, 256, 0, st>>>(p);
+    k_sf_tc_reduce<false><<<nred, 512, 0, st>>>(p);
   if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
-  const size_t sm2 = scat_smem(p.kc, p.tc_nst);
+  const size_t sm2 = (size_t)p.tc_scat_smem;
   const int nb = (p.n + kScParticles - 1) / kScParticles;
   if (full) {
     cudaFuncSetAttribute(k_kscat_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);

@@ -10,17 +10,15 @@
 // One kind::tf32 MMA consumes K = 8 elements (two core matrices along K), so
 // the k-th step starts 256 B * k after the tile.
 //
-// Every mbarrier wait is bounded: after kWaitLimit polls it gives up and the
+// Every mbarrier wait is bounded: after kWaitCycles it gives up and the
 // caller records an error (no wait can hang the GPU).
 #pragma once
 #include <cstdint>
 
 namespace md {
 
-// mbarrier polls before a wait gives up; each poll suspends for at most
-// kWaitHintNs, so a wait that never completes ends after about a second
-constexpr long kWaitLimit = 1000000;
-constexpr uint32_t kWaitHintNs = 1000;
+// A wait gives up after kWaitCycles SM clock cycles (about a second).
+constexpr long long kWaitCycles = 2000000000LL;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -49,6 +47,15 @@ __device__ __forceinline__ void tc_mma_tf32(uint32_t d_tmem, uint64_t a, uint64_
       "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
       "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)acc));
+}
+
+// D[tmem] (+)= A[tmem] * B[smem]^T: A (M x K, 32-bit elements) in tensor
+// memory, row m in lane m, element k in column a_tmem + k.
+__device__ __forceinline__ void tc_mma_tf32_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc, bool acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"((uint32_t)acc));
 }
 
 // The mbarrier completes one phase when every MMA issued so far by this
@@ -94,6 +101,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// 4 consecutive 32-bit columns into this thread's tensor-memory lane.
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, const float* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(__float_as_uint(v[0])),
+               "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3]))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // ------------------------------------------------------------- mbarriers
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -108,37 +122,37 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                "r"(bytes)
                : "memory");
 }
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 // Waits for the phase with the given parity to complete; false after
-// kWaitLimit polls.
+// kWaitCycles.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   const uint32_t a = smem_u32(bar);
-  for (long it = 0; it < kWaitLimit; it++) {
-    uint32_t ok;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(a), "r"(parity), "r"(kWaitHintNs)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
+  if (mbar_try(a, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try(a, parity))
+    if (clock64() - t0 > kWaitCycles) return false;
+  return true;
 }
 
 // As mbar_wait, but also gives up as soon as *abort is set (another role of
 // the block failed).
 __device__ __forceinline__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, volatile int* abort) {
   const uint32_t a = smem_u32(bar);
-  for (long it = 0; it < kWaitLimit; it++) {
-    uint32_t ok;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(a), "r"(parity), "r"(kWaitHintNs)
-        : "memory");
-    if (ok) return true;
-    if (*abort) return false;
+  if (mbar_try(a, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try(a, parity)) {
+    if (*abort || clock64() - t0 > kWaitCycles) return false;
   }
-  return false;
+  return true;
 }
 
 // Bulk copy global -> shared (16-byte aligned, size a multiple of 16),
