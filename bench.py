@@ -52,6 +52,22 @@ FLOPS_PAIR_FIELD = 58.0   # per unordered pair: field on both particles
 FLOPS_KSF = 11.0          # per (k, particle): phase step (6), weight (1), two accumulations (4)
 FLOPS_KSCAT_FULL = 21.0   # per (k, particle): phase step, field (6), force (9)
 FLOPS_KSCAT_FIELD = 12.0  # per (k, particle): phase step, field
+
+
+def tc_mma_flops(n, kc):
+    """Executed tensor-core FLOPs (3-pass TF32, padding included) per launch of
+    the tensor-core structure factor and scatter (md_ktc.cu) for kc: the same
+    row / tile shapes as kspace_tc_shape."""
+    rows = sum(1 for nz in range(kc + 1) for ny in range(-kc, kc + 1)
+               if ny * ny + nz * nz <= kc * kc and (nz > 0 or ny > 0)) + 1  # + the (0, 0) row (nx > 0)
+    ns = (2 * (2 * kc + 1) + 15) // 16 * 16
+    kp = (2 * (2 * kc + 1) + 7) // 8 * 8
+    mt = (rows + 63) // 64
+    npad = (n + 15) // 16 * 16
+    sf = 3 * 2.0 * (mt * 128) * ns * (2 * npad)
+    nb = (n + 127) // 128 * 128
+    nt_full, nt_field = (rows + 19) // 20, (rows + 31) // 32
+    return sf, 3 * 2.0 * nb * (nt_full * 128) * kp, 3 * 2.0 * nb * (nt_field * 128) * kp
 BYTES_CELLS = 60.0        # per particle (+8 per cell)
 BYTES_HEUN1 = 252.0       # per particle
 BYTES_HEUN2 = 404.0       # per particle
@@ -575,6 +591,17 @@ def run_ours(args):
             "kscat_full": ("fp32", nk_real * n * FLOPS_KSCAT_FULL),
             "kscat_field": ("fp32", nk_real * n * FLOPS_KSCAT_FIELD),
             "cells": ("hbm", n * BYTES_CELLS), "heun1": ("hbm", n * BYTES_HEUN1), "heun2": ("hbm", n * BYTES_HEUN2)}
+    peak_tf32 = None
+    if sim.kspace_tensor_cores():
+        # the tensor-core k space: executed 3-pass TF32 MMA work against the
+        # TF32 dense rate, half the measured bf16 rate (nominal 1:2)
+        sf_fl, scf_fl, scd_fl = tc_mma_flops(n, kc)
+        work.update(ksf_full=("tensor", sf_fl), ksf_field=("tensor", sf_fl), kscat_full=("tensor", scf_fl),
+                    kscat_field=("tensor", scd_fl))
+        try:
+            peak_tf32 = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"] / 2
+        except Exception:
+            peak_tf32 = 950.0
     segs = {}
     for k, ms in seg_mean.items():
         ent = {"ms": ms}
@@ -583,6 +610,10 @@ def run_ours(args):
             if kind == "fp32":
                 ach = amount / (ms * 1e-3) / 1e12
                 ent.update(bound="fp32", achieved=ach, unit="TFLOP/s", peak=peak_fp32, frac=ach / peak_fp32)
+            elif kind == "tensor":
+                ach = amount / (ms * 1e-3) / 1e12
+                ent.update(bound="tensor", achieved=ach, unit="TFLOP/s", peak=peak_tf32, frac=ach / peak_tf32,
+                           note="3-pass TF32 MMAs executed (padding included); peak = measured bf16 / 2")
             else:
                 ach = amount / (ms * 1e-3) / 1e9
                 ent.update(bound="hbm", achieved=ach, unit="GB/s", peak=hbm_peak,
