@@ -46,8 +46,9 @@
 //   k_kscat_tc   128 particles per block, their X phases (the A operand, hi
 //                and lo) in tensor memory; W tiles of 128 columns stream in
 //                by bulk copy (2-3 stages); two issuing warps alternate tiles
-//                into two tensor-memory accumulators, and 8 epilogue warps
-//                turn each accumulator into per-row terms of B and F.
+//                into two tensor-memory accumulators, and 16 epilogue warps
+//                (4 per tile quarter) turn each accumulator into per-row terms
+//                of B and F.
 //
 // Pipeline latency, not arithmetic, bounds these kernels on GB300: a stage
 // is released by tcgen05.commit -> mbarrier, and that round trip (~1-2 us,
@@ -69,23 +70,23 @@ constexpr int kSfThreads = 32 * (kSfGenWarps + 1 + kSfIssuers);  // + copy produ
 constexpr int kSfMaxSlots = 4;       // deepest operand rings
 constexpr int kTabPad = kSfSC + 1;   // Y, Z block row stride (bank spread)
 constexpr int kTcMaxKc = 25;         // operand bounds: A of the scatter in 256 tensor-memory columns
-constexpr int kScEpiWarps = 8;       // scatter: 2 warps per tensor-memory lane quarter (tile halves)
+constexpr int kScEpiWarps = 16;      // scatter: 4 warps per tensor-memory lane quarter (tile quarters)
 constexpr int kScThreads = 32 * (kScEpiWarps + 3);  // + copy producer + two MMA issuers
 constexpr int kScParticles = 128;    // particles per scatter block (tensor-memory lanes)
 constexpr int kScCols = 128;         // scatter tile: 128 output columns (MMA N)
 constexpr int kScMaxStages = 3;
 constexpr size_t kSmemLimit = 227 * 1024 - 5 * 1024;  // dynamic shared memory per block (static <= 4 KB)
 
-// Scatter tile: 128 real columns in two halves of 32 complex columns; a
-// half holds RH k rows x P complex columns Q_0 .. Q_{P-1} (+ padding), one
-// 64-column tensor-memory load of an epilogue warp.
+// Scatter tile: 128 real columns in four quarters of 16 complex columns; a
+// quarter holds RQ k rows x P complex columns Q_0 .. Q_{P-1} (+ padding),
+// one 32-column tensor-memory load of an epilogue warp.
 template <bool FULL>
 struct ScatLayout {
   static constexpr int P = FULL ? 3 : 2;       // Q_p per row
-  static constexpr int RH = FULL ? 10 : 16;    // rows per half tile
-  static constexpr int RT = 2 * RH;            // rows per tile
+  static constexpr int RQ = FULL ? 5 : 8;      // rows per quarter tile
+  static constexpr int RT = 4 * RQ;            // rows per tile
   // complex column of Q_p of the tile's row sl
-  __host__ __device__ static constexpr int ccol(int sl, int pp) { return (sl / RH) * 32 + (sl % RH) * P + pp; }
+  __host__ __device__ static constexpr int ccol(int sl, int pp) { return (sl / RQ) * 16 + (sl % RQ) * P + pp; }
 };
 
 static int tc_ns(int kc) { return (2 * (2 * kc + 1) + 15) / 16 * 16; }
@@ -475,9 +476,9 @@ __global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
 
 // ---------------------------------------------------------------- scatter
 
-// Roles (warps): 0-7 epilogue (warp w owns the tensor-memory lanes
-// 32 (w & 3) .. = its particles and the half w >> 2 of each tile), 8 copy
-// producer (bulk copies of W tiles into NST stages), 9 and 10 MMA issuers
+// Roles (warps): 0-15 epilogue (warp w owns the tensor-memory lanes
+// 32 (w & 3) .. = its particles and the quarter w >> 2 of each tile), 16 copy
+// producer (bulk copies of W tiles into NST stages), 17 and 18 MMA issuers
 // (tiles alternate between them, each into its own 128-column accumulator;
 // two issuing threads keep the tensor cores busy with these small MMAs).
 // The particles' X phases (the A operand, hi and lo) sit in tensor memory
@@ -493,14 +494,13 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
   __shared__ __align__(8) uint64_t dfree_bar[2];            // accumulator of issuer i loaded by the epilogue
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
-  __shared__ float part[6][kScParticles];                   // second tile halves' sums
   const int kp = p.tc_kp, kc = p.kc, K1 = kc + 1, n = p.n, R = p.tc_rows, NT = p.tc_nt, NST = p.tc_nst;
   const int tbytes = 2 * kScCols * kp * 4;
   unsigned char* stage0 = smem;
   int2* rows_s = (int2*)(stage0 + NST * tbytes);  // [R] (ny, nz)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool epi = warp < kScEpiWarps;
-  const int quarter = warp & 3, half = (warp >> 2) & 1;
+  const int quarter = warp & 3, cq = (warp >> 2) & 3;  // lane quarter, column quarter
   const int pl = 32 * quarter + lane;  // particle of this epilogue thread = tensor-memory lane
   const int i = blockIdx.x * kScParticles + pl;
   const bool act = epi && i < n;
@@ -527,10 +527,11 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
   const uint32_t tmem = tslot;
   if (epi) {
     // A row of this particle into its tensor-memory lane: X(nx), nx = q - kc,
-    // at k = 2q (Re), 2q + 1 (Im); hi at column k, lo at kp + k; the two
-    // warps of a lane quarter write half of the row each
+    // at k = 2q (Re), 2q + 1 (Im); hi at column k, lo at kp + k; the four
+    // warps of a lane quarter write a quarter of the row's 4-column groups each
     const uint32_t lrow = tmem + ((uint32_t)(32 * quarter) << 16);
-    for (int c = half * (kp / 8); c < (half + 1) * (kp / 8); c++) {
+    const int ng = kp / 4, gq = (ng + 3) / 4;
+    for (int c = cq * gq; c < min(ng, (cq + 1) * gq); c++) {
       float v[4];
 #pragma unroll
       for (int h = 0; h < 2; h++) {
@@ -626,11 +627,11 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
       c = (t - s) - y;
       s = t;
     };
-    // P = Y(ny) Z(nz) of this particle for the rows of its half of tile t
+    // P = Y(ny) Z(nz) of this particle for the rows of its quarter of tile t
     auto fetch = [&](int t, float2* P) {
 #pragma unroll
-      for (int sh = 0; sh < L::RH; sh++) {
-        const int r = t * L::RT + half * L::RH + sh;
+      for (int sh = 0; sh < L::RQ; sh++) {
+        const int r = t * L::RT + cq * L::RQ + sh;
         P[sh] = make_float2(0.f, 0.f);
         if (r < R) {
           const int2 rr = rows_s[r];
@@ -641,11 +642,11 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
         }
       }
     };
-    float2 Pc[L::RH];
+    float2 Pc[L::RQ];
     if (NT > 0) fetch(0, Pc);
     for (int t = 0; t < NT; t++) {
       const int is = t & 1, k = t >> 1;
-      float2 Pn[L::RH];
+      float2 Pn[L::RQ];
       if (t + 1 < NT) fetch(t + 1, Pn);  // in flight during this tile's wait and arithmetic
       bool w = mbar_wait_abort(&dfull_bar[is], k & 1, &abort_flag);
       w = __all_sync(kFull, w);
@@ -657,18 +658,16 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
         break;
       }
       tc_fence_after();
-      float v[64];
-      const uint32_t ta = tmem + ((uint32_t)(32 * quarter) << 16) + dcol[is] + (uint32_t)(64 * half);
-      tmem_ld32(ta, v);
-      tmem_ld32(ta + 32, v + 32);
+      float v[32];
+      tmem_ld32(tmem + ((uint32_t)(32 * quarter) << 16) + dcol[is] + (uint32_t)(32 * cq), v);
       tmem_wait_ld();
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&dfree_bar[is]);
       float tb0 = 0.f, tb1 = 0.f, tb2 = 0.f, tf0 = 0.f, tf1 = 0.f, tf2 = 0.f;
 #pragma unroll
-      for (int sh = 0; sh < L::RH; sh++) {
-        const int r = t * L::RT + half * L::RH + sh;
+      for (int sh = 0; sh < L::RQ; sh++) {
+        const int r = t * L::RT + cq * L::RQ + sh;
         if (r < R) {
           const int2 rr = rows_s[r];
           const float pr = Pc[sh].x, pi = Pc[sh].y;
@@ -699,31 +698,43 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
         kahan(f[2], cfr[2], tf2);
       }
 #pragma unroll
-      for (int sh = 0; sh < L::RH; sh++) Pc[sh] = Pn[sh];
-    }
-    if (half == 1) {
-#pragma unroll
-      for (int a = 0; a < 3; a++) {
-        part[a][pl] = b[a] - cb[a];
-        part[3 + a][pl] = f[a] - cfr[a];
-      }
+      for (int sh = 0; sh < L::RQ; sh++) Pc[sh] = Pn[sh];
     }
   }
   tc_fence_before();
   __syncthreads();
-  if (act && half == 0) {
-    // the two halves of the tiles, added in a fixed order
+  // the column quarters' sums of each particle, added in a fixed order; the
+  // stage buffers are free now (every copy landed, every MMA completed)
+  float* part = (float*)stage0;  // [3][6][kScParticles]
+  if (epi && cq > 0) {
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      part[((cq - 1) * 6 + a) * kScParticles + pl] = b[a] - cb[a];
+      part[((cq - 1) * 6 + 3 + a) * kScParticles + pl] = f[a] - cfr[a];
+    }
+  }
+  __syncthreads();
+  if (act && cq == 0) {
+    float sb[6];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      sb[a] = b[a] - cb[a];
+      sb[3 + a] = f[a] - cfr[a];
+    }
+    for (int g = 0; g < 3; g++)
+#pragma unroll
+      for (int a = 0; a < 6; a++) sb[a] += part[(g * 6 + a) * kScParticles + pl];
     float* B = (float*)p.B;
     const float cfl = (float)p.cflux;
-    B[i] = -cfl * ((b[0] - cb[0]) + part[0][pl]);
-    B[n + i] = -cfl * ((b[1] - cb[1]) + part[1][pl]);
-    B[2 * n + i] = -cfl * ((b[2] - cb[2]) + part[2][pl]);
+    B[i] = -cfl * sb[0];
+    B[n + i] = -cfl * sb[1];
+    B[2 * n + i] = -cfl * sb[2];
     if constexpr (FULL) {
       float* F = (float*)p.F;
       const float cfo = (float)p.cforce;
-      F[i] = cfo * ((f[0] - cfr[0]) + part[3][pl]);
-      F[n + i] = cfo * ((f[1] - cfr[1]) + part[4][pl]);
-      F[2 * n + i] = cfo * ((f[2] - cfr[2]) + part[5][pl]);
+      F[i] = cfo * sb[3];
+      F[n + i] = cfo * sb[4];
+      F[2 * n + i] = cfo * sb[5];
     }
   }
   if (warp == 0) tmem_free(tmem, 512);
