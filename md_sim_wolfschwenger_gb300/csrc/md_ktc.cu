@@ -22,10 +22,14 @@
 // Precision: each FP32 operand is split into TF32 hi + lo and the products
 // are hi*hi + hi*lo + lo*hi (three kind::tf32 MMAs into one FP32
 // accumulator), ~22 significant bits per product like FP32 arithmetic.  The
-// structure factor accumulates chunks of <= 2048 particles in the tensor
-// core's FP32 and sums the chunks in FP64 in a fixed order; the scatter sums
-// over the nx of a row in the MMA (<= 2 kc + 1 terms), over the rows of a
-// tile in FP32 and over tiles with compensated FP32 sums.  All sums have a
+// tensor core's FP32 accumulation loses precision with the number of MMAs
+// added into one accumulator (measured at N = 32768: 5.5e-6 relative error
+// of S with 392 particles per accumulator, 1.8e-6 with 128), so the
+// structure factor uses chunks of <= 512 particles (4 accumulators of <= 128
+// each, added in FP32) and sums the chunks with compensated FP32 sums, then
+// FP64; the scatter sums over the nx of a row in the MMA (<= 2 kc + 1 terms),
+// over the rows of a tile in FP32 and over tiles with compensated FP32 sums.
+// All sums have a
 // fixed order: results are deterministic.
 //
 // Kernels:
@@ -68,6 +72,7 @@ constexpr int kSfGenWarps = 16;      // structure factor: operand generators (64
 constexpr int kSfIssuers = 4;        // structure factor: MMA-issuing warps (one accumulator each)
 constexpr int kSfThreads = 32 * (kSfGenWarps + 1 + kSfIssuers);  // + copy producer + issuers
 constexpr int kSfMaxSlots = 4;       // deepest operand rings
+constexpr int kSfMaxChunk = 512;     // particles per structure-factor chunk (4 accumulators of <= 128)
 constexpr int kTabPad = kSfSC + 1;   // Y, Z block row stride (bank spread)
 constexpr int kTcMaxKc = 25;         // operand bounds: A of the scatter in 256 tensor-memory columns
 constexpr int kScEpiWarps = 16;      // scatter: 4 warps per tensor-memory lane quarter (tile quarters)
@@ -409,11 +414,19 @@ __device__ __forceinline__ void w_put(float* img, int kp, int row, int k, float 
 }
 
 // Block per (M tile, column q): 64 rows x 8 groups of chunks, the groups
-// combined in a fixed order.
+// combined in a fixed order.  The chunk partials are summed with compensated
+// FP32 sums (Kahan; GB300's FP64 rate is ~1/64 of FP32), the 8 group sums and
+// their compensations in FP64.
+__device__ __forceinline__ void kahan_f(float& s, float& c, float v) {
+  const float y = v - c, t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
 template <bool FULL>
 __global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
   using L = ScatLayout<FULL>;
-  __shared__ double red[8][4][64];
+  __shared__ float red[8][8][64];  // [group][sum, compensation x 4 values][row]
   const int Q = 2 * p.kc + 1;
   const int mtile = blockIdx.x / Q, q = blockIdx.x - mtile * Q;
   const int rl = threadIdx.x & 63, grp = threadIdx.x >> 6;
@@ -425,29 +438,28 @@ __global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
   const int NS = p.tc_ns;
   const size_t cstride = (size_t)p.tc_mt * NS * 128;
   const float* b = p.tc_part + (size_t)mtile * NS * 128;
-  double ur = 0, ui = 0, vr = 0, vi = 0;
-  #pragma unroll 4
+  float su[4] = {0.f, 0.f, 0.f, 0.f}, cu[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
   for (int c = grp; c < p.tc_nchunk; c += 8) {
     const float* bc = b + (size_t)c * cstride;
-    ur += (double)bc[(2 * q) * 128 + rl];
-    ui += (double)bc[(2 * q + 1) * 128 + rl];
-    vr += (double)bc[(2 * q) * 128 + 64 + rl];
-    vi += (double)bc[(2 * q + 1) * 128 + 64 + rl];
+    kahan_f(su[0], cu[0], bc[(2 * q) * 128 + rl]);
+    kahan_f(su[1], cu[1], bc[(2 * q + 1) * 128 + rl]);
+    kahan_f(su[2], cu[2], bc[(2 * q) * 128 + 64 + rl]);
+    kahan_f(su[3], cu[3], bc[(2 * q + 1) * 128 + 64 + rl]);
   }
-  red[grp][0][rl] = ur;
-  red[grp][1][rl] = ui;
-  red[grp][2][rl] = vr;
-  red[grp][3][rl] = vi;
+#pragma unroll
+  for (int v = 0; v < 4; v++) {
+    red[grp][2 * v][rl] = su[v];
+    red[grp][2 * v + 1][rl] = cu[v];
+  }
   __syncthreads();
   if (grp != 0) return;
-  ur = ui = vr = vi = 0;
+  double acc[4] = {0, 0, 0, 0};
 #pragma unroll
-  for (int g8 = 0; g8 < 8; g8++) {
-    ur += red[g8][0][rl];
-    ui += red[g8][1][rl];
-    vr += red[g8][2][rl];
-    vi += red[g8][3][rl];
-  }
+  for (int g8 = 0; g8 < 8; g8++)
+#pragma unroll
+    for (int v = 0; v < 4; v++) acc[v] += (double)red[g8][2 * v][rl] - (double)red[g8][2 * v + 1][rl];
+  const double ur = acc[0], ui = acc[1], vr = acc[2], vi = acc[3];
   const int r = mtile * 64 + rl;
   if (r >= p.tc_rows) return;
   const int kk = p.tc_kmap[r * Q + q];
@@ -771,12 +783,12 @@ TcShape kspace_tc_shape(int kc, int n, int rows, int nsm) {
   const SfLayout sl = sf_layout(kc);
   s.sfa = sl.na;
   s.sfb = sl.nb;
-  // structure-factor grid: M tiles x chunks of <= 2048 particles, the chunk
+  // structure-factor grid: M tiles x chunks of <= kSfMaxChunk particles, the chunk
   // count filling whole waves of resident blocks
   int res = (int)((228 * 1024) / (sf_smem(kc) + 4096));
   res = std::max(1, std::min(res, 2));
   const long slots = (long)nsm * res;
-  const long nch_min = std::max(1L, ((long)n + 2047) / 2048);
+  const long nch_min = std::max(1L, ((long)n + kSfMaxChunk - 1) / kSfMaxChunk);
   const long waves = std::max(1L, ((long)s.mt * nch_min + slots - 1) / slots);
   long nch = std::max(nch_min, waves * slots / (long)std::max(1, s.mt));
   nch = std::min<long>(nch, std::max(1L, ((long)n + kSfSC - 1) / kSfSC));

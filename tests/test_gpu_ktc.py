@@ -102,3 +102,27 @@ def test_engine_switch_rules():
     assert not fp64.kspace_tensor_cores()
     with pytest.raises(Exception):
         fp64.set_kspace_engine("tc")
+
+
+def test_tc_accuracy_large():
+    """N = 32768 polydisperse system: the accuracy of the tensor-core k space
+    depends on how many MMAs one FP32 tensor-memory accumulator takes (its
+    rounding error grows with that count), which small systems do not show.
+    The structure factor, the k-space field and the k-space force stay within
+    a few times the FP32 CUDA-core engine's error against FP64."""
+    from test_gpu_parity import random_system_fast
+    n = 32768
+    ini, g = random_system_fast(n, seed=4, phi=0.10, B0=0.02)
+    fAl, bAl, _ = scales(ini, g)
+    ref, s = engines(ini, g)
+    out = {}
+    for name, sim in (("fp64", ref), ("tc", s["tc"]), ("simt", s["simt"])):
+        B, F, _ = sim.CompInteractions()
+        Br, Fr = sim.debug_real_part()
+        out[name] = (B - Br, F - Fr, sf(sim))
+    S0 = out["fp64"][2]
+    srel = {k: np.sqrt(np.mean(np.abs(out[k][2] - S0) ** 2) / np.mean(np.abs(S0) ** 2)) for k in ("tc", "simt")}
+    assert srel["tc"] < 3e-6 and srel["simt"] < 1e-6
+    for k in ("tc", "simt"):
+        assert O.rms_rel(out[k][0], out["fp64"][0], bAl) < 1e-6
+        assert O.rms_rel(out[k][1], out["fp64"][1], fAl) < 1e-6
