@@ -144,17 +144,18 @@ struct KParams {
   int tc_mt;             // structure-factor M tiles of 64 rows (x U, V)
   int tc_ns;             // structure-factor N: 2 (2kc + 1) rounded up to 16
   int tc_kp;             // scatter K: 2 (2kc + 1) rounded up to 8
-  int tc_rt;             // rows per 64-column scatter tile: 10 (field + force) or 16
+  int tc_rt;             // k rows per 128-column scatter tile: 20 (field + force) or 32
   int tc_nt;             // scatter tiles: ceil(R / tc_rt)
   int tc_nst;            // scatter pipeline stages (2 or 3)
   int tc_chunk, tc_nchunk;  // structure-factor particle chunks (multiple of 16)
   const int2* tc_row;    // [R] (ny, nz)
   const int* tc_kmap;    // [R][2kc + 1] sorted k index, or -1
   float* tc_part;        // [nchunk][mt][ns][128] FP32 chunk partials (column-major tiles)
-  float* tc_w;           // scatter operand image [nt][hi, lo][64][kp] (this evaluation's layout)
+  float* tc_w;           // scatter operand image [nt][hi, lo][128][kp] (this evaluation's layout)
   float* tc_bimg;        // per step: X operand tiles per 16 particles [n/16][hi, lo][ns][32]
   float2* tc_tblk;       // per step: Y, Z of each 16 particles [n/16][2][kc + 1][17]
   int tc_scat_smem;      // dynamic shared memory of the scatter launch
+  int tc_yz;             // the scatter stages the Y, Z phases in shared memory
   int tc_sfa, tc_sfb;    // structure-factor ring slots (generated, copied)
   int* err;              // device error word (kErrTcWait on a wait that gave up)
 };

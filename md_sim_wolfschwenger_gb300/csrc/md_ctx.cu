@@ -229,6 +229,7 @@ KParams k_params(md_ctx* c, void* B, void* F) {
   p.tc_bimg = c->tc_bimg;
   p.tc_tblk = c->tc_tblk;
   p.tc_scat_smem = c->tcs.scat_smem;
+  p.tc_yz = c->tcs.yz;
   p.tc_sfa = c->tcs.sfa;
   p.tc_sfb = c->tcs.sfb;
   p.err = &c->sc->err;

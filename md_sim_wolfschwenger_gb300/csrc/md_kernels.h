@@ -68,6 +68,7 @@ struct TcShape {
   int nsb;                      // blocks of 16 particles (per-step operand images)
   int sfa, sfb;                 // structure-factor ring slots (generated, copied)
   int scat_smem;                // dynamic shared memory of the scatter
+  int yz;                       // scatter keeps the Y, Z phases in shared memory
 };
 bool kspace_tc_supported(int kc);
 int kspace_tc_max_kc();  // largest supported kc

@@ -120,9 +120,12 @@ static SfLayout sf_layout(int kc) {
   return SfLayout(ns, k1, 2, 2);
 }
 static size_t sf_smem(int kc) { return (size_t)sf_layout(kc).bytes; }
-static size_t scat_smem(int kc, int nst, int rows) {
+// Scatter shared memory: nst W-tile stages | k rows | (yz) the Y, Z phases
+// of the block's particles [2 (kc + 1)][128] float2.
+static size_t scat_smem(int kc, int nst, int rows, bool yz = false) {
   const int kp = tc_kp(kc);
-  return (size_t)nst * 2 * kScCols * kp * 4 + ((size_t)rows * 8 + 15) / 16 * 16;
+  return (size_t)nst * 2 * kScCols * kp * 4 + ((size_t)rows * 8 + 15) / 16 * 16 +
+         (yz ? (size_t)2 * (kc + 1) * kScParticles * 8 : 0);
 }
 
 // ------------------------------------------------------ per-step operands
@@ -510,6 +513,8 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
   const int tbytes = 2 * kScCols * kp * 4;
   unsigned char* stage0 = smem;
   int2* rows_s = (int2*)(stage0 + NST * tbytes);  // [R] (ny, nz)
+  // Y(|ny|), Z(nz) of the block's particles, [2 K1][128] (when p.tc_yz)
+  float2* yz_s = (float2*)(stage0 + NST * tbytes + ((size_t)R * 8 + 15) / 16 * 16);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool epi = warp < kScEpiWarps;
   const int quarter = warp & 3, cq = (warp >> 2) & 3;  // lane quarter, column quarter
@@ -538,6 +543,8 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
   tc_fence_after();
   const uint32_t tmem = tslot;
   if (epi) {
+    if (p.tc_yz)
+      for (int e = cq; e < 2 * K1; e += 4) yz_s[e * kScParticles + pl] = gtab[(size_t)(K1 + e) * n + ii];
     // A row of this particle into its tensor-memory lane: X(nx), nx = q - kc,
     // at k = 2q (Re), 2q + 1 (Im); hi at column k, lo at kp + k; the four
     // warps of a lane quarter write a quarter of the row's 4-column groups each
@@ -647,9 +654,16 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
         P[sh] = make_float2(0.f, 0.f);
         if (r < R) {
           const int2 rr = rows_s[r];
-          float2 y = gtab[(size_t)(K1 + (rr.x < 0 ? -rr.x : rr.x)) * n + ii];
+          const int ay = rr.x < 0 ? -rr.x : rr.x;
+          float2 y, z;
+          if (p.tc_yz) {
+            y = yz_s[ay * kScParticles + pl];
+            z = yz_s[(K1 + rr.y) * kScParticles + pl];
+          } else {
+            y = gtab[(size_t)(K1 + ay) * n + ii];
+            z = gtab[(size_t)(2 * K1 + rr.y) * n + ii];
+          }
           if (rr.x < 0) y.y = -y.y;
-          const float2 z = gtab[(size_t)(2 * K1 + rr.y) * n + ii];
           P[sh] = make_float2(y.x * z.x - y.y * z.y, y.x * z.y + y.y * z.x);
         }
       }
@@ -773,8 +787,11 @@ TcShape kspace_tc_shape(int kc, int n, int rows, int nsm) {
   s.ns = tc_ns(kc);
   s.kp = tc_kp(kc);
   s.mt = (rows + 63) / 64;
-  s.nst = scat_smem(kc, 3, rows) <= kSmemLimit ? 3 : 2;
-  s.scat_smem = (int)scat_smem(kc, s.nst, rows);
+  // the epilogue's Y, Z phases in shared memory when they fit beside two
+  // stages (the epilogue, not the W-tile copies, bounds the scatter)
+  s.yz = scat_smem(kc, 2, rows, true) <= kSmemLimit ? 1 : 0;
+  s.nst = s.yz ? 2 : (scat_smem(kc, 3, rows) <= kSmemLimit ? 3 : 2);
+  s.scat_smem = (int)scat_smem(kc, s.nst, rows, s.yz != 0);
   s.nt_full = (rows + ScatLayout<true>::RT - 1) / ScatLayout<true>::RT;
   s.nt_field = (rows + ScatLayout<false>::RT - 1) / ScatLayout<false>::RT;
   s.rt_full = ScatLayout<true>::RT;
