@@ -171,6 +171,112 @@ __device__ __forceinline__ void pair_terms(const RealParams& p, T dx, T dy, T dz
   }
 }
 
+// ------------------------------------------------- packed pair terms (FP32)
+// Two pairs at once in the halves of float2 operations (Blackwell's packed
+// FP32 instructions: one issue slot for two FMAs, the FMA rate unchanged), for
+// the mixed path's list loop, which gathers two neighbours per lane and
+// iteration.  The per-pair arithmetic is the one of pair_terms (same
+// operations and rounding per half); special functions stay scalar.
+__device__ __forceinline__ float2 pk(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 pk1(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+struct Acc2 {
+  float2 b0 = {0.f, 0.f}, b1 = {0.f, 0.f}, b2 = {0.f, 0.f}, f0 = {0.f, 0.f}, f1 = {0.f, 0.f}, f2 = {0.f, 0.f};
+  float2 p0 = {0.f, 0.f}, p1 = {0.f, 0.f}, p2 = {0.f, 0.f};
+};
+
+// Pairs A and B: fixed-point pair vectors (dxf..; 2^32 per box length),
+// r2f = |d|^2 in those units, neighbour moments ma, mb; inA, inB: the pair is
+// within rc.  Pairs outside get a harmless distance and weight 0.
+template <bool FULL>
+__device__ __forceinline__ void pair_terms2(const RealParams& p, float2 dxf, float2 dyf, float2 dzf, float2 r2f,
+                                            bool inA, bool inB, float rc2_fix, const float4& mi, const float4& ma,
+                                            const float4& mb, Acc<float>& a, Acc2& a2) {
+  const float sc = 2.3283064365386963e-10f;  // 2^-32 (exact scaling)
+  r2f = pk(inA ? r2f.x : rc2_fix, inB ? r2f.y : rc2_fix);
+  const float2 w = pk(inA ? 1.f : 0.f, inB ? 1.f : 0.f);
+  a.np += (int)inA + (int)inB;
+  const float2 dx = mul2(dxf, pk1(sc)), dy = mul2(dyf, pk1(sc)), dz = mul2(dzf, pk1(sc));
+  const float2 r2 = mul2(r2f, pk1(sc * sc));
+  const float2 ir0 = pk(rsqrtf(r2.x), rsqrtf(r2.y));
+  const float2 r0 = mul2(r2, ir0);
+  const float2 ux = mul2(dx, ir0), uy = mul2(dy, ir0), uz = mul2(dz, ir0);
+  float2 r = r0, ire = ir0;
+  const float2 dcont = add2(add2(pk1(mi.w), pk(ma.w, mb.w)), pk1((float)p.cont_eps));
+  const bool ovA = inA && r.x < dcont.x, ovB = inB && r.y < dcont.y;
+  if (ovA || ovB) {  // rare: clamp overlapping pairs to contact
+    if (ovA) {
+      if constexpr (FULL) {
+        const float h = 0.5f * (dcont.x - r.x);
+        a.o0 -= h * ux.x;
+        a.o1 -= h * uy.x;
+        a.o2 -= h * uz.x;
+      }
+      r.x = dcont.x;
+      ire.x = __fdividef(1.0f, r.x);
+    }
+    if (ovB) {
+      if constexpr (FULL) {
+        const float h = 0.5f * (dcont.y - r.y);
+        a.o0 -= h * ux.y;
+        a.o1 -= h * uy.y;
+        a.o2 -= h * uz.y;
+      }
+      r.y = dcont.y;
+      ire.y = __fdividef(1.0f, r.y);
+    }
+  }
+  const float2 ire2 = mul2(ire, ire), re2 = mul2(r, r);
+  const float2 ee = mul2(pk1(-(float)p.al2), re2);
+  const float2 e = pk(__expf(ee.x), __expf(ee.y));
+  // erfc (Numerical Recipes erfcc, as erfc_nr)
+  const float2 z = mul2(pk1((float)p.alpha), r);
+  const float2 den = fma2(pk1(0.5f), z, pk1(1.0f));
+  const float2 tt = pk(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
+  float2 q = pk1(0.17087277f);
+  q = fma2(q, tt, pk1(-0.82215223f));
+  q = fma2(q, tt, pk1(1.48851587f));
+  q = fma2(q, tt, pk1(-1.13520398f));
+  q = fma2(q, tt, pk1(0.27886807f));
+  q = fma2(q, tt, pk1(-0.18628806f));
+  q = fma2(q, tt, pk1(0.09678418f));
+  q = fma2(q, tt, pk1(0.37409196f));
+  q = fma2(q, tt, pk1(1.00002368f));
+  q = fma2(q, tt, pk1(-1.26551223f));
+  const float2 erfcv = mul2(mul2(tt, e), pk(__expf(q.x), __expf(q.y)));
+  const float2 t = mul2(mul2(pk1((float)p.c2a), e), ire2);
+  const float2 a1 = mul2(fma2(mul2(erfcv, ire2), ire, t), w);
+  const float2 tw = mul2(t, w);
+  const float2 a2c = fma2(mul2(pk1(3.f), a1), ire2, mul2(pk1(2.f * (float)p.al2), tw));
+  const float2 d1 = fma2(pk1(mi.z), uz, fma2(pk1(mi.y), uy, mul2(pk1(mi.x), ux)));
+  const float2 mjx = pk(ma.x, mb.x), mjy = pk(ma.y, mb.y), mjz = pk(ma.z, mb.z);
+  const float2 d2 = fma2(mjz, uz, fma2(mjy, uy, mul2(mjx, ux)));
+  const float2 c1 = mul2(mul2(a2c, d2), re2);
+  a2.b0 = add2(a2.b0, sub2(mul2(c1, ux), mul2(a1, mjx)));
+  a2.b1 = add2(a2.b1, sub2(mul2(c1, uy), mul2(a1, mjy)));
+  a2.b2 = add2(a2.b2, sub2(mul2(c1, uz), mul2(a1, mjz)));
+  if constexpr (FULL) {
+    const float2 a3 = fma2(mul2(pk1(5.f), a2c), ire2, mul2(pk1(4.f * (float)p.al4), tw));
+    const float2 m12 = fma2(pk1(mi.z), mjz, fma2(pk1(mi.y), mjy, mul2(pk1(mi.x), mjx)));
+    const float2 s1 = mul2(sub2(mul2(a2c, m12), mul2(mul2(mul2(a3, d1), d2), re2)), r);
+    const float2 s2 = mul2(a2c, r);
+    const float2 vx = fma2(s1, ux, mul2(s2, fma2(d2, pk1(mi.x), mul2(d1, mjx))));
+    const float2 vy = fma2(s1, uy, mul2(s2, fma2(d2, pk1(mi.y), mul2(d1, mjy))));
+    const float2 vz = fma2(s1, uz, mul2(s2, fma2(d2, pk1(mi.z), mul2(d1, mjz))));
+    a2.f0 = sub2(a2.f0, vx);
+    a2.f1 = sub2(a2.f1, vy);
+    a2.f2 = sub2(a2.f2, vz);
+    const float2 rux = mul2(r, ux);
+    a2.p0 = fma2(rux, vy, a2.p0);
+    a2.p1 = fma2(rux, vz, a2.p1);
+    a2.p2 = fma2(mul2(r, uy), vz, a2.p2);
+  }
+}
+
 // Own coordinates of sorted particle k.
 template <typename T>
 struct Self {
@@ -369,6 +475,7 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
   const int k = bx * kRealWarps + wib;
   if (k >= p.n) return;  // whole warp; no block-level synchronisation below
   Acc<T> a;
+  Acc2 a2;  // packed sums (mixed path list loop)
   const T4 mi = ((const T4*)p.s.mu)[k];
   const Self<T> me = load_self<T, COAT>(p, k);
   const float rc2_fix = (float)(p.rc2 * 18446744073709551616.0);  // (rc / (L 2^-32))^2
@@ -427,8 +534,20 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
         jb_n = tb + 64 < cnt ? lst[tb + 64] : k;
         const int4 sa = p.s.xi[ja], sb = p.s.xi[jb];
         const T4 ma = ((const T4*)p.s.mu)[ja], mb = ((const T4*)p.s.mu)[jb];
-        if (va) eval_loaded(sa, ma);
-        if (vb) eval_loaded(sb, mb);
+        if constexpr (!COAT && !FULL) {
+          // field pass: both neighbours in the halves of packed FP32
+          // operations (the field + force pass stays scalar: packed, it needs
+          // 80 registers and loses a quarter of its resident warps)
+          const float2 dxf = pk((float)(sa.x - me.si.x), (float)(sb.x - me.si.x));
+          const float2 dyf = pk((float)(sa.y - me.si.y), (float)(sb.y - me.si.y));
+          const float2 dzf = pk((float)(sa.z - me.si.z), (float)(sb.z - me.si.z));
+          const float2 r2f = fma2(dzf, dzf, fma2(dyf, dyf, mul2(dxf, dxf)));
+          const bool inA = va && r2f.x < rc2_fix, inB = vb && r2f.y < rc2_fix;
+          if (inA || inB) pair_terms2<FULL>(p, dxf, dyf, dzf, r2f, inA, inB, rc2_fix, mi, ma, mb, a, a2);
+        } else {
+          if (va) eval_loaded(sa, ma);
+          if (vb) eval_loaded(sb, mb);
+        }
       }
     } else {
       int jn = lane < cnt ? lst[lane] : 0;
@@ -458,6 +577,11 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
     if (tail - head > 0) flush(tail - head);
   }
 
+  if constexpr (F32 && !FULL && !COAT) {
+    a.b0 += a2.b0.x + a2.b0.y;
+    a.b1 += a2.b1.x + a2.b1.y;
+    a.b2 += a2.b2.x + a2.b2.y;
+  }
   a.b0 = warp_sum(a.b0);
   a.b1 = warp_sum(a.b1);
   a.b2 = warp_sum(a.b2);
