@@ -55,7 +55,10 @@
 
 namespace md {
 
-constexpr int kRealWarps = 8;  // warps (particles) per block
+constexpr int kRealWarps = 8;  // warps (particles) per block: list build, full pass, packed launches
+// warps per block of the single-system field pass (its packed pair maths
+// needs fewer registers; smaller blocks give finer occupancy steps)
+constexpr int kFieldWarps = 4;
 
 template <typename T>
 struct Acc {
@@ -256,9 +259,18 @@ __device__ __forceinline__ void pair_terms2(const RealParams& p, float2 dxf, flo
   const float2 mjx = pk(ma.x, mb.x), mjy = pk(ma.y, mb.y), mjz = pk(ma.z, mb.z);
   const float2 d2 = fma2(mjz, uz, fma2(mjy, uy, mul2(mjx, ux)));
   const float2 c1 = mul2(mul2(a2c, d2), re2);
-  a2.b0 = add2(a2.b0, sub2(mul2(c1, ux), mul2(a1, mjx)));
-  a2.b1 = add2(a2.b1, sub2(mul2(c1, uy), mul2(a1, mjy)));
-  a2.b2 = add2(a2.b2, sub2(mul2(c1, uz), mul2(a1, mjz)));
+  if constexpr (FULL) {
+    // field + force: the sums stay scalar (A then B), fewer live registers
+    const float2 bx = sub2(mul2(c1, ux), mul2(a1, mjx)), by = sub2(mul2(c1, uy), mul2(a1, mjy));
+    const float2 bz = sub2(mul2(c1, uz), mul2(a1, mjz));
+    a.b0 = (a.b0 + bx.x) + bx.y;
+    a.b1 = (a.b1 + by.x) + by.y;
+    a.b2 = (a.b2 + bz.x) + bz.y;
+  } else {
+    a2.b0 = add2(a2.b0, sub2(mul2(c1, ux), mul2(a1, mjx)));
+    a2.b1 = add2(a2.b1, sub2(mul2(c1, uy), mul2(a1, mjy)));
+    a2.b2 = add2(a2.b2, sub2(mul2(c1, uz), mul2(a1, mjz)));
+  }
   if constexpr (FULL) {
     const float2 a3 = fma2(mul2(pk1(5.f), a2c), ire2, mul2(pk1(4.f * (float)p.al4), tw));
     const float2 m12 = fma2(pk1(mi.z), mjz, fma2(pk1(mi.y), mjy, mul2(pk1(mi.x), mjx)));
@@ -267,13 +279,13 @@ __device__ __forceinline__ void pair_terms2(const RealParams& p, float2 dxf, flo
     const float2 vx = fma2(s1, ux, mul2(s2, fma2(d2, pk1(mi.x), mul2(d1, mjx))));
     const float2 vy = fma2(s1, uy, mul2(s2, fma2(d2, pk1(mi.y), mul2(d1, mjy))));
     const float2 vz = fma2(s1, uz, mul2(s2, fma2(d2, pk1(mi.z), mul2(d1, mjz))));
-    a2.f0 = sub2(a2.f0, vx);
-    a2.f1 = sub2(a2.f1, vy);
-    a2.f2 = sub2(a2.f2, vz);
-    const float2 rux = mul2(r, ux);
-    a2.p0 = fma2(rux, vy, a2.p0);
-    a2.p1 = fma2(rux, vz, a2.p1);
-    a2.p2 = fma2(mul2(r, uy), vz, a2.p2);
+    a.f0 = (a.f0 - vx.x) - vx.y;
+    a.f1 = (a.f1 - vy.x) - vy.y;
+    a.f2 = (a.f2 - vz.x) - vz.y;
+    const float2 rux = mul2(r, ux), ruy = mul2(r, uy);
+    a.p0 = fmaf(rux.y, vy.y, fmaf(rux.x, vy.x, a.p0));
+    a.p1 = fmaf(rux.y, vz.y, fmaf(rux.x, vz.x, a.p1));
+    a.p2 = fmaf(ruy.y, vz.y, fmaf(ruy.x, vz.x, a.p2));
   }
 }
 
@@ -466,13 +478,13 @@ __device__ __forceinline__ void nbr_scan(const RealParams& p) {
 
 // ------------------------------------------------------------ evaluation
 
-template <typename T, bool FULL, bool COAT>
+template <typename T, bool FULL, bool COAT, int NW = kRealWarps>
 __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
   using T4 = typename V4<T>::t;
   constexpr bool F32 = std::is_same<T, float>::value;
-  __shared__ float4 q[kRealWarps][64];
+  __shared__ float4 q[NW][64];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int k = bx * kRealWarps + wib;
+  const int k = bx * NW + wib;
   if (k >= p.n) return;  // whole warp; no block-level synchronisation below
   Acc<T> a;
   Acc2 a2;  // packed sums (mixed path list loop)
@@ -536,8 +548,8 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
         const T4 ma = ((const T4*)p.s.mu)[ja], mb = ((const T4*)p.s.mu)[jb];
         if constexpr (!COAT && !FULL) {
           // field pass: both neighbours in the halves of packed FP32
-          // operations (the field + force pass stays scalar: packed, it needs
-          // 80 registers and loses a quarter of its resident warps)
+          // operations (packed, the field + force pass needs 71 registers and
+          // loses more to the lower occupancy than it gains)
           const float2 dxf = pk((float)(sa.x - me.si.x), (float)(sb.x - me.si.x));
           const float2 dyf = pk((float)(sa.y - me.si.y), (float)(sb.y - me.si.y));
           const float2 dzf = pk((float)(sa.z - me.si.z), (float)(sb.z - me.si.z));
@@ -631,8 +643,8 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build(RealParams p, int
 }
 __global__ void __launch_bounds__(1024) k_nbr_scan(RealParams p) { nbr_scan(p); }
 template <typename T, bool FULL, bool COAT>
-__global__ void __launch_bounds__(kRealWarps * 32) k_real(RealParams p) {
-  real_eval<T, FULL, COAT>(p, blockIdx.x);
+__global__ void __launch_bounds__((FULL ? kRealWarps : kFieldWarps) * 32) k_real(RealParams p) {
+  real_eval<T, FULL, COAT, FULL ? kRealWarps : kFieldWarps>(p, blockIdx.x);
 }
 
 template <bool FILL>
@@ -679,7 +691,8 @@ int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64
 }
 
 int launch_real(cudaStream_t st, const RealParams& p, bool full, bool fp64) {
-  dim3 grid(real_blocks(p.n)), block(kRealWarps * 32);
+  const int nw = full ? kRealWarps : kFieldWarps;
+  dim3 grid((p.n + nw - 1) / nw), block(nw * 32);
   if (fp64) {
     if (full)
       p.coat ? k_real<double, true, true><<<grid, block, 0, st>>>(p)
