@@ -126,3 +126,22 @@ def test_tc_accuracy_large():
     for k in ("tc", "simt"):
         assert O.rms_rel(out[k][0], out["fp64"][0], bAl) < 1e-6
         assert O.rms_rel(out[k][1], out["fp64"][1], fAl) < 1e-6
+
+
+@pytest.mark.parametrize("n,kc", [(2, 3), (5, 6), (17, 8), (129, 12)])
+def test_tc_small_and_ragged(n, kc):
+    """Partial 16-particle stages, one mostly empty 128-particle scatter
+    block, chunk ends inside a stage block."""
+    ini, g = random_system(n, seed=100 + n, rc_frac=0.4)
+    g["kc"] = kc
+    fAl, bAl, _ = scales(ini, g)
+    ref, s = engines(ini, g)
+    assert s["tc"].kspace_tensor_cores()
+    B0, F0, _ = ref.CompInteractions()
+    Bt, Ft, _ = s["tc"].CompInteractions()
+    Bs, Fs, _ = s["simt"].CompInteractions()
+    assert np.all(np.isfinite(Bt)) and np.all(np.isfinite(Ft))
+    assert O.rms_rel(Bt, B0, bAl) < TOL_MIXED and O.rms_rel(Ft, F0, fAl) < TOL_MIXED
+    # with a handful of particles the k-space (periodic image) field is most
+    # of the field, so the engines' FP32-level differences weigh more
+    assert O.rms_rel(Bt, Bs, bAl) < 5e-6 and O.rms_rel(Ft, Fs, fAl) < 5e-6
