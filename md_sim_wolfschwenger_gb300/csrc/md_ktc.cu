@@ -71,7 +71,7 @@ constexpr int kSfSK = 2 * kSfSC;     // K elements per stage
 constexpr int kSfGenWarps = 16;      // structure factor: operand generators (64 rows x U, V)
 constexpr int kSfIssuers = 4;        // structure factor: MMA-issuing warps (one accumulator each)
 constexpr int kSfThreads = 32 * (kSfGenWarps + 1 + kSfIssuers);  // + copy producer + issuers
-constexpr int kSfMaxSlots = 4;       // deepest operand rings
+constexpr int kSfMaxSlots = 8;       // deepest operand rings
 constexpr int kSfMaxChunk = 512;     // particles per structure-factor chunk (4 accumulators of <= 128)
 constexpr int kTabPad = kSfSC + 1;   // Y, Z block row stride (bank spread)
 constexpr int kTcMaxKc = 25;         // operand bounds: A of the scatter in 256 tensor-memory columns
@@ -104,15 +104,15 @@ static int tc_kp(int kc) { return (2 * (2 * kc + 1) + 7) / 8 * 8; }
 struct SfLayout {
   int na, nb, a, b, t, m, bt, bytes;
   __host__ __device__ SfLayout(int ns, int k1, int na_, int nb_)
-      : na(na_), nb(nb_), a(128 * kSfSK * 4), b(ns * kSfSK * 4), t(2 * k1 * kTabPad * 8), m(kSfSC * 16),
+      : na(na_), nb(nb_), a(128 * kSfSK * 2), b(ns * kSfSK * 2), t(2 * k1 * kTabPad * 8), m(kSfSC * 16),
         bt(2 * b + t + m), bytes(na_ * 2 * a + nb_ * bt) {}
   __host__ __device__ int aslot(int s) const { return (s % na) * 2 * a; }
   __host__ __device__ int btslot(int s) const { return na * 2 * a + (s % nb) * bt; }
 };
-// deepest rings that fit: (4, 4), (4, 3), (3, 3), (2, 3)
+// deepest rings that fit
 static SfLayout sf_layout(int kc) {
   const int ns = tc_ns(kc), k1 = kc + 1;
-  const int opts[4][2] = {{4, 4}, {4, 3}, {3, 3}, {2, 3}};
+  const int opts[6][2] = {{8, 6}, {8, 5}, {8, 4}, {6, 4}, {4, 4}, {4, 3}};
   for (const auto& o : opts) {
     SfLayout l(ns, k1, o[0], o[1]);
     if ((size_t)l.bytes <= kSmemLimit) return l;
@@ -138,7 +138,8 @@ __global__ void __launch_bounds__(256) k_tc_prep(KParams p) {
   const int NS = p.tc_ns, kc = p.kc, K1 = kc + 1, n = p.n;
   const int j0 = sb * kSfSC;
   const float2* gtab = (const float2*)p.tab;
-  unsigned char* bimg = (unsigned char*)(p.tc_bimg + (size_t)sb * 2 * NS * kSfSK);
+  // FP16 tiles [hi, lo][NS][32]: 2 bytes per element
+  unsigned char* bimg = (unsigned char*)p.tc_bimg + (size_t)sb * 2 * NS * kSfSK * 2;
   for (int e = threadIdx.x; e < NS * (kSfSK / 4); e += blockDim.x) {
     // 8 rows x 8 particle pairs per 64 threads: whole 128-byte core-matrix rows
     const int nrow = (e & 7) + 8 * (e >> 6), c = (e >> 3) & 7;
@@ -157,13 +158,11 @@ __global__ void __launch_bounds__(256) k_tc_prep(KParams p) {
         }
       }
     }
-    float4 h4, l4;
-    tf32_split(v[0], h4.x, l4.x);
-    tf32_split(v[1], h4.y, l4.y);
-    tf32_split(v[2], h4.z, l4.z);
-    tf32_split(v[3], h4.w, l4.w);
-    *(float4*)(bimg + cm_off(nrow, 4 * c, kSfSK)) = h4;
-    *(float4*)(bimg + NS * kSfSK * 4 + cm_off(nrow, 4 * c, kSfSK)) = l4;
+    uint2 hi, lo;
+    f16_split2(v[0], v[1], hi.x, lo.x);
+    f16_split2(v[2], v[3], hi.y, lo.y);
+    *(uint2*)(bimg + cm_off16(nrow, 4 * c, kSfSK)) = hi;
+    *(uint2*)(bimg + NS * kSfSK * 2 + cm_off16(nrow, 4 * c, kSfSK)) = lo;
   }
   float2* tb = p.tc_tblk + (size_t)sb * 2 * K1 * kTabPad;
   for (int e = threadIdx.x; e < 2 * K1 * kTabPad; e += blockDim.x) {
@@ -229,7 +228,7 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
         const int j0 = p0 + s * kSfSC, sb = j0 / kSfSC;
         const uint32_t mb = (uint32_t)(min(kSfSC, p1 - j0) * 16);
         mbar_expect_tx(bar, (uint32_t)(2 * L.b + L.t) + mb);
-        bulk_g2s(st, p.tc_bimg + (size_t)sb * 2 * NS * kSfSK, 2 * L.b, bar);
+        bulk_g2s(st, (const unsigned char*)p.tc_bimg + (size_t)sb * 2 * NS * kSfSK * 2, 2 * L.b, bar);
         bulk_g2s(st + 2 * L.b, p.tc_tblk + (size_t)sb * 2 * K1 * kTabPad, L.t, bar);
         bulk_g2s(st + 2 * L.b + L.t, (const float4*)p.s.mu + j0, mb, bar);
       };
@@ -258,23 +257,23 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
     // MMA issuer is: stages is, is + kSfIssuers, ...
     const int is = warp - kSfGenWarps - 1;
     if (lane == 0) {
-      const uint32_t idesc = tc_idesc_tf32(128, NS);
-      const uint32_t sbo = kSfSK * 32;
+      const uint32_t idesc = tc_idesc_f16(128, NS);
+      const uint32_t sbo = kSfSK * 16;  // 8-row groups of kSfSK 2-byte elements
       const uint32_t d = tmem + (uint32_t)is * acols;
       bool ok = true, any = false;
       for (int s = is; s < nstage && ok; s += kSfIssuers) {
         ok = mbar_wait_abort(&full_a[s % kSfA], (s / kSfA) & 1, &abort_flag);
         if (!ok) break;
         tc_fence_after();
-        // descriptors of the slots' tiles; k step ks starts 256 B (16 address units) further
+        // descriptors of the slots' tiles; k step ks (16 elements) starts 256 B (16 address units) further
         const uint64_t dah = tc_desc(smem_u32(smem + L.aslot(s)), 128, sbo), dal = dah + (uint64_t)(L.a >> 4);
         const uint64_t dbh = tc_desc(smem_u32(smem + L.btslot(s)), 128, sbo), dbl = dbh + (uint64_t)(L.b >> 4);
 #pragma unroll
-        for (int ks = 0; ks < kSfSK / 8; ks++) {
+        for (int ks = 0; ks < kSfSK / 16; ks++) {
           const uint64_t o = 16 * ks;
-          tc_mma_tf32(d, dah + o, dbh + o, idesc, any || ks > 0);
-          tc_mma_tf32(d, dah + o, dbl + o, idesc, true);
-          tc_mma_tf32(d, dal + o, dbh + o, idesc, true);
+          tc_mma_f16(d, dah + o, dbh + o, idesc, any || ks > 0);
+          tc_mma_f16(d, dah + o, dbl + o, idesc, true);
+          tc_mma_f16(d, dal + o, dbh + o, idesc, true);
         }
         any = true;
         tc_commit(smem_u32(&bt_empty[s % kSfB]));
@@ -329,19 +328,15 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
           V[2 * h + 1] = mu.x * pi;
         }
       }
-      float4 h4, l4;
-      tf32_split(U[0], h4.x, l4.x);
-      tf32_split(U[1], h4.y, l4.y);
-      tf32_split(U[2], h4.z, l4.z);
-      tf32_split(U[3], h4.w, l4.w);
-      *(float4*)(sa + cm_off(arow, 4 * c, kSfSK)) = h4;
-      *(float4*)(sa + L.a + cm_off(arow, 4 * c, kSfSK)) = l4;
-      tf32_split(V[0], h4.x, l4.x);
-      tf32_split(V[1], h4.y, l4.y);
-      tf32_split(V[2], h4.z, l4.z);
-      tf32_split(V[3], h4.w, l4.w);
-      *(float4*)(sa + cm_off(64 + arow, 4 * c, kSfSK)) = h4;
-      *(float4*)(sa + L.a + cm_off(64 + arow, 4 * c, kSfSK)) = l4;
+      uint2 hi, lo;
+      f16_split2(U[0], U[1], hi.x, lo.x);
+      f16_split2(U[2], U[3], hi.y, lo.y);
+      *(uint2*)(sa + cm_off16(arow, 4 * c, kSfSK)) = hi;
+      *(uint2*)(sa + L.a + cm_off16(arow, 4 * c, kSfSK)) = lo;
+      f16_split2(V[0], V[1], hi.x, lo.x);
+      f16_split2(V[2], V[3], hi.y, lo.y);
+      *(uint2*)(sa + cm_off16(64 + arow, 4 * c, kSfSK)) = hi;
+      *(uint2*)(sa + L.a + cm_off16(64 + arow, 4 * c, kSfSK)) = lo;
       fence_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(&full_a[s % kSfA]);
@@ -815,7 +810,7 @@ TcShape kspace_tc_shape(int kc, int n, int rows, int nsm) {
 }
 
 size_t kspace_tc_image_floats(int kc, int nt) { return (size_t)nt * 2 * kScCols * tc_kp(kc); }
-size_t kspace_tc_bimg_floats(int kc, int nsb) { return (size_t)nsb * 2 * tc_ns(kc) * kSfSK; }
+size_t kspace_tc_bimg_floats(int kc, int nsb) { return (size_t)nsb * tc_ns(kc) * kSfSK; }  // FP16 hi, lo
 size_t kspace_tc_tblk_entries(int kc, int nsb) { return (size_t)nsb * 2 * (kc + 1) * kTabPad; }
 
 int launch_kspace_tc_prep(cudaStream_t st, const KParams& p) {

@@ -13,6 +13,8 @@
 // Every mbarrier wait is bounded: after kWaitCycles it gives up and the
 // caller records an error (no wait can hang the GPU).
 #pragma once
+#include <cuda_fp16.h>
+
 #include <cstdint>
 
 namespace md {
@@ -39,6 +41,38 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_
 // (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
 __host__ __device__ constexpr uint32_t tc_idesc_tf32(int m, int n) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// byte offset of element (r, k) of a K-major no-swizzle tile of 16-bit
+// elements with kt columns (core matrices of 8 rows x 8 elements)
+__host__ __device__ __forceinline__ int cm_off16(int r, int k, int kt) {
+  return (r >> 3) * (kt * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// Instruction descriptor of kind::f16 with FP16 A and B (formats 0) and an
+// FP32 accumulator (bits 4-5 = 1), both K-major.
+__host__ __device__ constexpr uint32_t tc_idesc_f16(int m, int n) {
+  return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T with FP16 operands (K = 16 per MMA).
+__device__ __forceinline__ void tc_mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, bool acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)acc));
+}
+
+// Two FP32 values -> packed FP16 (hi, lo) pairs: hi = round-to-nearest FP16,
+// lo = FP16 of the remainder; hi*y_hi + hi*y_lo + lo*y_hi carries ~21 bits of
+// a product with values of magnitude >= 2^-14 (smaller ones to an absolute
+// 2^-25).  Returned as the 32-bit words of the two packed pairs.
+__device__ __forceinline__ void f16_split2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __half2 h = __floats2half2_rn(a, b);
+  const float2 hf = __half22float2(h);
+  const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.
