@@ -258,34 +258,36 @@ __device__ __forceinline__ void pair_terms2(const RealParams& p, float2 dxf, flo
   const float2 d1 = fma2(pk1(mi.z), uz, fma2(pk1(mi.y), uy, mul2(pk1(mi.x), ux)));
   const float2 mjx = pk(ma.x, mb.x), mjy = pk(ma.y, mb.y), mjz = pk(ma.z, mb.z);
   const float2 d2 = fma2(mjz, uz, fma2(mjy, uy, mul2(mjx, ux)));
-  const float2 c1 = mul2(mul2(a2c, d2), re2);
   if constexpr (FULL) {
-    // field + force: the sums stay scalar (A then B), fewer live registers
-    const float2 bx = sub2(mul2(c1, ux), mul2(a1, mjx)), by = sub2(mul2(c1, uy), mul2(a1, mjy));
-    const float2 bz = sub2(mul2(c1, uz), mul2(a1, mjz));
-    a.b0 = (a.b0 + bx.x) + bx.y;
-    a.b1 = (a.b1 + by.x) + by.y;
-    a.b2 = (a.b2 + bz.x) + bz.y;
+    // field + force: packed coefficients, then each pair assembled in scalar
+    // code (as pair_terms), which keeps fewer values live
+    const float2 a3 = fma2(mul2(pk1(5.f), a2c), ire2, mul2(pk1(4.f * (float)p.al4), tw));
+    auto assemble = [&](float a1s, float a2s, float a3s, float rs, float re2s, float uxs, float uys, float uzs,
+                        float d1s, float d2s, const float4& mj) {
+      const float c1 = a2s * d2s * re2s;
+      a.b0 += c1 * uxs - a1s * mj.x;
+      a.b1 += c1 * uys - a1s * mj.y;
+      a.b2 += c1 * uzs - a1s * mj.z;
+      const float m12 = mi.x * mj.x + mi.y * mj.y + mi.z * mj.z;
+      const float s1 = (a2s * m12 - a3s * d1s * d2s * re2s) * rs;
+      const float s2 = a2s * rs;
+      const float vx = s1 * uxs + s2 * (d2s * mi.x + d1s * mj.x);
+      const float vy = s1 * uys + s2 * (d2s * mi.y + d1s * mj.y);
+      const float vz = s1 * uzs + s2 * (d2s * mi.z + d1s * mj.z);
+      a.f0 -= vx;
+      a.f1 -= vy;
+      a.f2 -= vz;
+      a.p0 += rs * uxs * vy;
+      a.p1 += rs * uxs * vz;
+      a.p2 += rs * uys * vz;
+    };
+    assemble(a1.x, a2c.x, a3.x, r.x, re2.x, ux.x, uy.x, uz.x, d1.x, d2.x, ma);
+    assemble(a1.y, a2c.y, a3.y, r.y, re2.y, ux.y, uy.y, uz.y, d1.y, d2.y, mb);
   } else {
+    const float2 c1 = mul2(mul2(a2c, d2), re2);
     a2.b0 = add2(a2.b0, sub2(mul2(c1, ux), mul2(a1, mjx)));
     a2.b1 = add2(a2.b1, sub2(mul2(c1, uy), mul2(a1, mjy)));
     a2.b2 = add2(a2.b2, sub2(mul2(c1, uz), mul2(a1, mjz)));
-  }
-  if constexpr (FULL) {
-    const float2 a3 = fma2(mul2(pk1(5.f), a2c), ire2, mul2(pk1(4.f * (float)p.al4), tw));
-    const float2 m12 = fma2(pk1(mi.z), mjz, fma2(pk1(mi.y), mjy, mul2(pk1(mi.x), mjx)));
-    const float2 s1 = mul2(sub2(mul2(a2c, m12), mul2(mul2(mul2(a3, d1), d2), re2)), r);
-    const float2 s2 = mul2(a2c, r);
-    const float2 vx = fma2(s1, ux, mul2(s2, fma2(d2, pk1(mi.x), mul2(d1, mjx))));
-    const float2 vy = fma2(s1, uy, mul2(s2, fma2(d2, pk1(mi.y), mul2(d1, mjy))));
-    const float2 vz = fma2(s1, uz, mul2(s2, fma2(d2, pk1(mi.z), mul2(d1, mjz))));
-    a.f0 = (a.f0 - vx.x) - vx.y;
-    a.f1 = (a.f1 - vy.x) - vy.y;
-    a.f2 = (a.f2 - vz.x) - vz.y;
-    const float2 rux = mul2(r, ux), ruy = mul2(r, uy);
-    a.p0 = fmaf(rux.y, vy.y, fmaf(rux.x, vy.x, a.p0));
-    a.p1 = fmaf(rux.y, vz.y, fmaf(rux.x, vz.x, a.p1));
-    a.p2 = fmaf(ruy.y, vz.y, fmaf(ruy.x, vz.x, a.p2));
   }
 }
 
@@ -546,10 +548,9 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
         jb_n = tb + 64 < cnt ? lst[tb + 64] : k;
         const int4 sa = p.s.xi[ja], sb = p.s.xi[jb];
         const T4 ma = ((const T4*)p.s.mu)[ja], mb = ((const T4*)p.s.mu)[jb];
-        if constexpr (!COAT && !FULL) {
-          // field pass: both neighbours in the halves of packed FP32
-          // operations (packed, the field + force pass needs 71 registers and
-          // loses more to the lower occupancy than it gains)
+        if constexpr (!COAT) {
+          // both neighbours in the halves of packed FP32 operations (the
+          // field + force pass assembles each pair in scalar code)
           const float2 dxf = pk((float)(sa.x - me.si.x), (float)(sb.x - me.si.x));
           const float2 dyf = pk((float)(sa.y - me.si.y), (float)(sb.y - me.si.y));
           const float2 dzf = pk((float)(sa.z - me.si.z), (float)(sb.z - me.si.z));
@@ -643,8 +644,8 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build(RealParams p, int
 }
 __global__ void __launch_bounds__(1024) k_nbr_scan(RealParams p) { nbr_scan(p); }
 template <typename T, bool FULL, bool COAT>
-__global__ void __launch_bounds__((FULL ? kRealWarps : kFieldWarps) * 32) k_real(RealParams p) {
-  real_eval<T, FULL, COAT, FULL ? kRealWarps : kFieldWarps>(p, blockIdx.x);
+__global__ void __launch_bounds__(((FULL && COAT) ? kRealWarps : kFieldWarps) * 32) k_real(RealParams p) {
+  real_eval<T, FULL, COAT, (FULL && COAT) ? kRealWarps : kFieldWarps>(p, blockIdx.x);
 }
 
 template <bool FILL>
@@ -691,7 +692,7 @@ int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64
 }
 
 int launch_real(cudaStream_t st, const RealParams& p, bool full, bool fp64) {
-  const int nw = full ? kRealWarps : kFieldWarps;
+  const int nw = (full && p.coat) ? kRealWarps : kFieldWarps;
   dim3 grid((p.n + nw - 1) / nw), block(nw * 32);
   if (fp64) {
     if (full)
