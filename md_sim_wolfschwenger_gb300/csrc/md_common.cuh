@@ -81,6 +81,39 @@ struct Task {
 };
 
 // ------------------------------------------------------- real space
+// FP32 loop constants of the packed pair terms (mixed path), computed once on
+// the host: the pair loop reads them from the kernel parameters, so nothing
+// in it is recomputed from the FP64 fields (GB300's FP64 rate is ~1/64 of
+// FP32).  Pair vectors arrive in the fixed-point unit (2^-32 box lengths):
+// d_fix = 2^32 d, r2f = 2^64 r^2; the unit scale and the exp -> 2^x
+// conversion are folded into the factors.
+struct PairK {
+  float ke;     // -alpha^2 log2(e) 2^-64: exp(-alpha^2 r^2) = 2^(ke r2f)
+  float kz;     // alpha 2^-32 / 2: erfc denominator 1 + alpha r / 2 = 1 + kz r_fix
+  float c2a;    // 2 alpha / sqrt(pi)
+  float ka2n;   // -3 2^-64 and -2 alpha^2 2^-64: field-pass a2 r^2 from a1, t
+  float kt2n;   //   with the pair weight negated
+  float al2x2;  // 2 alpha^2
+  float al4x4;  // 4 alpha^4
+  float eps;    // contact offset
+  float rc2f;   // rc^2 2^64: the cutoff test on r2f
+};
+inline PairK make_pair_consts(double alpha, double c2a, double cont_eps, double rc2) {
+  const double s64 = 5.421010862427522e-20;  // 2^-64
+  const double al2 = alpha * alpha;
+  PairK k;
+  k.ke = (float)(-al2 * 1.4426950408889634 * s64);
+  k.kz = (float)(0.5 * alpha * 2.3283064365386963e-10);
+  k.c2a = (float)c2a;
+  k.ka2n = (float)(-3.0 * s64);
+  k.kt2n = (float)(-2.0 * al2 * s64);
+  k.al2x2 = (float)(2.0 * al2);
+  k.al4x4 = (float)(4.0 * al2 * al2);
+  k.eps = (float)cont_eps;
+  k.rc2f = (float)(rc2 * 18446744073709551616.0);
+  return k;
+}
+
 struct RealParams {
   int n;
   CellGrid grid;
@@ -89,6 +122,7 @@ struct RealParams {
   double c2a;            // 2 alpha / sqrt(pi)
   double al2, al4;       // alpha^2, alpha^4
   double cont_eps;       // 1e-10 m / L (contact offset, interaction.cpp:120)
+  PairK pk;              // FP32 constants of the packed pair terms
   // coating potentials (src/interaction.cpp:766-832), box units / F_unit
   int coat;
   double rcut_sr2;       // (rCutSR / L)^2

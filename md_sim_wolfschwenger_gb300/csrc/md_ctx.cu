@@ -119,6 +119,7 @@ RealParams real_params(md_ctx* c, void* B, void* F, void* ov) {
   p.rc2 = rcb * rcb;
   const double rt = rcb * (1.0 + 1e-6) + 2e-7;
   p.rc2_test = rt * rt;
+  p.pk = make_pair_consts(a, 2.0 * a * g.irPi, 1e-10 / L, p.rc2);
   p.c2a = 2.0 * a * g.irPi;
   p.al2 = a * a;
   p.al4 = p.al2 * p.al2;
@@ -370,9 +371,8 @@ static int issue_step(md_ctx* c, double dt) {
   l += launch_heun1(c->stream, int_params(c, dt, c->Br, c->Bk), fp64(c));
   l += issue_field(c);
   mark(c, MD_SEG_HEUN2);
-  l += launch_heun2(c->stream, int_params(c, dt, c->Br2, c->Bk2), fp64(c));
-  mark(c, MD_SEG_OBS);
-  l += launch_obs(c->stream, obs_params(c, dt));
+  l += launch_heun2_obs(c->stream, int_params(c, dt, c->Br2, c->Bk2), obs_params(c, dt), &c->sc->done, fp64(c));
+  mark(c, MD_SEG_OBS);  // the records are taken inside the stage-2 launch
   mark(c, MD_NSEG);
   return l;
 }

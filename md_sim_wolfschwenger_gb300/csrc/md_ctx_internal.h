@@ -23,7 +23,7 @@ struct DevScalars {
   long long step;
   long long nrec;
   int err;
-  int pad;
+  unsigned done;  // blocks of the fused stage-2 + records kernel that finished (0 between launches)
   double musum[3];
   unsigned long long pairs;
   StepFlags flags;

@@ -28,6 +28,7 @@
 namespace md {
 
 constexpr int kIntThreads = 256;
+static_assert(kIntThreads >= 7 * 32, "one warp per step record in the block sums");
 
 __device__ __forceinline__ double ext_field_z(const IntParams& p, double t) {
   if (p.field_kind == 1) return p.fieldAmp * sinpi(2.0 * p.fieldFreq * t);
@@ -152,9 +153,16 @@ __device__ __forceinline__ void heun1(const IntParams& p, int bx) {
 // step-start force plus thermal force fth and the overlap push, the single
 // wrap (IntegrationTrans + ApplyBoundaryCondArr); unwrapped MSD, m_z and the
 // pressure partials into acc; squared displacement since the last list build.
+//
+// GB300 runs FP64 at 1/64 of the FP32 rate, so FP64 is spent only where the
+// value needs it (positions, MSD).  The multiples of L that wrap and unwrap
+// are integers taken from FP32 quotients that sit next to an integer (a
+// step moves a particle far less than L / 2), so they equal the FP64
+// round(.../L) of the reference; the displacement since the list build only
+// feeds the rebuild test and is FP32.
 template <typename T>
 __device__ __forceinline__ void finish_particle(const IntParams& p, int i, int r, const T mn[3], const T en[3],
-                                                const T fth[3], double acc[7], double& disp2) {
+                                                const T fth[3], double acc[7], float& disp2) {
   const int n = p.n;
   acc[4] = p.Ppart[3 * i];
   acc[5] = p.Ppart[3 * i + 1];
@@ -165,6 +173,7 @@ __device__ __forceinline__ void finish_particle(const IntParams& p, int i, int r
   const T* Fk = (const T*)p.Fk;
   const T* ov = (const T*)p.ov;
   const double L = p.L, half = 0.5 * L, dtd = p.dt;
+  const float Lf = (float)L, iLf = 1.0f / Lf;
   const T izt = (T)p.invZt[i];
   bool bad = false;
 #pragma unroll
@@ -174,16 +183,17 @@ __device__ __forceinline__ void finish_particle(const IntParams& p, int i, int r
     p.ea[a * n + i] = (double)ef;
     const T f = (T)(((double)Fr[a * n + r] + (double)Fk[a * n + r]) * p.F_unit) + fth[a];
     double x = p.pos[a * n + i] + (double)ov[a * n + r] * L + dtd * (double)(f * izt);
-    x -= L * (double)(x > half);
-    x += L * (double)(x < -half);
+    if (x > half) x -= L;
+    if (x < -half) x += L;
     p.pos[a * n + i] = x;
     if (p.xbuild) {
-      double db = x - p.xbuild[a * n + i];
-      db -= L * round(db / L);
+      float db = (float)(x - p.xbuild[a * n + i]);
+      db -= Lf * rintf(db * iLf);
       disp2 += db * db;
     }
     double tp = p.truePos[a * n + i];
-    tp = x + round((tp - x) / L) * L;
+    const float wraps = rintf((float)(tp - x) * iLf);
+    tp = x + (double)wraps * L;
     p.truePos[a * n + i] = tp;
     const double d = tp - p.posRef[a * n + i];
     acc[a] = d * d;
@@ -194,25 +204,28 @@ __device__ __forceinline__ void finish_particle(const IntParams& p, int i, int r
 }
 
 // Block sums of the step records and the largest displacement since the
-// last list build (every thread of the block calls this).
-__device__ __forceinline__ void step_block_sums(const IntParams& p, int bx, const double acc[7], double disp2) {
+// last list build (every thread of the block calls this).  The seven sums
+// go through shared memory: warp q adds column q's 256 values with 7 + 5
+// FP64 additions per lane (a butterfly per quantity and warp would take
+// 7 x 5 per warp).
+__device__ __forceinline__ void step_block_sums(const IntParams& p, int bx, const double acc[7], float disp2) {
   if (p.flags) {
-    float d = (float)(sqrt(disp2) / p.L);
+    float d = sqrtf(disp2) * (1.0f / (float)p.L);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_xor_sync(kFull, d, o));
     if ((threadIdx.x & 31) == 0 && d > 0.f) atomicMax(&p.flags->maxdisp, __float_as_uint(d));
   }
-  __shared__ double red[7][kIntThreads / 32];
+  __shared__ double red[7][kIntThreads];
 #pragma unroll
-  for (int q = 0; q < 7; q++) {
-    const double v = warp_sum(acc[q]);
-    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v;
-  }
+  for (int q = 0; q < 7; q++) red[q][threadIdx.x] = acc[q];
   __syncthreads();
-  if (threadIdx.x < 7) {
-    double s = 0;
-    for (int w = 0; w < kIntThreads / 32; w++) s += red[threadIdx.x][w];
-    p.obs_part[7 * bx + threadIdx.x] = s;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (w < 7) {
+    double s = red[w][l];
+#pragma unroll
+    for (int k = 1; k < kIntThreads / 32; k++) s += red[w][l + 32 * k];
+    s = warp_sum(s);
+    if (l == 0) p.obs_part[7 * bx + w] = s;
   }
 }
 
@@ -221,7 +234,7 @@ __device__ __forceinline__ void heun2(const IntParams& p, int bx) {
   const int i = bx * kIntThreads + threadIdx.x;
   const int n = p.n;
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  double disp2 = 0;  // squared displacement since the last neighbour-list build
+  float disp2 = 0;  // squared displacement since the last neighbour-list build
   if (i < n) {
     const int r = p.s.rank[i];
     const T* th = (const T*)p.th;
@@ -258,7 +271,7 @@ __device__ __forceinline__ void obs(const ObsParams& p) {
   __shared__ double red[7][8];
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < p.nblk_int; b += blockDim.x)
-    for (int q = 0; q < 7; q++) acc[q] += p.obs_part[7 * b + q];
+    for (int q = 0; q < 7; q++) acc[q] += __ldcg(p.obs_part + 7 * b + q);
   for (int q = 0; q < 7; q++) {
     const double v = warp_sum(acc[q]);
     if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v;
@@ -293,11 +306,24 @@ template <typename T>
 __global__ void __launch_bounds__(kIntThreads) k_heun1(IntParams p) {
   heun1<T>(p, blockIdx.x);
 }
-template <typename T>
-__global__ void __launch_bounds__(kIntThreads) k_heun2(IntParams p) {
-  heun2<T>(p, blockIdx.x);
-}
 __global__ void __launch_bounds__(256) k_obs(ObsParams p) { obs(p); }
+
+// Stage 2 and the step records in one launch: the block that finishes last
+// (counted in *done) sums the blocks' partials in block order, so the
+// records do not depend on which block that is, and clears the counter.
+template <typename T>
+__global__ void __launch_bounds__(kIntThreads) k_heun2_obs(IntParams p, ObsParams o, unsigned* done) {
+  heun2<T>(p, blockIdx.x);
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  obs(o);
+  if (threadIdx.x == 0) *done = 0;
+}
 
 __global__ void __launch_bounds__(kIntThreads, 4) k_heun1_packed(const IntParams* __restrict__ ps,
                                                              const Task* __restrict__ tk) {
@@ -467,7 +493,7 @@ __global__ void __launch_bounds__(kIntThreads) k_rk_accept(RKStage q) {
   const int i = blockIdx.x * kIntThreads + threadIdx.x;
   const int n = p.n;
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  double disp2 = 0;
+  float disp2 = 0;
   if (i < n) {
     const int r = p.s.rank[i];
     T mn[3], en[3], z[9], fth[3];
@@ -526,11 +552,11 @@ int launch_heun1(cudaStream_t st, const IntParams& p, bool fp64) {
   return 1;
 }
 
-int launch_heun2(cudaStream_t st, const IntParams& p, bool fp64) {
+int launch_heun2_obs(cudaStream_t st, const IntParams& p, const ObsParams& o, unsigned* done, bool fp64) {
   if (fp64)
-    k_heun2<double><<<int_blocks(p.n), kIntThreads, 0, st>>>(p);
+    k_heun2_obs<double><<<int_blocks(p.n), kIntThreads, 0, st>>>(p, o, done);
   else
-    k_heun2<float><<<int_blocks(p.n), kIntThreads, 0, st>>>(p);
+    k_heun2_obs<float><<<int_blocks(p.n), kIntThreads, 0, st>>>(p, o, done);
   return 1;
 }
 

@@ -91,8 +91,9 @@ int scatter_particles(int kc, bool fp64);
 
 // Integrator.
 int launch_heun1(cudaStream_t st, const IntParams& p, bool fp64);
-int launch_heun2(cudaStream_t st, const IntParams& p, bool fp64);
 int launch_obs(cudaStream_t st, const ObsParams& p);
+// Stage 2 with the step records (k_obs) fused: done = a zeroed block counter.
+int launch_heun2_obs(cudaStream_t st, const IntParams& p, const ObsParams& o, unsigned* done, bool fp64);
 int launch_heun1_packed(cudaStream_t st, const IntParams* ps, const Packed& n256);
 int launch_heun2_packed(cudaStream_t st, const IntParams* ps, const Packed& n256);
 int launch_obs_packed(cudaStream_t st, const ObsParams* ps, int R);

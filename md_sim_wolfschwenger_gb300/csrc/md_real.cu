@@ -192,26 +192,48 @@ struct Acc2 {
   float2 p0 = {0.f, 0.f}, p1 = {0.f, 0.f}, p2 = {0.f, 0.f};
 };
 
-// Pairs A and B: fixed-point pair vectors (dxf..; 2^32 per box length),
-// r2f = |d|^2 in those units, neighbour moments ma, mb; inA, inB: the pair is
-// within rc.  Pairs outside get a harmless distance and weight 0.
+// Single-instruction approximations (PTX ex2/rsqrt/rcp .approx.ftz); their
+// arguments here are never subnormal, so flushing changes nothing.
+__device__ __forceinline__ float ex2_ftz(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// erfc polynomial of Numerical Recipes' erfcc (the one of erfc_nr) times
+// log2(e), so that 2^q replaces exp(q); the coefficients stay below 2 in
+// magnitude, so the scaling costs no precision.
+__host__ __device__ constexpr float erfc_c(double c) { return (float)(c * 1.4426950408889634); }
+
+// Pairs A and B: fixed-point pair vectors (dxf..), r2f = |d_fix|^2, the
+// neighbour moments ma, mb; inA, inB: the pair is within rc.  Pairs outside
+// get a harmless distance and weight 0.  Same formulas as pair_terms, with
+// the field sums of the field-only pass as two FMAs per component.
 template <bool FULL>
-__device__ __forceinline__ void pair_terms2(const RealParams& p, float2 dxf, float2 dyf, float2 dzf, float2 r2f,
+__device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dxf, float2 dyf, float2 dzf, float2 r2f,
                                             bool inA, bool inB, float rc2_fix, const float4& mi, const float4& ma,
                                             const float4& mb, Acc<float>& a, Acc2& a2) {
   const float sc = 2.3283064365386963e-10f;  // 2^-32 (exact scaling)
   r2f = pk(inA ? r2f.x : rc2_fix, inB ? r2f.y : rc2_fix);
-  const float2 w = pk(inA ? 1.f : 0.f, inB ? 1.f : 0.f);
   a.np += (int)inA + (int)inB;
-  const float2 dx = mul2(dxf, pk1(sc)), dy = mul2(dyf, pk1(sc)), dz = mul2(dzf, pk1(sc));
-  const float2 r2 = mul2(r2f, pk1(sc * sc));
-  const float2 ir0 = pk(rsqrtf(r2.x), rsqrtf(r2.y));
-  const float2 r0 = mul2(r2, ir0);
-  const float2 ux = mul2(dx, ir0), uy = mul2(dy, ir0), uz = mul2(dz, ir0);
-  float2 r = r0, ire = ir0;
-  const float2 dcont = add2(add2(pk1(mi.w), pk(ma.w, mb.w)), pk1((float)p.cont_eps));
+  float2 irf = pk(rsqrt_ftz(r2f.x), rsqrt_ftz(r2f.y));  // 1 / r_fix
+  const float2 ux = mul2(dxf, irf), uy = mul2(dyf, irf), uz = mul2(dzf, irf);
+  float2 rfx = mul2(r2f, irf);  // r_fix
+  float2 r = mul2(rfx, pk1(sc));
+  const float2 dcont = add2(pk1(wdc), pk(ma.w, mb.w));
   const bool ovA = inA && r.x < dcont.x, ovB = inB && r.y < dcont.y;
   if (ovA || ovB) {  // rare: clamp overlapping pairs to contact
+    const float s32 = 4294967296.0f;
     if (ovA) {
       if constexpr (FULL) {
         const float h = 0.5f * (dcont.x - r.x);
@@ -220,7 +242,9 @@ __device__ __forceinline__ void pair_terms2(const RealParams& p, float2 dxf, flo
         a.o2 -= h * uz.x;
       }
       r.x = dcont.x;
-      ire.x = __fdividef(1.0f, r.x);
+      rfx.x = dcont.x * s32;
+      irf.x = rcp_ftz(rfx.x);
+      r2f.x = rfx.x * rfx.x;
     }
     if (ovB) {
       if constexpr (FULL) {
@@ -230,38 +254,41 @@ __device__ __forceinline__ void pair_terms2(const RealParams& p, float2 dxf, flo
         a.o2 -= h * uz.y;
       }
       r.y = dcont.y;
-      ire.y = __fdividef(1.0f, r.y);
+      rfx.y = dcont.y * s32;
+      irf.y = rcp_ftz(rfx.y);
+      r2f.y = rfx.y * rfx.y;
     }
   }
-  const float2 ire2 = mul2(ire, ire), re2 = mul2(r, r);
-  const float2 ee = mul2(pk1(-(float)p.al2), re2);
-  const float2 e = pk(__expf(ee.x), __expf(ee.y));
-  // erfc (Numerical Recipes erfcc, as erfc_nr)
-  const float2 z = mul2(pk1((float)p.alpha), r);
-  const float2 den = fma2(pk1(0.5f), z, pk1(1.0f));
-  const float2 tt = pk(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
-  float2 q = pk1(0.17087277f);
-  q = fma2(q, tt, pk1(-0.82215223f));
-  q = fma2(q, tt, pk1(1.48851587f));
-  q = fma2(q, tt, pk1(-1.13520398f));
-  q = fma2(q, tt, pk1(0.27886807f));
-  q = fma2(q, tt, pk1(-0.18628806f));
-  q = fma2(q, tt, pk1(0.09678418f));
-  q = fma2(q, tt, pk1(0.37409196f));
-  q = fma2(q, tt, pk1(1.00002368f));
-  q = fma2(q, tt, pk1(-1.26551223f));
-  const float2 erfcv = mul2(mul2(tt, e), pk(__expf(q.x), __expf(q.y)));
-  const float2 t = mul2(mul2(pk1((float)p.c2a), e), ire2);
-  const float2 a1 = mul2(fma2(mul2(erfcv, ire2), ire, t), w);
-  const float2 tw = mul2(t, w);
-  const float2 a2c = fma2(mul2(pk1(3.f), a1), ire2, mul2(pk1(2.f * (float)p.al2), tw));
-  const float2 d1 = fma2(pk1(mi.z), uz, fma2(pk1(mi.y), uy, mul2(pk1(mi.x), ux)));
+  const float2 ire = mul2(irf, pk1(4294967296.0f));  // 1 / r
+  const float2 ire2 = mul2(ire, ire);
+  const float2 ee = mul2(pk1(K.ke), r2f);
+  const float2 e = pk(ex2_ftz(ee.x), ex2_ftz(ee.y));  // exp(-alpha^2 r^2)
+  const float2 den = fma2(pk1(K.kz), rfx, pk1(1.0f));
+  const float2 tt = pk(rcp_ftz(den.x), rcp_ftz(den.y));
+  float2 q = pk1(erfc_c(0.17087277));
+  q = fma2(q, tt, pk1(erfc_c(-0.82215223)));
+  q = fma2(q, tt, pk1(erfc_c(1.48851587)));
+  q = fma2(q, tt, pk1(erfc_c(-1.13520398)));
+  q = fma2(q, tt, pk1(erfc_c(0.27886807)));
+  q = fma2(q, tt, pk1(erfc_c(-0.18628806)));
+  q = fma2(q, tt, pk1(erfc_c(0.09678418)));
+  q = fma2(q, tt, pk1(erfc_c(0.37409196)));
+  q = fma2(q, tt, pk1(erfc_c(1.00002368)));
+  q = fma2(q, tt, pk1(erfc_c(-1.26551223)));
+  const float2 erfcv = mul2(mul2(tt, e), pk(ex2_ftz(q.x), ex2_ftz(q.y)));
+  const float2 t = mul2(mul2(pk1(K.c2a), e), ire2);
   const float2 mjx = pk(ma.x, mb.x), mjy = pk(ma.y, mb.y), mjz = pk(ma.z, mb.z);
   const float2 d2 = fma2(mjz, uz, fma2(mjy, uy, mul2(mjx, ux)));
   if constexpr (FULL) {
     // field + force: packed coefficients, then each pair assembled in scalar
     // code (as pair_terms), which keeps fewer values live
-    const float2 a3 = fma2(mul2(pk1(5.f), a2c), ire2, mul2(pk1(4.f * (float)p.al4), tw));
+    const float2 w = pk(inA ? 1.f : 0.f, inB ? 1.f : 0.f);
+    const float2 a1 = mul2(fma2(mul2(erfcv, ire2), ire, t), w);
+    const float2 tw = mul2(t, w);
+    const float2 a2c = fma2(mul2(pk1(3.f), a1), ire2, mul2(pk1(K.al2x2), tw));
+    const float2 a3 = fma2(mul2(pk1(5.f), a2c), ire2, mul2(pk1(K.al4x4), tw));
+    const float2 re2 = mul2(r, r);
+    const float2 d1 = fma2(pk1(mi.z), uz, fma2(pk1(mi.y), uy, mul2(pk1(mi.x), ux)));
     auto assemble = [&](float a1s, float a2s, float a3s, float rs, float re2s, float uxs, float uys, float uzs,
                         float d1s, float d2s, const float4& mj) {
       const float c1 = a2s * d2s * re2s;
@@ -284,10 +311,15 @@ __device__ __forceinline__ void pair_terms2(const RealParams& p, float2 dxf, flo
     assemble(a1.x, a2c.x, a3.x, r.x, re2.x, ux.x, uy.x, uz.x, d1.x, d2.x, ma);
     assemble(a1.y, a2c.y, a3.y, r.y, re2.y, ux.y, uy.y, uz.y, d1.y, d2.y, mb);
   } else {
-    const float2 c1 = mul2(mul2(a2c, d2), re2);
-    a2.b0 = add2(a2.b0, sub2(mul2(c1, ux), mul2(a1, mjx)));
-    a2.b1 = add2(a2.b1, sub2(mul2(c1, uy), mul2(a1, mjy)));
-    a2.b2 = add2(a2.b2, sub2(mul2(c1, uz), mul2(a1, mjz)));
+    // B += a2 (mj.u) r^2 u - a1 mj, with the weight negated (wn = -w): a1n =
+    // -a1, and a2 r^2 = (3 a1 ire2 + 2 alpha^2 t w) r2f 2^-64
+    const float2 wn = pk(inA ? -1.f : 0.f, inB ? -1.f : 0.f);
+    const float2 a1n = mul2(fma2(mul2(erfcv, ire2), ire, t), wn);
+    const float2 a2s = fma2(mul2(pk1(K.ka2n), a1n), ire2, mul2(pk1(K.kt2n), mul2(t, wn)));
+    const float2 c1 = mul2(mul2(a2s, d2), r2f);
+    a2.b0 = fma2(c1, ux, fma2(a1n, mjx, a2.b0));
+    a2.b1 = fma2(c1, uy, fma2(a1n, mjy, a2.b1));
+    a2.b2 = fma2(c1, uz, fma2(a1n, mjz, a2.b2));
   }
 }
 
@@ -492,7 +524,8 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
   Acc2 a2;  // packed sums (mixed path list loop)
   const T4 mi = ((const T4*)p.s.mu)[k];
   const Self<T> me = load_self<T, COAT>(p, k);
-  const float rc2_fix = (float)(p.rc2 * 18446744073709551616.0);  // (rc / (L 2^-32))^2
+  const float rc2_fix = p.pk.rc2f;  // (rc / (L 2^-32))^2
+  const float wdc = (float)mi.w + p.pk.eps;  // own core radius + contact offset
 
   // pair terms with the neighbour's loaded coordinates and moment (mixed path)
   auto eval_loaded = [&](const int4& sj, const T4& mj) {
@@ -556,7 +589,7 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
           const float2 dzf = pk((float)(sa.z - me.si.z), (float)(sb.z - me.si.z));
           const float2 r2f = fma2(dzf, dzf, fma2(dyf, dyf, mul2(dxf, dxf)));
           const bool inA = va && r2f.x < rc2_fix, inB = vb && r2f.y < rc2_fix;
-          if (inA || inB) pair_terms2<FULL>(p, dxf, dyf, dzf, r2f, inA, inB, rc2_fix, mi, ma, mb, a, a2);
+          if (inA || inB) pair_terms2<FULL>(p.pk, wdc, dxf, dyf, dzf, r2f, inA, inB, rc2_fix, mi, ma, mb, a, a2);
         } else {
           if (va) eval_loaded(sa, ma);
           if (vb) eval_loaded(sb, mb);
