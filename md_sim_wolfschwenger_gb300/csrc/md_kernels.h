@@ -65,7 +65,7 @@ struct TcShape {
   int nt_full, nt_field;        // scatter tiles (field + force, field only)
   int rt_full, rt_field;        // k rows per scatter tile
   int chunk, nchunk;            // structure-factor particle chunks
-  int nsb;                      // blocks of 16 particles (per-step operand images)
+  int nsb;                      // structure-factor stages of 32 particles (per-step operand images)
   int sfa, sfb;                 // structure-factor ring slots (generated, copied)
   int scat_smem;                // dynamic shared memory of the scatter
   int yz;                       // scatter keeps the Y, Z phases in shared memory

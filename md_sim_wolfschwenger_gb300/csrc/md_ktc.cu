@@ -34,11 +34,11 @@
 //
 // Kernels:
 //   k_tc_prep    once per step (positions are frozen across the step's
-//                evaluations): the X operand tiles (hi, lo) of every 16
-//                particles in the shared-memory layout of the structure
-//                factor, and their Y, Z phases in blocks.
+//                evaluations): the X operand tiles (hi, lo) of every stage
+//                of 32 particles in the shared-memory layout of the
+//                structure factor, and their Y, Z phases in blocks.
 //   k_sf_tc      grid (M tiles, chunks); 16 warps generate the U, V operand
-//                of 16 particles per stage into a ring of shared-memory
+//                of 32 particles per stage into a ring of shared-memory
 //                slots, one warp bulk-copies each stage's X tiles, tables and
 //                moments into a second ring, 4 warps issue the MMAs (stages
 //                dealt round-robin, one accumulator each, added in a fixed
@@ -57,7 +57,8 @@
 // Pipeline latency, not arithmetic, bounds these kernels on GB300: a stage
 // is released by tcgen05.commit -> mbarrier, and that round trip (~1-2 us,
 // measured with the stage work removed) is long against the ~0.3 us of MMA
-// work per 16-particle stage; the rings hide it only partly.
+// work per 16 particles; stages of 32 particles halve the hand-offs per
+// block, and the rings hide the rest only partly.
 #include "md_common.cuh"
 #include "md_kernels.h"
 #include "md_tc.cuh"
@@ -66,7 +67,7 @@
 
 namespace md {
 
-constexpr int kSfSC = 16;            // particles per structure-factor stage
+constexpr int kSfSC = 32;            // particles per structure-factor stage (a multiple of 16)
 constexpr int kSfSK = 2 * kSfSC;     // K elements per stage
 constexpr int kSfGenWarps = 16;      // structure factor: operand generators (64 rows x U, V)
 constexpr int kSfIssuers = 4;        // structure factor: MMA-issuing warps (one accumulator each)
@@ -74,12 +75,14 @@ constexpr int kSfThreads = 32 * (kSfGenWarps + 1 + kSfIssuers);  // + copy produ
 constexpr int kSfMaxSlots = 8;       // deepest operand rings
 constexpr int kSfMaxChunk = 512;     // particles per structure-factor chunk (4 accumulators of <= 128)
 constexpr int kTabPad = kSfSC + 1;   // Y, Z block row stride (bank spread)
+constexpr int kSfPairs = kSfSC / 2;  // particle pairs per stage (4 K elements each)
+static_assert(kSfSC % 16 == 0, "stages of whole 16-particle generator passes");
 constexpr int kTcMaxKc = 25;         // operand bounds: A of the scatter in 256 tensor-memory columns
 constexpr int kScEpiWarps = 16;      // scatter: 4 warps per tensor-memory lane quarter (tile quarters)
 constexpr int kScThreads = 32 * (kScEpiWarps + 3);  // + copy producer + two MMA issuers
 constexpr int kScParticles = 128;    // particles per scatter block (tensor-memory lanes)
 constexpr int kScCols = 128;         // scatter tile: 128 output columns (MMA N)
-constexpr int kScMaxStages = 3;
+constexpr int kScMaxStages = 4;
 constexpr size_t kSmemLimit = 227 * 1024 - 5 * 1024;  // dynamic shared memory per block (static <= 4 KB)
 
 // Scatter tile: 128 real columns in four quarters of 16 complex columns; a
@@ -109,15 +112,22 @@ struct SfLayout {
   __host__ __device__ int aslot(int s) const { return (s % na) * 2 * a; }
   __host__ __device__ int btslot(int s) const { return na * 2 * a + (s % nb) * bt; }
 };
-// deepest rings that fit
+// Deepest rings that fit.  The generated ring's depth is a multiple of the
+// issuer count: an issuer waits on full_a of its stage s by parity, which is
+// only unambiguous if the slot's previous phase (stage s - na) is already
+// complete, i.e. was this issuer's own earlier stage.  (With na = 3 and four
+// issuers, an issuer could pass the wait one phase early and read a slot
+// that still held stage s - na.)  The copied ring is waited on only by the
+// copy producer and the generators, which take every stage in order.
 static SfLayout sf_layout(int kc) {
   const int ns = tc_ns(kc), k1 = kc + 1;
-  const int opts[6][2] = {{8, 6}, {8, 5}, {8, 4}, {6, 4}, {4, 4}, {4, 3}};
+  const int opts[6][2] = {{8, 6}, {8, 5}, {8, 4}, {4, 4}, {4, 3}, {4, 2}};
+  static_assert(8 % kSfIssuers == 0 && 4 % kSfIssuers == 0, "generated ring depths: multiples of the issuers");
   for (const auto& o : opts) {
     SfLayout l(ns, k1, o[0], o[1]);
     if ((size_t)l.bytes <= kSmemLimit) return l;
   }
-  return SfLayout(ns, k1, 2, 2);
+  return SfLayout(ns, k1, 4, 1);
 }
 static size_t sf_smem(int kc) { return (size_t)sf_layout(kc).bytes; }
 // Scatter shared memory: nst W-tile stages | k rows | (yz) the Y, Z phases
@@ -130,9 +140,10 @@ static size_t scat_smem(int kc, int nst, int rows, bool yz = false) {
 
 // ------------------------------------------------------ per-step operands
 
-// Block per 16 particles: X operand rows 2q = (Re X, -Im X), 2q + 1 =
-// (Im X, Re X) per particle (q = nx + kc; zero beyond 2 kc and beyond n) as
-// hi, lo TF32 tiles [ns][32]; Y(|ny|), Z(nz) of the 16 particles.
+// Block per stage of kSfSC particles: X operand rows 2q = (Re X, -Im X),
+// 2q + 1 = (Im X, Re X) per particle (q = nx + kc; zero beyond 2 kc and
+// beyond n) as FP16 hi, lo tiles [ns][2 kSfSC]; Y(|ny|), Z(nz) of the stage's
+// particles.
 __global__ void __launch_bounds__(256) k_tc_prep(KParams p) {
   const int sb = blockIdx.x;
   const int NS = p.tc_ns, kc = p.kc, K1 = kc + 1, n = p.n;
@@ -141,8 +152,8 @@ __global__ void __launch_bounds__(256) k_tc_prep(KParams p) {
   // FP16 tiles [hi, lo][NS][32]: 2 bytes per element
   unsigned char* bimg = (unsigned char*)p.tc_bimg + (size_t)sb * 2 * NS * kSfSK * 2;
   for (int e = threadIdx.x; e < NS * (kSfSK / 4); e += blockDim.x) {
-    // 8 rows x 8 particle pairs per 64 threads: whole 128-byte core-matrix rows
-    const int nrow = (e & 7) + 8 * (e >> 6), c = (e >> 3) & 7;
+    // 8 rows x kSfPairs particle pairs per 8-row group: whole core-matrix rows
+    const int nrow = (e & 7) + 8 * (e / (8 * kSfPairs)), c = (e >> 3) % kSfPairs;
     const int q = nrow >> 1, par = nrow & 1;
     float v[4] = {0.f, 0.f, 0.f, 0.f};
     if (q <= 2 * kc) {
@@ -287,9 +298,9 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
     }
   } else {
     // generator: row 8 (warp & 7) + (lane & 7) of this M tile (U at m = row,
-    // V at m = 64 + row), particle pair c = (lane >> 3) + 4 (warp >> 3)
+    // V at m = 64 + row), particle pairs c = (lane >> 3) + 4 (warp >> 3) + 8 u
     const int arow = 8 * (warp & 7) + (lane & 7);
-    const int c = (lane >> 3) + 4 * (warp >> 3);  // particles 2c, 2c + 1 -> k = 4c .. 4c + 3
+    const int c0 = (lane >> 3) + 4 * (warp >> 3);  // pair c: particles 2c, 2c + 1 -> k = 4c .. 4c + 3
     const int rg = mtile * 64 + arow;
     const bool rvalid = rg < p.tc_rows;
     const int2 rr = rvalid ? p.tc_row[rg] : make_int2(0, 0);
@@ -311,32 +322,36 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
       const float2* tb = (const float2*)(sbt + 2 * L.b);
       const float4* mus = (const float4*)(sbt + 2 * L.b + L.t);
       const int nval = p1 - (p0 + s * kSfSC);
-      float U[4] = {0.f, 0.f, 0.f, 0.f}, V[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+      for (int u = 0; u < kSfPairs / 8; u++) {
+        const int c = c0 + 8 * u;
+        float U[4] = {0.f, 0.f, 0.f, 0.f}, V[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int j = 2 * c + h;
-        if (rvalid && j < nval) {
-          float2 Y = tb[ay * kTabPad + j];
-          if (ny < 0) Y.y = -Y.y;
-          const float2 Z = tb[(K1 + nz) * kTabPad + j];
-          const float4 mu = mus[j];
-          const float pr = Y.x * Z.x - Y.y * Z.y, pi = Y.x * Z.y + Y.y * Z.x;
-          const float cf = nyf * mu.y + nzf * mu.z;
-          U[2 * h] = cf * pr;
-          U[2 * h + 1] = cf * pi;
-          V[2 * h] = mu.x * pr;
-          V[2 * h + 1] = mu.x * pi;
+        for (int h = 0; h < 2; h++) {
+          const int j = 2 * c + h;
+          if (rvalid && j < nval) {
+            float2 Y = tb[ay * kTabPad + j];
+            if (ny < 0) Y.y = -Y.y;
+            const float2 Z = tb[(K1 + nz) * kTabPad + j];
+            const float4 mu = mus[j];
+            const float pr = Y.x * Z.x - Y.y * Z.y, pi = Y.x * Z.y + Y.y * Z.x;
+            const float cf = nyf * mu.y + nzf * mu.z;
+            U[2 * h] = cf * pr;
+            U[2 * h + 1] = cf * pi;
+            V[2 * h] = mu.x * pr;
+            V[2 * h + 1] = mu.x * pi;
+          }
         }
+        uint2 hi, lo;
+        f16_split2(U[0], U[1], hi.x, lo.x);
+        f16_split2(U[2], U[3], hi.y, lo.y);
+        *(uint2*)(sa + cm_off16(arow, 4 * c, kSfSK)) = hi;
+        *(uint2*)(sa + L.a + cm_off16(arow, 4 * c, kSfSK)) = lo;
+        f16_split2(V[0], V[1], hi.x, lo.x);
+        f16_split2(V[2], V[3], hi.y, lo.y);
+        *(uint2*)(sa + cm_off16(64 + arow, 4 * c, kSfSK)) = hi;
+        *(uint2*)(sa + L.a + cm_off16(64 + arow, 4 * c, kSfSK)) = lo;
       }
-      uint2 hi, lo;
-      f16_split2(U[0], U[1], hi.x, lo.x);
-      f16_split2(U[2], U[3], hi.y, lo.y);
-      *(uint2*)(sa + cm_off16(arow, 4 * c, kSfSK)) = hi;
-      *(uint2*)(sa + L.a + cm_off16(arow, 4 * c, kSfSK)) = lo;
-      f16_split2(V[0], V[1], hi.x, lo.x);
-      f16_split2(V[2], V[3], hi.y, lo.y);
-      *(uint2*)(sa + cm_off16(64 + arow, 4 * c, kSfSK)) = hi;
-      *(uint2*)(sa + L.a + cm_off16(64 + arow, 4 * c, kSfSK)) = lo;
       fence_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(&full_a[s % kSfA]);
@@ -785,7 +800,9 @@ TcShape kspace_tc_shape(int kc, int n, int rows, int nsm) {
   // the epilogue's Y, Z phases in shared memory when they fit beside two
   // stages (the epilogue, not the W-tile copies, bounds the scatter)
   s.yz = scat_smem(kc, 2, rows, true) <= kSmemLimit ? 1 : 0;
-  s.nst = s.yz ? 2 : (scat_smem(kc, 3, rows) <= kSmemLimit ? 3 : 2);
+  // W-tile stages: a multiple of the two issuers, which alternate tiles and
+  // wait on their tile's stage by parity (see sf_layout)
+  s.nst = s.yz ? 2 : (scat_smem(kc, 4, rows) <= kSmemLimit ? 4 : 2);
   s.scat_smem = (int)scat_smem(kc, s.nst, rows, s.yz != 0);
   s.nt_full = (rows + ScatLayout<true>::RT - 1) / ScatLayout<true>::RT;
   s.nt_field = (rows + ScatLayout<false>::RT - 1) / ScatLayout<false>::RT;
