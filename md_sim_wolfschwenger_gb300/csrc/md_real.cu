@@ -230,7 +230,7 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
   const float2 ux = mul2(dxf, irf), uy = mul2(dyf, irf), uz = mul2(dzf, irf);
   float2 rfx = mul2(r2f, irf);  // r_fix
   float2 r = mul2(rfx, pk1(sc));
-  const float2 dcont = add2(pk1(wdc), pk(ma.w, mb.w));
+  const float2 dcont = pk(wdc + ma.w, wdc + mb.w);
   const bool ovA = inA && r.x < dcont.x, ovB = inB && r.y < dcont.y;
   if (ovA || ovB) {  // rare: clamp overlapping pairs to contact
     const float s32 = 4294967296.0f;
@@ -277,8 +277,6 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
   q = fma2(q, tt, pk1(erfc_c(-1.26551223)));
   const float2 erfcv = mul2(mul2(tt, e), pk(ex2_ftz(q.x), ex2_ftz(q.y)));
   const float2 t = mul2(mul2(pk1(K.c2a), e), ire2);
-  const float2 mjx = pk(ma.x, mb.x), mjy = pk(ma.y, mb.y), mjz = pk(ma.z, mb.z);
-  const float2 d2 = fma2(mjz, uz, fma2(mjy, uy, mul2(mjx, ux)));
   if constexpr (FULL) {
     // field + force: packed coefficients, then each pair assembled in scalar
     // code (as pair_terms), which keeps fewer values live
@@ -288,13 +286,16 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
     const float2 a2c = fma2(mul2(pk1(3.f), a1), ire2, mul2(pk1(K.al2x2), tw));
     const float2 a3 = fma2(mul2(pk1(5.f), a2c), ire2, mul2(pk1(K.al4x4), tw));
     const float2 re2 = mul2(r, r);
-    const float2 d1 = fma2(pk1(mi.z), uz, fma2(pk1(mi.y), uy, mul2(pk1(mi.x), ux)));
     auto assemble = [&](float a1s, float a2s, float a3s, float rs, float re2s, float uxs, float uys, float uzs,
-                        float d1s, float d2s, const float4& mj) {
+                        const float4& mj) {
+      // dot products in scalar code: packed, they would first pair up the
+      // two neighbours' moment components
+      const float d1s = mi.x * uxs + mi.y * uys + mi.z * uzs;
+      const float d2s = mj.x * uxs + mj.y * uys + mj.z * uzs;
       const float c1 = a2s * d2s * re2s;
-      a.b0 += c1 * uxs - a1s * mj.x;
-      a.b1 += c1 * uys - a1s * mj.y;
-      a.b2 += c1 * uzs - a1s * mj.z;
+      a.b0 = fmaf(c1, uxs, fmaf(-a1s, mj.x, a.b0));
+      a.b1 = fmaf(c1, uys, fmaf(-a1s, mj.y, a.b1));
+      a.b2 = fmaf(c1, uzs, fmaf(-a1s, mj.z, a.b2));
       const float m12 = mi.x * mj.x + mi.y * mj.y + mi.z * mj.z;
       const float s1 = (a2s * m12 - a3s * d1s * d2s * re2s) * rs;
       const float s2 = a2s * rs;
@@ -308,11 +309,13 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
       a.p1 += rs * uxs * vz;
       a.p2 += rs * uys * vz;
     };
-    assemble(a1.x, a2c.x, a3.x, r.x, re2.x, ux.x, uy.x, uz.x, d1.x, d2.x, ma);
-    assemble(a1.y, a2c.y, a3.y, r.y, re2.y, ux.y, uy.y, uz.y, d1.y, d2.y, mb);
+    assemble(a1.x, a2c.x, a3.x, r.x, re2.x, ux.x, uy.x, uz.x, ma);
+    assemble(a1.y, a2c.y, a3.y, r.y, re2.y, ux.y, uy.y, uz.y, mb);
   } else {
     // B += a2 (mj.u) r^2 u - a1 mj, with the weight negated (wn = -w): a1n =
     // -a1, and a2 r^2 = (3 a1 ire2 + 2 alpha^2 t w) r2f 2^-64
+    const float2 mjx = pk(ma.x, mb.x), mjy = pk(ma.y, mb.y), mjz = pk(ma.z, mb.z);
+    const float2 d2 = fma2(mjz, uz, fma2(mjy, uy, mul2(mjx, ux)));
     const float2 wn = pk(inA ? -1.f : 0.f, inB ? -1.f : 0.f);
     const float2 a1n = mul2(fma2(mul2(erfcv, ire2), ire, t), wn);
     const float2 a2s = fma2(mul2(pk1(K.ka2n), a1n), ire2, mul2(pk1(K.kt2n), mul2(t, wn)));
@@ -589,7 +592,9 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
           const float2 dzf = pk((float)(sa.z - me.si.z), (float)(sb.z - me.si.z));
           const float2 r2f = fma2(dzf, dzf, fma2(dyf, dyf, mul2(dxf, dxf)));
           const bool inA = va && r2f.x < rc2_fix, inB = vb && r2f.y < rc2_fix;
-          if (inA || inB) pair_terms2<FULL>(p.pk, wdc, dxf, dyf, dzf, r2f, inA, inB, rc2_fix, mi, ma, mb, a, a2);
+          // unconditional: nearly every iteration has a pair in range, and
+          // entries out of range carry weight 0
+          pair_terms2<FULL>(p.pk, wdc, dxf, dyf, dzf, r2f, inA, inB, rc2_fix, mi, ma, mb, a, a2);
         } else {
           if (va) eval_loaded(sa, ma);
           if (vb) eval_loaded(sb, mb);
