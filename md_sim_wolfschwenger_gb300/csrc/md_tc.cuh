@@ -166,13 +166,27 @@ __device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait with a suspend-time hint: the thread sleeps until the phase
+// completes or about kSuspendNs pass, instead of spinning on short polls
+// (each poll of many waiting warps costs issue slots of the working ones).
+constexpr uint32_t kSuspendNs = 20000;
+__device__ __forceinline__ bool mbar_try_sleep(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(a), "r"(parity), "n"(kSuspendNs)
+      : "memory");
+  return ok != 0;
+}
+
 // Waits for the phase with the given parity to complete; false after
 // kWaitCycles.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   const uint32_t a = smem_u32(bar);
   if (mbar_try(a, parity)) return true;
   const long long t0 = clock64();
-  while (!mbar_try(a, parity))
+  while (!mbar_try_sleep(a, parity))
     if (clock64() - t0 > kWaitCycles) return false;
   return true;
 }
@@ -183,7 +197,7 @@ __device__ __forceinline__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, 
   const uint32_t a = smem_u32(bar);
   if (mbar_try(a, parity)) return true;
   const long long t0 = clock64();
-  while (!mbar_try(a, parity)) {
+  while (!mbar_try_sleep(a, parity)) {
     if (*abort || clock64() - t0 > kWaitCycles) return false;
   }
   return true;
