@@ -109,8 +109,12 @@ struct SfLayout {
   __host__ __device__ SfLayout(int ns, int k1, int na_, int nb_)
       : na(na_), nb(nb_), a(128 * kSfSK * 2), b(ns * kSfSK * 2), t(2 * k1 * kTabPad * 8), m(kSfSC * 16),
         bt(2 * b + t + m), bytes(na_ * 2 * a + nb_ * bt) {}
-  __host__ __device__ int aslot(int s) const { return (s % na) * 2 * a; }
-  __host__ __device__ int btslot(int s) const { return na * 2 * a + (s % nb) * bt; }
+  // byte offsets of generated slot q and copied slot q (the roles keep the
+  // slot index and phase of their stage as counters: the ring depths are
+  // runtime values, and a division per stage costs the generators as much
+  // as their arithmetic)
+  __host__ __device__ int aslot_at(int q) const { return q * 2 * a; }
+  __host__ __device__ int btslot_at(int q) const { return na * 2 * a + q * bt; }
 };
 // Deepest rings that fit.  The generated ring's depth is a multiple of the
 // issuer count: an issuer waits on full_a of its stage s by parity, which is
@@ -233,9 +237,9 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
   if (warp == kSfGenWarps) {
     // copy producer
     if (lane == 0) {
-      auto issue_copy = [&](int s) {
-        unsigned char* st = smem + L.btslot(s);
-        uint64_t* bar = &full_bt[s % kSfB];
+      auto issue_copy = [&](int s, int q) {  // stage s into copied slot q
+        unsigned char* st = smem + L.btslot_at(q);
+        uint64_t* bar = &full_bt[q];
         const int j0 = p0 + s * kSfSC, sb = j0 / kSfSC;
         const uint32_t mb = (uint32_t)(min(kSfSC, p1 - j0) * 16);
         mbar_expect_tx(bar, (uint32_t)(2 * L.b + L.t) + mb);
@@ -246,15 +250,20 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
       bool ok = true;
       int issued = 0;
       for (int s = 0; s < kSfB && s < nstage; s++) {
-        issue_copy(s);
+        issue_copy(s, s);
         issued = s + 1;
       }
+      int q = 0, ph = 0;  // slot and phase parity of stage s
       for (int s = 0; s + kSfB < nstage && ok; s++) {
         // the copied slot of stage s takes stage s + kSfB once stage s's MMAs are done
-        ok = mbar_wait_abort(&bt_empty[s % kSfB], (s / kSfB) & 1, &abort_flag);
+        ok = mbar_wait_abort(&bt_empty[q], ph, &abort_flag);
         if (!ok) break;
-        issue_copy(s + kSfB);
+        issue_copy(s + kSfB, q);
         issued = s + kSfB + 1;
+        if (++q == kSfB) {
+          q = 0;
+          ph ^= 1;
+        }
       }
       if (!ok) {
         abort_flag = 1;
@@ -272,13 +281,16 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
       const uint32_t sbo = kSfSK * 16;  // 8-row groups of kSfSK 2-byte elements
       const uint32_t d = tmem + (uint32_t)is * acols;
       bool ok = true, any = false;
+      // generated slot qa (kSfA is a multiple of kSfIssuers: exact wraps) and
+      // its phase parity, copied slot qb of stage s
+      int qa = is, pha = 0, qb = is % kSfB;
       for (int s = is; s < nstage && ok; s += kSfIssuers) {
-        ok = mbar_wait_abort(&full_a[s % kSfA], (s / kSfA) & 1, &abort_flag);
+        ok = mbar_wait_abort(&full_a[qa], pha, &abort_flag);
         if (!ok) break;
         tc_fence_after();
         // descriptors of the slots' tiles; k step ks (16 elements) starts 256 B (16 address units) further
-        const uint64_t dah = tc_desc(smem_u32(smem + L.aslot(s)), 128, sbo), dal = dah + (uint64_t)(L.a >> 4);
-        const uint64_t dbh = tc_desc(smem_u32(smem + L.btslot(s)), 128, sbo), dbl = dbh + (uint64_t)(L.b >> 4);
+        const uint64_t dah = tc_desc(smem_u32(smem + L.aslot_at(qa)), 128, sbo), dal = dah + (uint64_t)(L.a >> 4);
+        const uint64_t dbh = tc_desc(smem_u32(smem + L.btslot_at(qb)), 128, sbo), dbl = dbh + (uint64_t)(L.b >> 4);
 #pragma unroll
         for (int ks = 0; ks < kSfSK / 16; ks++) {
           const uint64_t o = 16 * ks;
@@ -287,8 +299,15 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
           tc_mma_f16(d, dal + o, dbh + o, idesc, true);
         }
         any = true;
-        tc_commit(smem_u32(&bt_empty[s % kSfB]));
-        tc_commit(smem_u32(&a_empty[s % kSfA]));
+        tc_commit(smem_u32(&bt_empty[qb]));
+        tc_commit(smem_u32(&a_empty[qa]));
+        qa += kSfIssuers;
+        if (qa >= kSfA) {
+          qa -= kSfA;
+          pha ^= 1;
+        }
+        qb += kSfIssuers;
+        while (qb >= kSfB) qb -= kSfB;
       }
       if (!ok) {
         abort_flag = 1;
@@ -306,9 +325,13 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
     const int2 rr = rvalid ? p.tc_row[rg] : make_int2(0, 0);
     const int ny = rr.x, nz = rr.y, ay = ny < 0 ? -ny : ny;
     const float nyf = (float)ny, nzf = (float)nz;
+    const int yo = ay * kTabPad, zo = (K1 + nz) * kTabPad;  // Y, Z rows in the stage's table block
+    // slots and phase parities of stage s; the a_empty phase that frees the
+    // generated slot for stage s is the one of stage s - kSfA (parity pha ^ 1)
+    int qa = 0, pha = 0, qb = 0, phb = 0;
     for (int s = 0; s < nstage; s++) {
-      bool w = mbar_wait_abort(&full_bt[s % kSfB], (s / kSfB) & 1, &abort_flag);
-      if (w && s >= kSfA) w = mbar_wait_abort(&a_empty[s % kSfA], ((s - kSfA) / kSfA) & 1, &abort_flag);
+      bool w = mbar_wait_abort(&full_bt[qb], phb, &abort_flag);
+      if (w && s >= kSfA) w = mbar_wait_abort(&a_empty[qa], pha ^ 1, &abort_flag);
       w = __all_sync(kFull, w);
       if (!w) {
         if (lane == 0) {
@@ -317,8 +340,8 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
         }
         break;
       }
-      unsigned char* sa = smem + L.aslot(s);
-      const unsigned char* sbt = smem + L.btslot(s);
+      unsigned char* sa = smem + L.aslot_at(qa);
+      const unsigned char* sbt = smem + L.btslot_at(qb);
       const float2* tb = (const float2*)(sbt + 2 * L.b);
       const float4* mus = (const float4*)(sbt + 2 * L.b + L.t);
       const int nval = p1 - (p0 + s * kSfSC);
@@ -330,9 +353,9 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
         for (int h = 0; h < 2; h++) {
           const int j = 2 * c + h;
           if (rvalid && j < nval) {
-            float2 Y = tb[ay * kTabPad + j];
+            float2 Y = tb[yo + j];
             if (ny < 0) Y.y = -Y.y;
-            const float2 Z = tb[(K1 + nz) * kTabPad + j];
+            const float2 Z = tb[zo + j];
             const float4 mu = mus[j];
             const float pr = Y.x * Z.x - Y.y * Z.y, pi = Y.x * Z.y + Y.y * Z.x;
             const float cf = nyf * mu.y + nzf * mu.z;
@@ -354,7 +377,15 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
       }
       fence_async_smem();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&full_a[s % kSfA]);
+      if (lane == 0) mbar_arrive(&full_a[qa]);
+      if (++qa == kSfA) {
+        qa = 0;
+        pha ^= 1;
+      }
+      if (++qb == kSfB) {
+        qb = 0;
+        phb ^= 1;
+      }
     }
   }
   tc_fence_before();
