@@ -183,6 +183,7 @@ struct KParams {
   int tc_nst;            // scatter pipeline stages (2 or 3)
   int tc_chunk, tc_nchunk;  // structure-factor particle chunks (multiple of 16)
   const int2* tc_row;    // [R] (ny, nz)
+  const float4* tc_rowd; // scatter row descriptors (kspace_tc_row_desc)
   const int* tc_kmap;    // [R][2kc + 1] sorted k index, or -1
   float* tc_part;        // [nchunk][mt][ns][128] FP32 chunk partials (column-major tiles)
   float* tc_w;           // scatter operand image [nt][hi, lo][128][kp] (this evaluation's layout)

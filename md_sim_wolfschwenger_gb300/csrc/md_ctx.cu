@@ -224,6 +224,7 @@ KParams k_params(md_ctx* c, void* B, void* F) {
   p.tc_chunk = c->tcs.chunk;
   p.tc_nchunk = c->tcs.nchunk;
   p.tc_row = c->tc_row;
+  p.tc_rowd = c->tc_rowd;
   p.tc_kmap = c->tc_kmap;
   p.tc_part = c->tc_part;
   p.tc_w = F ? c->tc_wfull : c->tc_wfield;
@@ -459,9 +460,10 @@ static int setup_tc(md_ctx* c) {
   int nsm = 148;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
   const md::TcShape t = md::kspace_tc_shape(kc, (int)c->n, R, nsm);
-  void* old[] = {c->tc_row, c->tc_kmap, c->tc_part, c->tc_wfull, c->tc_wfield, c->tc_bimg, c->tc_tblk};
+  void* old[] = {c->tc_row, c->tc_rowd, c->tc_kmap, c->tc_part, c->tc_wfull, c->tc_wfield, c->tc_bimg, c->tc_tblk};
   for (void* q : old) dfree(c, q);
   c->tc_row = nullptr;
+  c->tc_rowd = nullptr;
   c->tc_kmap = nullptr;
   c->tc_part = nullptr;
   c->tc_wfull = c->tc_wfield = nullptr;
@@ -470,6 +472,9 @@ static int setup_tc(md_ctx* c) {
   const size_t wfull = md::kspace_tc_image_floats(kc, t.nt_full), wfield = md::kspace_tc_image_floats(kc, t.nt_field);
   int st;
   if ((st = dalloc(c, &c->tc_row, sizeof(int2) * (size_t)R))) return st;
+  std::vector<float4> rowd((size_t)md::kspace_tc_rows_pad(R));
+  md::kspace_tc_row_desc(rows.data(), R, kc, (int)c->n, t.yz != 0, rowd.data());
+  if ((st = dalloc(c, &c->tc_rowd, sizeof(float4) * rowd.size()))) return st;
   if ((st = dalloc(c, &c->tc_kmap, sizeof(int) * kmap.size()))) return st;
   if ((st = dalloc(c, &c->tc_part, sizeof(float) * (size_t)t.nchunk * t.mt * t.ns * 128))) return st;
   if ((st = dalloc(c, &c->tc_wfull, sizeof(float) * wfull))) return st;
@@ -483,6 +488,7 @@ static int setup_tc(md_ctx* c) {
     c->musum_cap = t.nchunk;
   }
   CK(c, cudaMemcpy(c->tc_row, rows.data(), sizeof(int2) * (size_t)R, cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->tc_rowd, rowd.data(), sizeof(float4) * rowd.size(), cudaMemcpyHostToDevice));
   CK(c, cudaMemcpy(c->tc_kmap, kmap.data(), sizeof(int) * kmap.size(), cudaMemcpyHostToDevice));
   // operand entries of k's outside the sphere or the half space stay zero
   CK(c, cudaMemset(c->tc_wfull, 0, sizeof(float) * wfull));

@@ -118,6 +118,7 @@ struct md_ctx {
   int tc_rows = 0;
   TcShape tcs{};
   int2* tc_row = nullptr;
+  float4* tc_rowd = nullptr;  // scatter row descriptors
   int* tc_kmap = nullptr;
   float* tc_part = nullptr;
   float *tc_wfull = nullptr, *tc_wfield = nullptr;

@@ -74,6 +74,11 @@ bool kspace_tc_supported(int kc);
 int kspace_tc_max_kc();  // largest supported kc
 TcShape kspace_tc_shape(int kc, int n, int rows, int nsm);
 size_t kspace_tc_image_floats(int kc, int nt);  // scatter operand image of nt tiles
+// Scatter row descriptors: R rows padded to whole tiles of both shapes;
+// (ny, nz, Y offset, Z offset bits) per row into out[kspace_tc_rows_pad(R)],
+// offsets into the block's Y, Z copy (yz) or the global phase table.
+int kspace_tc_rows_pad(int R);
+void kspace_tc_row_desc(const int2* rows, int R, int kc, int n, bool yz, float4* out);
 size_t kspace_tc_bimg_floats(int kc, int nsb);   // per-step X operand tiles
 size_t kspace_tc_tblk_entries(int kc, int nsb);  // per-step Y, Z blocks (float2)
 // Per-step operand images (after the phase tables), then per evaluation.

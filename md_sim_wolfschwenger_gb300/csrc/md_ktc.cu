@@ -64,6 +64,7 @@
 #include "md_tc.cuh"
 
 #include <algorithm>
+#include <cstring>
 
 namespace md {
 
@@ -96,6 +97,15 @@ struct ScatLayout {
   // complex column of Q_p of the tile's row sl
   __host__ __device__ static constexpr int ccol(int sl, int pp) { return (sl / RQ) * 16 + (sl % RQ) * P + pp; }
 };
+
+// Row descriptors of the scatter (built once by the host, read with
+// warp-uniform loads): both tile shapes' rows, padded to whole tiles
+// (padding rows have zero W columns).
+__host__ __device__ inline int scat_rows_pad(int R) {
+  const int a = (R + ScatLayout<true>::RT - 1) / ScatLayout<true>::RT * ScatLayout<true>::RT;
+  const int b = (R + ScatLayout<false>::RT - 1) / ScatLayout<false>::RT * ScatLayout<false>::RT;
+  return a > b ? a : b;
+}
 
 static int tc_ns(int kc) { return (2 * (2 * kc + 1) + 15) / 16 * 16; }
 static int tc_kp(int kc) { return (2 * (2 * kc + 1) + 7) / 8 * 8; }
@@ -134,11 +144,11 @@ static SfLayout sf_layout(int kc) {
   return SfLayout(ns, k1, 4, 1);
 }
 static size_t sf_smem(int kc) { return (size_t)sf_layout(kc).bytes; }
-// Scatter shared memory: nst W-tile stages | k rows | (yz) the Y, Z phases
-// of the block's particles [2 (kc + 1)][128] float2.
-static size_t scat_smem(int kc, int nst, int rows, bool yz = false) {
+// Scatter shared memory: nst W-tile stages | (yz) the Y, Z phases of the
+// block's particles [2 (kc + 1)][128] float2.
+static size_t scat_smem(int kc, int nst, int /*rows*/, bool yz = false) {
   const int kp = tc_kp(kc);
-  return (size_t)nst * 2 * kScCols * kp * 4 + ((size_t)rows * 8 + 15) / 16 * 16 +
+  return (size_t)nst * 2 * kScCols * kp * 4 +
          (yz ? (size_t)2 * (kc + 1) * kScParticles * 8 : 0);
 }
 
@@ -553,9 +563,11 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
   const int kp = p.tc_kp, kc = p.kc, K1 = kc + 1, n = p.n, R = p.tc_rows, NT = p.tc_nt, NST = p.tc_nst;
   const int tbytes = 2 * kScCols * kp * 4;
   unsigned char* stage0 = smem;
-  int2* rows_s = (int2*)(stage0 + NST * tbytes);  // [R] (ny, nz)
+  // row descriptors (kspace_tc_row_desc): ny, nz, offsets of Y(|ny|) and
+  // Z(nz) in the phase table this block reads; the sign of ny conjugates Y
+  const float4* __restrict__ rows_d = p.tc_rowd;
   // Y(|ny|), Z(nz) of the block's particles, [2 K1][128] (when p.tc_yz)
-  float2* yz_s = (float2*)(stage0 + NST * tbytes + ((size_t)R * 8 + 15) / 16 * 16);
+  float2* yz_s = (float2*)(stage0 + NST * tbytes);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool epi = warp < kScEpiWarps;
   const int quarter = warp & 3, cq = (warp >> 2) & 3;  // lane quarter, column quarter
@@ -564,7 +576,6 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
   const bool act = epi && i < n;
   const int ii = i < n ? i : n - 1;
   const float2* gtab = (const float2*)p.tab;
-  for (int r = tid; r < R; r += kScThreads) rows_s[r] = p.tc_row[r];
 
   if (tid == 0) {
     for (int q = 0; q < kScMaxStages; q++) {
@@ -691,22 +702,19 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
     auto fetch = [&](int t, float2* P) {
 #pragma unroll
       for (int sh = 0; sh < L::RQ; sh++) {
-        const int r = t * L::RT + cq * L::RQ + sh;
-        P[sh] = make_float2(0.f, 0.f);
-        if (r < R) {
-          const int2 rr = rows_s[r];
-          const int ay = rr.x < 0 ? -rr.x : rr.x;
-          float2 y, z;
-          if (p.tc_yz) {
-            y = yz_s[ay * kScParticles + pl];
-            z = yz_s[(K1 + rr.y) * kScParticles + pl];
-          } else {
-            y = gtab[(size_t)(K1 + ay) * n + ii];
-            z = gtab[(size_t)(2 * K1 + rr.y) * n + ii];
-          }
-          if (rr.x < 0) y.y = -y.y;
-          P[sh] = make_float2(y.x * z.x - y.y * z.y, y.x * z.y + y.y * z.x);
+        const float4 d = __ldg(rows_d + t * L::RT + cq * L::RQ + sh);
+        const int yo = __float_as_int(d.z), zo = __float_as_int(d.w);
+        float2 y, z;
+        if (p.tc_yz) {
+          y = yz_s[yo + pl];
+          z = yz_s[zo + pl];
+        } else {
+          y = gtab[yo + ii];
+          z = gtab[zo + ii];
         }
+        // conj Y for ny < 0: the sign bit of ny onto Im Y
+        y.y = __int_as_float(__float_as_int(y.y) ^ (__float_as_int(d.x) & 0x80000000));
+        P[sh] = make_float2(y.x * z.x - y.y * z.y, y.x * z.y + y.y * z.x);
       }
     };
     float2 Pc[L::RQ];
@@ -734,11 +742,10 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
       float tb0 = 0.f, tb1 = 0.f, tb2 = 0.f, tf0 = 0.f, tf1 = 0.f, tf2 = 0.f;
 #pragma unroll
       for (int sh = 0; sh < L::RQ; sh++) {
-        const int r = t * L::RT + cq * L::RQ + sh;
-        if (r < R) {
-          const int2 rr = rows_s[r];
+        {
+          const float2 nn = __ldg((const float2*)(rows_d + t * L::RT + cq * L::RQ + sh));
           const float pr = Pc[sh].x, pi = Pc[sh].y;
-          const float nyf = (float)rr.x, nzf = (float)rr.y;
+          const float nyf = nn.x, nzf = nn.y;
           const float* qv = v + 2 * L::P * sh;
           const float re0 = pr * qv[0] - pi * qv[1];
           const float re1 = pr * qv[2] - pi * qv[3];
@@ -855,6 +862,23 @@ TcShape kspace_tc_shape(int kc, int n, int rows, int nsm) {
   s.chunk = (int)((((long)n + nch - 1) / nch + kSfSC - 1) / kSfSC * kSfSC);
   s.nchunk = (n + s.chunk - 1) / s.chunk;
   return s;
+}
+
+int kspace_tc_rows_pad(int R) { return scat_rows_pad(R); }
+
+void kspace_tc_row_desc(const int2* rows, int R, int kc, int n, bool yz, float4* out) {
+  const int K1 = kc + 1, ts = yz ? kScParticles : n;  // row stride of the phase table the scatter reads
+  for (int r = 0; r < scat_rows_pad(R); r++) {
+    const int2 rr = r < R ? rows[r] : make_int2(0, 0);
+    const int ay = rr.x < 0 ? -rr.x : rr.x;
+    const int yo = (yz ? ay : K1 + ay) * ts, zo = (yz ? K1 + rr.y : 2 * K1 + rr.y) * ts;
+    float4 d;
+    d.x = (float)rr.x;
+    d.y = (float)rr.y;
+    std::memcpy(&d.z, &yo, 4);
+    std::memcpy(&d.w, &zo, 4);
+    out[r] = d;
+  }
 }
 
 size_t kspace_tc_image_floats(int kc, int nt) { return (size_t)nt * 2 * kScCols * tc_kp(kc); }
