@@ -80,11 +80,23 @@ __device__ __forceinline__ void demag_si(const IntParams& p, int r, R b[3]) {
   const T* Br = (const T*)p.Br;
   const T* Bk = (const T*)p.Bk;
   const T4 mu = ((const T4*)p.s.mu)[r];
-  const double mu3[3] = {(double)mu.x, (double)mu.y, (double)mu.z};
+  if constexpr (std::is_same<R, float>::value) {
+    // mixed integrator: the FP32 stage outputs combined in FP32 (FP64 runs
+    // at ~1/64 of the FP32 rate on GB300; the self term that cancels the
+    // k-space self field is small against the pair fields, so the FP32 sum
+    // loses nothing measurable)
+    const float cs = (float)p.cself, cu = (float)p.csurf, bu = (float)p.B_unit;
+    const float mu3[3] = {(float)mu.x, (float)mu.y, (float)mu.z};
 #pragma unroll
-  for (int a = 0; a < 3; a++) {
-    const double selfsurf = p.cself * mu3[a] - p.csurf * p.musum[a];
-    b[a] = (R)((((double)Br[a * n + r] + (double)Bk[a * n + r]) + selfsurf) * p.B_unit);
+    for (int a = 0; a < 3; a++)
+      b[a] = (((float)Br[a * n + r] + (float)Bk[a * n + r]) + (cs * mu3[a] - cu * (float)p.musum[a])) * bu;
+  } else {
+    const double mu3[3] = {(double)mu.x, (double)mu.y, (double)mu.z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const double selfsurf = p.cself * mu3[a] - p.csurf * p.musum[a];
+      b[a] = (R)((((double)Br[a * n + r] + (double)Bk[a * n + r]) + selfsurf) * p.B_unit);
+    }
   }
 }
 
@@ -181,7 +193,11 @@ __device__ __forceinline__ void finish_particle(const IntParams& p, int i, int r
     const T mf = mn[a] / nm, ef = en[a] / ne;
     p.mm[a * n + i] = (double)mf;
     p.ea[a * n + i] = (double)ef;
-    const T f = (T)(((double)Fr[a * n + r] + (double)Fk[a * n + r]) * p.F_unit) + fth[a];
+    T f;
+    if constexpr (std::is_same<T, float>::value)
+      f = (Fr[a * n + r] + Fk[a * n + r]) * (float)p.F_unit + fth[a];
+    else
+      f = (Fr[a * n + r] + Fk[a * n + r]) * p.F_unit + fth[a];
     double x = p.pos[a * n + i] + (double)ov[a * n + r] * L + dtd * (double)(f * izt);
     if (x > half) x -= L;
     if (x < -half) x += L;
