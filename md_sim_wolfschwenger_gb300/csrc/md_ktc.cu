@@ -64,6 +64,7 @@
 #include "md_tc.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <cstring>
 
 namespace md {
@@ -334,8 +335,54 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
     const bool rvalid = rg < p.tc_rows;
     const int2 rr = rvalid ? p.tc_row[rg] : make_int2(0, 0);
     const int ny = rr.x, nz = rr.y, ay = ny < 0 ? -ny : ny;
-    const float nyf = (float)ny, nzf = (float)nz;
-    const int yo = ay * kTabPad, zo = (K1 + nz) * kTabPad;  // Y, Z rows in the stage's table block
+    // rows beyond R (last M tile) get zero coefficients: their U, V are 0
+    const float nyf = (float)ny, nzf = (float)nz, vsc = rvalid ? 1.f : 0.f;
+    const float ysg = ny < 0 ? -1.f : 1.f;  // conj Y for ny < 0
+    // this thread's first particle in the stage's Y, Z rows and moments
+    const int yo = ay * kTabPad + 2 * c0, zo = (K1 + nz) * kTabPad + 2 * c0, mo = 2 * c0;
+    // store offset of pair c0 in the U rows; pair c0 + 8 u is kPairStep u
+    // bytes further (4 core matrices along K), the V rows kVRows further
+    constexpr int kPairStep = 8 * 4 / 8 * 128, kVRows = 64 / 8 * kSfSK * 16;
+    static_assert(kSfPairs % 8 == 0, "whole passes of 8 pairs");
+    const int so = cm_off16(arow, 4 * c0, kSfSK);
+    // U, V of this thread's pairs; CHECKED zeroes particles j >= jlim (the
+    // last stage of a chunk: its slot beyond jlim holds older data)
+    auto gen = [&](auto checked, unsigned char* sa, const float2* tb, const float4* mus, int jlim) {
+      constexpr bool CHECKED = decltype(checked)::value;
+#pragma unroll 1
+      for (int u = 0; u < kSfPairs / 8; u++) {
+        float U[4], V[4];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int jj = 16 * u + h;
+          float2 Y = tb[yo + jj];
+          const float2 Z = tb[zo + jj];
+          float4 mu = mus[mo + jj];
+          float pr = Y.x * Z.x - ysg * Y.y * Z.y, pi = Y.x * Z.y + ysg * Y.y * Z.x;
+          if constexpr (CHECKED) {
+            const bool in = mo + jj < jlim;
+            pr = in ? pr : 0.f;
+            pi = in ? pi : 0.f;
+            mu = in ? mu : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+          const float cf = (nyf * mu.y + nzf * mu.z) * vsc, mx = mu.x * vsc;
+          U[2 * h] = cf * pr;
+          U[2 * h + 1] = cf * pi;
+          V[2 * h] = mx * pr;
+          V[2 * h + 1] = mx * pi;
+        }
+        uint2 hi, lo;
+        unsigned char* d = sa + so + kPairStep * u;
+        f16_split2(U[0], U[1], hi.x, lo.x);
+        f16_split2(U[2], U[3], hi.y, lo.y);
+        *(uint2*)d = hi;
+        *(uint2*)(d + L.a) = lo;
+        f16_split2(V[0], V[1], hi.x, lo.x);
+        f16_split2(V[2], V[3], hi.y, lo.y);
+        *(uint2*)(d + kVRows) = hi;
+        *(uint2*)(d + kVRows + L.a) = lo;
+      }
+    };
     // slots and phase parities of stage s; the a_empty phase that frees the
     // generated slot for stage s is the one of stage s - kSfA (parity pha ^ 1)
     int qa = 0, pha = 0, qb = 0, phb = 0;
@@ -355,36 +402,10 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
       const float2* tb = (const float2*)(sbt + 2 * L.b);
       const float4* mus = (const float4*)(sbt + 2 * L.b + L.t);
       const int nval = p1 - (p0 + s * kSfSC);
-#pragma unroll 1
-      for (int u = 0; u < kSfPairs / 8; u++) {
-        const int c = c0 + 8 * u;
-        float U[4] = {0.f, 0.f, 0.f, 0.f}, V[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const int j = 2 * c + h;
-          if (rvalid && j < nval) {
-            float2 Y = tb[yo + j];
-            if (ny < 0) Y.y = -Y.y;
-            const float2 Z = tb[zo + j];
-            const float4 mu = mus[j];
-            const float pr = Y.x * Z.x - Y.y * Z.y, pi = Y.x * Z.y + Y.y * Z.x;
-            const float cf = nyf * mu.y + nzf * mu.z;
-            U[2 * h] = cf * pr;
-            U[2 * h + 1] = cf * pi;
-            V[2 * h] = mu.x * pr;
-            V[2 * h + 1] = mu.x * pi;
-          }
-        }
-        uint2 hi, lo;
-        f16_split2(U[0], U[1], hi.x, lo.x);
-        f16_split2(U[2], U[3], hi.y, lo.y);
-        *(uint2*)(sa + cm_off16(arow, 4 * c, kSfSK)) = hi;
-        *(uint2*)(sa + L.a + cm_off16(arow, 4 * c, kSfSK)) = lo;
-        f16_split2(V[0], V[1], hi.x, lo.x);
-        f16_split2(V[2], V[3], hi.y, lo.y);
-        *(uint2*)(sa + cm_off16(64 + arow, 4 * c, kSfSK)) = hi;
-        *(uint2*)(sa + L.a + cm_off16(64 + arow, 4 * c, kSfSK)) = lo;
-      }
+      if (nval >= kSfSC)
+        gen(std::false_type{}, sa, tb, mus, kSfSC);
+      else
+        gen(std::true_type{}, sa, tb, mus, nval);
       fence_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(&full_a[qa]);
