@@ -559,7 +559,9 @@ def run_ours(args):
     nk_real = len(sim.debug_structure_factor())
     clk = clocks.stop()  # sampled over both timed runs
 
-    # end to end through the C ABI with pinned host buffers, copies timed
+    # end to end through the C ABI with pinned host buffers, copies timed:
+    # each step the state goes in from host memory and comes back
+    # (md_step_io: upload, step, download, one synchronisation)
     host_in = [torch.empty((3, n), dtype=torch.float64).pin_memory().numpy() for _ in range(3)]
     host_out = [torch.empty((3, n), dtype=torch.float64).pin_memory().numpy() for _ in range(3)]
     st = sim.get_state(out=host_in)
@@ -569,9 +571,7 @@ def run_ours(args):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim.set_state(*host_in, reset=False)
-        sim.step(1, 1e-12)
-        sim.get_state(out=host_out)
+        sim.step_io(host_in, 1, 1e-12, out=host_out)
         e2e_s += time.perf_counter() - t0
         for a_, b_ in zip(host_in, host_out):
             a_[...] = b_

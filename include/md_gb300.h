@@ -231,6 +231,14 @@ int md_set_noise(md_ctx* ctx, int mode, uint64_t seed);
  * [torque N x 3][field N x 3][force N x 3] column-major (the order of the
  * three Rand::normal draws of DefThermFluct); NULL otherwise. */
 int md_step(md_ctx* ctx, int64_t nsteps, double dt, const double* xi);
+/* The state in, nsteps of md_step, the state out, in one call with one
+ * synchronisation: md_state_upload(pos, mm, ea, reset = 0), md_step(nsteps,
+ * dt) with the context's drawn noise (Philox or off; MD_NOISE_UPLOADED is
+ * MD_ERR_INVALID), md_state_download(pos_out, mm_out, ea_out).  For a caller
+ * that keeps the state on the host between steps, as the reference's own
+ * loop does (src/simulation.cpp:469-518); pinned host buffers copy fastest. */
+int md_step_io(md_ctx* ctx, const double* pos, const double* mm, const double* ea, int64_t nsteps, double dt,
+               double* pos_out, double* mm_out, double* ea_out);
 /* RunSimulation's loop with the adaptive solvers of IntegrationRot
  * (src/simulation.cpp:707-871; the configuration's SOLVER: 0 Heun-Euler 1(2),
  * 1 Bogacki-Shampine 2(3), 2 Dormand-Prince 4(5)) and the step control

@@ -120,6 +120,7 @@ def lib():
         "md_compute_field": (C.c_int, [V, P, P]),
         "md_set_noise": (C.c_int, [V, C.c_int, C.c_uint64]),
         "md_step": (C.c_int, [V, I64, C.c_double, P]),
+        "md_step_io": (C.c_int, [V, P, P, P, I64, C.c_double, P, P, P]),
         "md_step_adaptive": (C.c_int, [V, I64, C.c_double, P, P, PI64]),
         "md_records": (C.c_int, [V, I64, I64, P]),
         "md_num_records": (C.c_int, [V, PI64]),

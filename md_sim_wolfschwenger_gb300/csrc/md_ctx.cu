@@ -401,10 +401,16 @@ int alloc_nbr(md_ctx* c, long long cap) {
 
 // After work on the stream: a neighbour list that did not fit was replaced by
 // the direct cell scan (results are correct); grow it for the next steps.
+static int handle_overflow(md_ctx* c, const StepFlags& f);
+
 int check_overflow(md_ctx* c) {
   StepFlags f;
   CK(c, cudaMemcpyAsync(&f, &c->sc->flags, sizeof f, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
+  return handle_overflow(c, f);
+}
+
+static int handle_overflow(md_ctx* c, const StepFlags& f) {
   if (!f.overflow) return MD_OK;
   int total = 0;
   CK(c, cudaMemcpy(&total, c->nbr_off + c->n, sizeof(int), cudaMemcpyDeviceToHost));
@@ -417,16 +423,19 @@ int check_overflow(md_ctx* c) {
   return force_rebuild(c);
 }
 
+// Error word and list flags of the work on the stream, read together (one
+// copy of the device scalars, one synchronisation).
 int read_err_word(md_ctx* c) {
-  int e = 0;
-  CK(c, cudaMemcpyAsync(&e, &c->sc->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  DevScalars h;
+  CK(c, cudaMemcpyAsync(&h, c->sc, sizeof h, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
+  const int e = h.err;
   if (e) {
     CK(c, cudaMemsetAsync(&c->sc->err, 0, sizeof(int), c->stream));
     if (e & kErrNonFinite) return set_err(c, MD_ERR_NONFINITE, "non-finite position or orientation after the step");
     if (e & kErrTcWait) return set_err(c, MD_ERR_CUDA, "tensor-core k space: a pipeline wait gave up");
   }
-  return check_overflow(c);
+  return handle_overflow(c, h.flags);
 }
 
 // ============================================================== C ABI
@@ -711,8 +720,8 @@ int md_set_box(md_ctx* c, double lBox) {
   return MD_OK;
 }
 
-int md_state_upload(md_ctx* c, const double* pos, const double* mm, const double* ea, int reset) {
-  if (!c || !pos || !mm || !ea) return set_err(c, MD_ERR_INVALID, "null argument");
+// The copies and checks of md_state_upload, queued on the stream.
+static int enqueue_upload(md_ctx* c, const double* pos, const double* mm, const double* ea, int reset) {
   const size_t B = 24 * (size_t)c->n;
   CK(c, cudaMemcpyAsync(c->pos, pos, B, cudaMemcpyHostToDevice, c->stream));
   CK(c, cudaMemcpyAsync(c->mm, mm, B, cudaMemcpyHostToDevice, c->stream));
@@ -727,9 +736,15 @@ int md_state_upload(md_ctx* c, const double* pos, const double* mm, const double
   } else if (int st = force_rebuild(c)) {
     return st;
   }
-  CK(c, cudaStreamSynchronize(c->stream));
   c->have_state = true;
   c->have_geometry = false;
+  return MD_OK;
+}
+
+int md_state_upload(md_ctx* c, const double* pos, const double* mm, const double* ea, int reset) {
+  if (!c || !pos || !mm || !ea) return set_err(c, MD_ERR_INVALID, "null argument");
+  if (int st = enqueue_upload(c, pos, mm, ea, reset)) return st;
+  CK(c, cudaStreamSynchronize(c->stream));
   return MD_OK;
 }
 
@@ -997,9 +1012,19 @@ int md_set_noise(md_ctx* c, int mode, uint64_t seed) {
 
 }  // extern "C"
 
+// Room for `extra` more step records.  The host keeps an upper bound of the
+// device's record count (records issued since it was last read or cleared)
+// and reads the device only when the bound would pass the capacity, so a
+// step does not wait on a device read.
 int ensure_records(md_ctx* c, int64_t extra) {
+  if (c->nrec_bound + extra <= c->rec_cap) {
+    c->nrec_bound += extra;
+    return MD_OK;
+  }
   long long nrec = 0;
+  CK(c, cudaStreamSynchronize(c->stream));
   CK(c, cudaMemcpy(&nrec, &c->sc->nrec, sizeof nrec, cudaMemcpyDeviceToHost));
+  c->nrec_bound = nrec + extra;
   if (nrec + extra <= c->rec_cap) return MD_OK;
   long long cap = std::max<long long>(1024, 2 * (nrec + extra));
   double* nr = nullptr;
@@ -1027,10 +1052,8 @@ int prepare_dt(md_ctx* c, double dt) {
   return MD_OK;
 }
 
-extern "C" {
-
-int md_step(md_ctx* c, int64_t nsteps, double dt, const double* xi) {
-  NvtxRange nv("md_step");
+// md_step's work queued on the stream (no synchronisation).
+static int enqueue_steps(md_ctx* c, int64_t nsteps, double dt, const double* xi) {
   int st = check_ready(c, true);
   if (st) return st;
   if (nsteps < 0 || !(dt > 0)) return set_err(c, MD_ERR_INVALID, "bad nsteps or dt");
@@ -1058,6 +1081,32 @@ int md_step(md_ctx* c, int64_t nsteps, double dt, const double* xi) {
     c->launches = c->launches_per_step * nsteps;
   }
   c->have_geometry = true;
+  return MD_OK;
+}
+
+extern "C" {
+
+int md_step(md_ctx* c, int64_t nsteps, double dt, const double* xi) {
+  NvtxRange nv("md_step");
+  if (int st = enqueue_steps(c, nsteps, dt, xi)) return st;
+  return read_err_word(c);
+}
+
+int md_step_io(md_ctx* c, const double* pos, const double* mm, const double* ea, int64_t nsteps, double dt,
+               double* pos_out, double* mm_out, double* ea_out) {
+  NvtxRange nv("md_step_io");
+  if (!c || !pos || !mm || !ea || !pos_out || !mm_out || !ea_out) return set_err(c, MD_ERR_INVALID, "null argument");
+  if (c->noise == MD_NOISE_UPLOADED) return set_err(c, MD_ERR_INVALID, "md_step_io draws its noise (Philox or off)");
+  int st = enqueue_upload(c, pos, mm, ea, 0);
+  if (!st) st = enqueue_steps(c, nsteps, dt, nullptr);
+  if (st) {
+    cudaStreamSynchronize(c->stream);
+    return st;
+  }
+  const size_t B = 24 * (size_t)c->n;
+  CK(c, cudaMemcpyAsync(pos_out, c->pos, B, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(mm_out, c->mm, B, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(ea_out, c->ea, B, cudaMemcpyDeviceToHost, c->stream));
   return read_err_word(c);
 }
 
@@ -1295,6 +1344,7 @@ int md_clear_records(md_ctx* c) {
   if (!c) return MD_ERR_INVALID;
   CK(c, cudaMemsetAsync(&c->sc->nrec, 0, sizeof(long long), c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
+  c->nrec_bound = 0;
   return MD_OK;
 }
 

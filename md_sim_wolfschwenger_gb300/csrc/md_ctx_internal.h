@@ -97,6 +97,7 @@ struct md_ctx {
   DevScalars* sc = nullptr;
   double* records = nullptr;
   long long rec_cap = 0;
+  long long nrec_bound = 0;  // upper bound of the device's record count (ensure_records)
   // k space
   KSeg* kseg = nullptr;
   int* koff = nullptr;

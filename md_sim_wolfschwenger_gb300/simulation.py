@@ -232,6 +232,16 @@ class Simulation:
             xp = _P(xi)
         self._ck(self.L.md_step(self.h, int(nsteps), dt, xp))
 
+    def step_io(self, state, nsteps=1, dt=None, out=None):
+        """State (pos, mm, ea) in, nsteps of step(), state out, in one call
+        and one synchronisation (md_step_io); `out` may be three (3, N)
+        float64 arrays to fill.  Pinned host arrays copy fastest."""
+        dt = float(self.config.c.deltaTinit if dt is None else dt)
+        a = [np.ascontiguousarray(x, dtype=np.float64).reshape(3, self.n) for x in state]
+        o = out if out is not None else [np.empty((3, self.n)) for _ in range(3)]
+        self._ck(self.L.md_step_io(self.h, *(_P(x) for x in a), int(nsteps), dt, *(_P(x) for x in o)))
+        return tuple(o)
+
     def step_adaptive(self, max_steps, dt, t_end=float("inf"), xi=None):
         """Accepted steps of RunSimulation's loop with the configuration's
         SOLVER (0 Heun-Euler, 1 Bogacki-Shampine, 2 Dormand-Prince) and the
