@@ -26,8 +26,8 @@
 // added into one accumulator (measured at N = 32768: 5.5e-6 relative error
 // of S with 392 particles per accumulator, 1.8e-6 with 128), so the
 // structure factor uses chunks of <= 512 particles (4 accumulators of <= 128
-// each, added in FP32) and sums the chunks with compensated FP32 sums, then
-// FP64; the scatter sums over the nx of a row in the MMA (<= 2 kc + 1 terms),
+// each, added in FP32) and sums the chunks with compensated FP32 sums (in
+// two levels); the scatter sums over the nx of a row in the MMA (<= 2 kc + 1 terms),
 // over the rows of a tile in FP32 and over tiles with compensated FP32 sums.
 // All sums have a
 // fixed order: results are deterministic.
@@ -44,7 +44,7 @@
 //                dealt round-robin, one accumulator each, added in a fixed
 //                order at the end); mbarriers hand stages between the roles
 //                and tcgen05.commit releases the slots.
-//   k_sf_tc_reduce  FP64 sum of the chunk partials, S(n) = C_U + nx C_V,
+//   k_sf_tc_reduce  compensated sum of the chunk partials, S(n) = C_U + nx C_V,
 //                e(n) S(n), and the scatter's W operand image (hi, lo) in
 //                the shared-memory layout the scatter copies in bulk.
 //   k_kscat_tc   128 particles per block, their X phases (the A operand, hi
@@ -490,8 +490,8 @@ __device__ __forceinline__ void w_put(float* img, int kp, int row, int k, float 
 
 // Block per (M tile, column q): 64 rows x 8 groups of chunks, the groups
 // combined in a fixed order.  The chunk partials are summed with compensated
-// FP32 sums (Kahan; GB300's FP64 rate is ~1/64 of FP32), the 8 group sums and
-// their compensations in FP64.
+// FP32 sums (Kahan; GB300's FP64 rate is ~1/64 of FP32), then the 8 group
+// sums and their compensations in one more compensated FP32 sum.
 __device__ __forceinline__ void kahan_f(float& s, float& c, float v) {
   const float y = v - c, t = s + y;
   c = (t - s) - y;
@@ -529,29 +529,35 @@ __global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
   }
   __syncthreads();
   if (grp != 0) return;
-  double acc[4] = {0, 0, 0, 0};
+  // the groups' sums and compensations in one more compensated FP32 sum
+  float acc[4], cmp[4];
+#pragma unroll
+  for (int v = 0; v < 4; v++) acc[v] = cmp[v] = 0.f;
 #pragma unroll
   for (int g8 = 0; g8 < 8; g8++)
 #pragma unroll
-    for (int v = 0; v < 4; v++) acc[v] += (double)red[g8][2 * v][rl] - (double)red[g8][2 * v + 1][rl];
-  const double ur = acc[0], ui = acc[1], vr = acc[2], vi = acc[3];
+    for (int v = 0; v < 4; v++) {
+      kahan_f(acc[v], cmp[v], red[g8][2 * v][rl]);
+      kahan_f(acc[v], cmp[v], -red[g8][2 * v + 1][rl]);
+    }
+  const float ur = acc[0] - cmp[0], ui = acc[1] - cmp[1], vr = acc[2] - cmp[2], vi = acc[3] - cmp[3];
   const int r = mtile * 64 + rl;
   if (r >= p.tc_rows) return;
   const int kk = p.tc_kmap[r * Q + q];
   if (kk < 0) return;
-  const double nx = (double)(q - p.kc);
-  const double sr = ur + nx * vr, si = ui + nx * vi;
-  p.S[kk] = make_double2(sr, si);
-  const double e = p.ek[kk];
-  const double er = e * sr, ei = e * si;
+  const float nx = (float)(q - p.kc);  // small integer: its powers below are exact
+  const float sr = fmaf(nx, vr, ur), si = fmaf(nx, vi, ui);
+  p.S[kk] = make_double2((double)sr, (double)si);
+  const float e = (float)p.ek[kk];
+  const float er = e * sr, ei = e * si;
   const int tt = r / L::RT, sl = r - tt * L::RT;
   const int kp = p.tc_kp;
   float* img = p.tc_w + (size_t)tt * 2 * kScCols * kp;
-  double f = 1.0;
+  float f = 1.f;
 #pragma unroll
   for (int pp = 0; pp < L::P; pp++) {
     // W_p = nx^p conj(e S): (wr, wi)
-    const float wr = (float)(f * er), wi = (float)(-f * ei);
+    const float wr = f * er, wi = -f * ei;
     const int col = L::ccol(sl, pp);
     w_put(img, kp, 2 * col, 2 * q, wr);
     w_put(img, kp, 2 * col, 2 * q + 1, -wi);
