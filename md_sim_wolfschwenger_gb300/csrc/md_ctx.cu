@@ -630,7 +630,7 @@ int md_ctx_create(const md_config* cfg, int64_t n, int precision, md_ctx** out) 
   if ((st = dalloc(c, &c->nbr_off, 4 * (N + 1)))) return fail(st);
   if ((st = dalloc(c, &c->xbuild, 24 * N))) return fail(st);
   if ((st = dalloc(c, &c->Ppart, 24 * N))) return fail(st);
-  if ((st = dalloc(c, &c->obs_part, 56 * (size_t)int_blocks((int)n)))) return fail(st);
+  if ((st = dalloc(c, &c->obs_part, 56 * (size_t)std::max(int_blocks((int)n), int_blocks_one((int)n))))) return fail(st);
   if ((st = dalloc(c, &c->sc, sizeof(DevScalars)))) return fail(st);
   if (cudaMemsetAsync(c->sc, 0, sizeof(DevScalars), c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->xi, 0, 72 * N, c->stream) != cudaSuccess ||

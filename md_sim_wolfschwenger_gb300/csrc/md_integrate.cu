@@ -27,8 +27,10 @@
 
 namespace md {
 
-constexpr int kIntThreads = 256;
-static_assert(kIntThreads >= 7 * 32, "one warp per step record in the block sums");
+constexpr int kIntThreads = 256;  // largest block (packed batches, adaptive solvers)
+// Single-system Heun launches: 128-thread blocks, so that N = 32768 spreads
+// over every SM (256 blocks; these short kernels are latency bound).
+constexpr int kIntOne = 128;
 
 __device__ __forceinline__ double ext_field_z(const IntParams& p, double t) {
   if (p.field_kind == 1) return p.fieldAmp * sinpi(2.0 * p.fieldFreq * t);
@@ -103,7 +105,7 @@ __device__ __forceinline__ void demag_si(const IntParams& p, int r, R b[3]) {
 template <typename T>
 __device__ __forceinline__ void heun1(const IntParams& p, int bx) {
   using T4 = typename V4<T>::t;
-  const int i = bx * kIntThreads + threadIdx.x;
+  const int i = bx * (int)blockDim.x + threadIdx.x;
   const int n = p.n;
   if (i >= n) return;
   const int r = p.s.rank[i];
@@ -220,10 +222,11 @@ __device__ __forceinline__ void finish_particle(const IntParams& p, int i, int r
 }
 
 // Block sums of the step records and the largest displacement since the
-// last list build (every thread of the block calls this).  The seven sums
-// go through shared memory: warp q adds column q's 256 values with 7 + 5
-// FP64 additions per lane (a butterfly per quantity and warp would take
-// 7 x 5 per warp).
+// last list build (every thread of the block calls this; blocks of up to
+// kIntThreads threads).  The seven sums go through shared memory: a warp
+// adds a record's column of values with one FP64 addition per warp of the
+// block and five butterfly steps per lane (a butterfly per record and warp
+// would take 7 x 5 per warp).
 __device__ __forceinline__ void step_block_sums(const IntParams& p, int bx, const double acc[7], float disp2) {
   if (p.flags) {
     float d = sqrtf(disp2) * (1.0f / (float)p.L);
@@ -235,19 +238,18 @@ __device__ __forceinline__ void step_block_sums(const IntParams& p, int bx, cons
 #pragma unroll
   for (int q = 0; q < 7; q++) red[q][threadIdx.x] = acc[q];
   __syncthreads();
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (w < 7) {
-    double s = red[w][l];
-#pragma unroll
-    for (int k = 1; k < kIntThreads / 32; k++) s += red[w][l + 32 * k];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (int)blockDim.x >> 5;
+  for (int q = w; q < 7; q += nw) {
+    double s = red[q][l];
+    for (int k = 1; k < nw; k++) s += red[q][l + 32 * k];
     s = warp_sum(s);
-    if (l == 0) p.obs_part[7 * bx + w] = s;
+    if (l == 0) p.obs_part[7 * bx + q] = s;
   }
 }
 
 template <typename T>
 __device__ __forceinline__ void heun2(const IntParams& p, int bx) {
-  const int i = bx * kIntThreads + threadIdx.x;
+  const int i = bx * (int)blockDim.x + threadIdx.x;
   const int n = p.n;
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   float disp2 = 0;  // squared displacement since the last neighbour-list build
@@ -559,20 +561,23 @@ int launch_rk_accept(cudaStream_t st, const RKStage& q, bool fp64) {
 }
 
 int int_blocks(int n) { return (n + kIntThreads - 1) / kIntThreads; }
+int int_blocks_one(int n) { return (n + kIntOne - 1) / kIntOne; }
 
 int launch_heun1(cudaStream_t st, const IntParams& p, bool fp64) {
   if (fp64)
-    k_heun1<double><<<int_blocks(p.n), kIntThreads, 0, st>>>(p);
+    k_heun1<double><<<int_blocks_one(p.n), kIntOne, 0, st>>>(p);
   else
-    k_heun1<float><<<int_blocks(p.n), kIntThreads, 0, st>>>(p);
+    k_heun1<float><<<int_blocks_one(p.n), kIntOne, 0, st>>>(p);
   return 1;
 }
 
-int launch_heun2_obs(cudaStream_t st, const IntParams& p, const ObsParams& o, unsigned* done, bool fp64) {
+int launch_heun2_obs(cudaStream_t st, const IntParams& p, const ObsParams& o_in, unsigned* done, bool fp64) {
+  ObsParams o = o_in;
+  o.nblk_int = int_blocks_one(p.n);  // partials of this launch's blocks
   if (fp64)
-    k_heun2_obs<double><<<int_blocks(p.n), kIntThreads, 0, st>>>(p, o, done);
+    k_heun2_obs<double><<<int_blocks_one(p.n), kIntOne, 0, st>>>(p, o, done);
   else
-    k_heun2_obs<float><<<int_blocks(p.n), kIntThreads, 0, st>>>(p, o, done);
+    k_heun2_obs<float><<<int_blocks_one(p.n), kIntOne, 0, st>>>(p, o, done);
   return 1;
 }
 

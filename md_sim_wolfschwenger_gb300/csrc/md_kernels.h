@@ -30,6 +30,7 @@ int sk_resident_blocks(int kc, bool fp64);
 int skred_blocks(const KParams& p);
 int scatter_blocks(const KParams& p, int np);
 int int_blocks(int n);
+int int_blocks_one(int n);        // single-system Heun launches (128-thread blocks)
 
 // Step start: decides whether this step rebuilds the cell order and the
 // neighbour list (host request, or a particle moved more than half_skin).
