@@ -283,7 +283,7 @@ int md_debug_pairs(md_ctx* ctx, int64_t* pairs);
  * the last md_compute_interactions, N x 3 column-major SI: the part of
  * CompDipInteractEwaldR (src/interaction.cpp:383-422). */
 int md_debug_real_part(md_ctx* ctx, double* B, double* F);
-/* Skin of the real-space neighbour list as a fraction of rc (default 0.02):
+/* Skin of the real-space neighbour list as a fraction of rc (default 0.005):
  * the list holds pairs within rc (1 + skin) and is rebuilt on the device when
  * a particle has moved more than skin rc / 2 since the last build. */
 int md_set_neighbor_skin(md_ctx* ctx, double skin_frac);

@@ -129,7 +129,11 @@ struct md_ctx {
   int *nbr = nullptr, *nbr_cnt = nullptr, *nbr_off = nullptr;
   long long nbr_cap = 0;
   double* xbuild = nullptr;
-  double skin_frac = 0.02;  // skin = skin_frac * rc
+  // skin = skin_frac * rc.  Entries between rc and rc (1 + skin) cost a lane
+  // each in both passes (~3 skin of the list); a Brownian step moves a
+  // particle ~5 pm at dt = 1e-12 s, so even a 0.5 % skin (1 nm at rc = 400
+  // nm) is crossed only after ~1e4 steps and rebuilds stay rare.
+  double skin_frac = 0.005;
   bool list_valid = false;  // a build for the current particles, grid and skin exists
   // profiling: events between the kernel segments of a step
   bool prof = false;
