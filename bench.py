@@ -29,21 +29,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-COMMON = ("magnetite (Ms 4.8e5 A/m, K 1.1e4 J/m^3, damping 0.1), 5 nm shell, T=300 K, viscosity 1e-3 Pa s, "
-          "dt=1e-12 s, Philox thermal noise, Ewald at 1e-5 relative force error")
-WORKLOADS = {
-    # the headline: the single large instance of the benchmark suite
-    "large": dict(n=32768, median=1e-8, sigma=0.2, phi=0.10, B0=0.02,
-                  desc="single large instance: N=32768, log-normal core diameters (median 20 nm, sigma 0.2), "
-                       "volume fraction 0.10, static 20 mT, " + COMMON),
-    # the reference's own CPU-runnable case (monodisperse, N=512)
-    "small": dict(n=512, median=1e-8, sigma=0.0, phi=0.05, B0=0.01,
-                  desc="plain case: N=512 monodisperse 20/30 nm, volume fraction 0.05, static 10 mT, " + COMMON),
-    # stress instance
-    "stress": dict(n=131072, median=1.25e-8, sigma=0.25, phi=0.20, B0=0.03,
-                   desc="stress instance: N=131072, log-normal core diameters (median 25 nm, sigma 0.25), "
-                        "volume fraction 0.20, static 30 mT, " + COMMON),
-}
+from md_sim_wolfschwenger_gb300.workloads import WORKLOADS  # noqa: E402  (plain data, no library load)
+
 W = dict(WORKLOADS["large"])
 
 # Algorithmic FLOPs (FMA = 2) per unit of work, counted from the formulas.
@@ -90,29 +77,22 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=256, help="served-stream sample: requests (0 skips it)")
     p.add_argument("--serve-step-scale", type=float, default=0.01,
                    help="served-stream sample: factor on the drawn step counts (1e3..1e5 log-uniform)")
+    p.add_argument("--stress-steps", type=int, default=20, help="stress-instance sample: steps (0 skips it)")
     p.add_argument("--autotune", type=int, default=0, help="candidate cutoffs timed (0: the cost-model choice, the same one the reference arm uses)")
     return p.parse_args()
 
 
 def workload_config(n, seed):
-    from md_sim_wolfschwenger_gb300 import MD_NOISE_PHILOX, MD_PREC_MIXED, Configuration
-    cfg = Configuration.default()
-    cfg.set(SIZE_DIST=1 if W["sigma"] > 0 else 0, rMagMean=W["median"], sigmaLog=W["sigma"], dShell=5e-9,
-            volFrac=W["phi"], magFluxDens=W["B0"], tMag=1.0,
-            tRelax=0.0, deltaTinit=1e-12, satMag=4.8e5, anisEn=1.1e4, magDamp=0.1, temp=300.0, visOverride=1e-3,
-            numbPartOverride=n, errTolEwald=1e-5, seed=seed, SOLVER=0, ENABLE_MOBILIZATION=1, ENABLE_THERM_FIELD=1,
-            ENABLE_THERM_TORQUE=1, ENABLE_THERM_FORCE=1, ENABLE_COATING_POT=0, INIT_CONFIG_ROT=4,
-            INIT_CONFIG_TRANS=1, precision=MD_PREC_MIXED, noise=MD_NOISE_PHILOX)
-    return cfg
+    from md_sim_wolfschwenger_gb300 import workloads
+    return workloads.config(dict(W, n=n), seed)
 
 
 def workload_state(n, seed):
     """Initial system from the library's InitParticleProps + InitCoordsFromSketch
     (md_init_system: log-normal radii, random sequential addition placed
     largest first, moments and easy axes independent and uniform)."""
-    import md_sim_wolfschwenger_gb300 as m
-    rMag, rHydr, pos, mm, ea, L = m.init_system(workload_config(n, seed), n, 1000 + seed)
-    return rMag, rHydr, L, pos, mm, ea
+    from md_sim_wolfschwenger_gb300 import workloads
+    return workloads.state(dict(W, n=n), seed)
 
 
 def oracle_ini(n, seed):
@@ -318,23 +298,12 @@ def fp64_plain(n, sysd, ewald, seed, steps=4, warm=1):
     RMS over particles, the reference's error metric)."""
     import torch
     from md_sim_wolfschwenger_gb300 import MD_NOISE_PHILOX, MD_PREC_FP64, MD_PREC_MIXED, Simulation
+    from md_sim_wolfschwenger_gb300 import workloads
     rMag, rHydr, L, pos, mm, ea = sysd
     cfg = workload_config(n, seed)
-    out = {}
-    for prec in (MD_PREC_MIXED, MD_PREC_FP64):
-        sim = Simulation(cfg, n, prec, rMag=rMag, rHydr=rHydr)
-        sim.set_state(pos, mm, ea)
-        sim.set_ewald(*ewald)
-        out[prec] = sim.CompInteractions()[:2]
-        sim.close()
-    fAl, bAl, tAl = contact_scales(cfg, rMag, rHydr)
-    mom = cfg.c.satMag * 4.0 / 3.0 * cfg.c.my_pi * np.asarray(rMag) ** 3
-    tq = {p: np.cross((np.asarray(mm) * mom).T, out[p][0].T).T for p in out}
-    err = {"B": rms_rel(out[MD_PREC_MIXED][0], out[MD_PREC_FP64][0], bAl),
-           "F": rms_rel(out[MD_PREC_MIXED][1], out[MD_PREC_FP64][1], fAl),
-           "torque": rms_rel(tq[MD_PREC_MIXED], tq[MD_PREC_FP64], tAl),
-           "metric": "RMS over particles of |mixed - fp64| / contact value (CheckEwaldSum's metric); the "
-                     "Ewald truncation budget is 1e-5"}
+    err, _ = workloads.mixed_vs_fp64(cfg, rMag, rHydr, pos, mm, ea, ewald)
+    err["metric"] = ("RMS over particles of |mixed - fp64| / contact value (CheckEwaldSum's metric); the "
+                     "Ewald truncation budget is 1e-5")
     sim = Simulation(cfg, n, MD_PREC_FP64, rMag=rMag, rHydr=rHydr)
     sim.set_state(pos, mm, ea)
     sim.set_ewald(*ewald)
@@ -354,6 +323,58 @@ def fp64_plain(n, sysd, ewald, seed, steps=4, warm=1):
     return {"value": n / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms, "steps": steps,
             "dtype": "f64", "note": "same system and Ewald parameters, plain FP64 path, one instance",
             "mixed_error_vs_fp64": err}
+
+
+def stress_sample(steps, warm=3, fp64_steps=2, seed=1):
+    """The stress instance (N = 131072, log-normal sigma 0.25, volume fraction
+    0.20, 30 mT): mixed particle-steps/s from CUDA events around `steps`
+    graph replays, the plain FP64 path on the same system and Ewald
+    parameters, and the mixed path's error against it (B, F, torque)."""
+    import torch
+    from md_sim_wolfschwenger_gb300 import MD_NOISE_PHILOX, MD_PREC_FP64, MD_PREC_MIXED, Simulation, workloads
+    w = workloads.spec("stress")
+    n = w["n"]
+    cfg = workloads.config(w, seed)
+    rMag, rHydr, L, pos, mm, ea = workloads.state(w, seed)
+    out = {}
+    for prec, k in ((MD_PREC_MIXED, steps), (MD_PREC_FP64, fp64_steps)):
+        sim = Simulation(cfg, n, prec, rMag=rMag, rHydr=rHydr)
+        sim.set_state(pos, mm, ea)
+        if prec == MD_PREC_MIXED:
+            alpha, rc, kc, errF, errT = sim.ewald_params()
+        sim.set_ewald(alpha, rc, kc)
+        sim.set_noise(MD_NOISE_PHILOX, seed)
+        sim.step(warm if prec == MD_PREC_MIXED else 1, 1e-12)
+        sim.sync()
+        ext = torch.cuda.ExternalStream(sim.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            e0.record()
+        sim.step(k, 1e-12)
+        with torch.cuda.stream(ext):
+            e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        extra = {}
+        if prec == MD_PREC_MIXED:
+            extra = {"pairs": sim.pairs(), "strong_pair_entries_fp64": sim.strong_pairs(),
+                     "kspace_tensor_cores": sim.kspace_tensor_cores()}
+        sim.close()
+        out[prec] = (ms, k, extra)
+    err, _ = workloads.mixed_vs_fp64(cfg, rMag, rHydr, pos, mm, ea, (alpha, rc, kc))
+    ms, k, extra = out[MD_PREC_MIXED]
+    ms64, k64, _ = out[MD_PREC_FP64]
+    return {"value": n / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms, "steps": k,
+            "workload": w["desc"], "n": n, "lBox_m": L,
+            "ewald": {"alpha_L": alpha * L, "rc_over_L": rc / L, "kc": kc, "pred_force_err_rel_contact": errF,
+                      "pred_torque_err_rel_contact": errT, **extra},
+            "fp64_plain": {"value": n / (ms64 * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms64,
+                           "steps": k64},
+            "mixed_over_fp64_plain": ms64 / ms,
+            "mixed_error_vs_fp64": err,
+            "note": "graph replays back to back (no L2 flush; the working set exceeds the 129 MB L2); torque "
+                    "error is the FP32 k-space floor for a moment ratio of ~700 (below the parameters' own "
+                    "Ewald truncation error pred_torque_err_rel_contact)"}
 
 
 def sweep_sample(replicas, steps, seed=3):
@@ -556,6 +577,7 @@ def run_ours(args):
     seg_mean = {k: v / psteps for k, v in seg_sum.items()}
     serial_ms = sum(seg_mean.values())
     pairs = sim.pairs()
+    strong = sim.strong_pairs()
     nk_real = len(sim.debug_structure_factor())
     clk = clocks.stop()  # sampled over both timed runs
 
@@ -648,10 +670,12 @@ def run_ours(args):
                "sample": f"1 step of the same N={n} system and Ewald parameters, single thread (the reference "
                          f"is single-threaded): all-pairs list, FP64, Philox noise; {per[0]:.1f} s"}
 
-    fp64 = sweep = serving = None
+    fp64 = sweep = serving = stress = None
     if rank == 0 and ws == 1:
         if not args.no_fp64:
             fp64 = fp64_plain(n, sysd, (alpha, rc, kc), seed)
+        if args.stress_steps > 0 and args.workload == "large":
+            stress = stress_sample(args.stress_steps)
         if args.sweep_replicas > 0:
             sweep = sweep_sample(args.sweep_replicas, args.sweep_steps)
         if args.serve_requests > 0:
@@ -663,15 +687,18 @@ def run_ours(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if prec == MD_PREC_FP64 else "f32",
                 "precision": ("fp64 (plain)" if prec == MD_PREC_FP64 else
-                              "mixed: FP32 pair maths, phases, scatter and integrator; FP64 structure-factor "
-                              "sums across chunks, self/surface terms, positions, reductions"),
+                              "mixed: FP32 pair maths, phases, scatter and integrator; real-space pairs above 3 "
+                              "contact forces (strong pairs) in FP64; structure-factor chunk partials summed "
+                              "exactly (TwoSum FP32 pairs, then FP64), S(n) and e(n)S(n) in FP64; FP64 self/"
+                              "surface terms, positions, reductions"),
                 "data": "synthetic (seeded log-normal radii, random sequential addition, moments and easy axes "
                         "independent and uniform on the sphere)",
                 "config": {"workload": W["desc"], "n": n, "lBox_m": L, "replicas_per_gpu": 1,
                            "parallelism": f"replicas x{ws}" if ws > 1 else "single instance",
                            "ewald": {"alpha_L": alpha * L, "rc_over_L": rc / L, "kc": kc,
                                      "pred_force_err_rel_contact": errF, "pred_torque_err_rel_contact": errT,
-                                     "pairs": pairs, "k_vectors": nk_real},
+                                     "pairs": pairs, "k_vectors": nk_real,
+                                     "strong_pair_entries_fp64": strong},
                            "l2": "flushed between timed steps (256 MiB write); step time from CUDA events on the "
                                  "library's stream around each step's graph launch"},
                 "e2e": e2e, "roofline": roofline, "segments": segs,
@@ -682,7 +709,7 @@ def run_ours(args):
                                        "concurrency), the sum of the segments; per-kernel figures come from it"},
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches_per_step * args.steps,
                 "fp64_plain": fp64, "mixed_over_fp64_plain": (value / fp64["value"]) if fp64 else None,
-                "sweep": sweep, "serving": serving}
+                "sweep": sweep, "serving": serving, "stress": stress}
         print(json.dumps(line), flush=True)
     sim.close()
 

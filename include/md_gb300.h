@@ -287,6 +287,19 @@ int md_debug_real_part(md_ctx* ctx, double* B, double* F);
  * the list holds pairs within rc (1 + skin) and is rebuilt on the device when
  * a particle has moved more than skin rc / 2 since the last build. */
 int md_set_neighbor_skin(md_ctx* ctx, double skin_frac);
+/* Mixed path: real-space pairs whose force weight
+ * (|mu_i| |mu_j| / mu_min^2) (2 rHydr_min / r)^4 exceeds theta (contact
+ * forces of the smallest particles, the scale of CheckEwaldSum's relative
+ * error, src/interaction.cpp:180, 741-754) are evaluated in FP64 with the
+ * reference's pair formula (src/interaction.cpp:396-417) instead of FP32.
+ * Classified at each neighbour-list build; default theta = 3 (about 0.2 % of
+ * the pairs of a log-normal sigma 0.2 system); 0 turns it off; no effect on
+ * the FP64 path, with coating potentials on, or on a system without pairs
+ * above theta (monodisperse: none for theta >= 1). */
+int md_set_strong_pairs(md_ctx* ctx, double theta);
+/* Entries of the strong-pair list of the last build (each ordered pair
+ * once); 0 when the path is off, -1 while the list is not in use. */
+int md_debug_strong_pairs(md_ctx* ctx, int64_t* entries);
 /* Test hook: caps the neighbour-list capacity (entries); a list that does not
  * fit makes the real-space kernels scan the cells directly for that step. */
 int md_debug_neighbor_capacity(md_ctx* ctx, int64_t cap, int64_t* used);

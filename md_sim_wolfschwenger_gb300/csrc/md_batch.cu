@@ -105,6 +105,11 @@ int upload_params(md_batch* b) {
     kfield[r] = k_params(c, c->Bk2, nullptr);
     i1[r] = int_params(c, s.dt, c->Br, c->Bk);
     i2[r] = int_params(c, s.dt, c->Br2, c->Bk2);
+    // packed launches evaluate every pair in FP32 (no strong-pair kernels):
+    // builds do not classify, and flagged entries of an earlier build count
+    // as ordinary ones
+    rfull[r].strong = rfield[r].strong = 0;
+    i1[r].sv.off = i2[r].sv.off = nullptr;
     obs[r] = obs_params(c, s.dt);
     obs[r].status = b->d_status + r;
   }

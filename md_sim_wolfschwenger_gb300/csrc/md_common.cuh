@@ -51,6 +51,7 @@ struct StepFlags {
   int overflow;       // the neighbour list did not fit: real space scans cells
   int force;          // host request: rebuild on the next step
   unsigned maxdisp;   // float bits of the largest displacement since the build (box units)
+  int soverflow;      // the strong-pair list did not fit: every pair stays on the FP32 path
 };
 
 // Cell-list build of one system (positions in particle order, FP64).
@@ -144,6 +145,50 @@ struct RealParams {
   int* nbr_off;               // [n + 1]
   long long nbr_cap;
   StepFlags* flags;           // rebuild / overflow
+  // Strong pairs (mixed path): list entries with |mu_i|^2 |mu_j|^2 >
+  // strong_w4sq r^8 at the build (box units, moments in mu_max) carry the
+  // sign bit in nbr, are left out of the FP32 field, force and pressure sums
+  // (the FP32 pass still pushes them apart when they overlap) and are
+  // evaluated in FP64 from the list snbr by the same kernel's warps, one
+  // term set per entry into svals; the integrator adds each particle's
+  // entries (StrongView).
+  int strong;                 // 1: classify at builds and honour the flags
+  float strong_w4sq;
+  int2* snbr;                 // [scap] (i, j) sorted indices, grouped by i
+  int* snbr_cnt;              // [n]
+  int* snbr_off;              // [n + 1]
+  long long scap;
+  double* svals;              // [3][scap] B (+ [3][scap] F, [3][scap] P when FULL) per entry
+  // moments of the strong entries: FP64 master directions x |mu| / mu_max
+  // (particle order, via s.perm) when the evaluated moments are the master
+  // state; null: the sorted view's (FP32 stage moments, exact there)
+  const double* smm;
+  const double* smag;
+};
+
+// The FP64 strong-pair terms of one evaluation, as the integrator reads
+// them: per sorted slot r, entries snbr_off[r] .. snbr_off[r + 1] of each
+// component array.  off == nullptr: the path is off; the flags say whether
+// the list of the last build is in use.
+struct StrongView {
+  const int* off;
+  long long cap;
+  const double* B;  // [3][cap]
+  const double* F;  // [3][cap] (full evaluation)
+  const double* P;  // [3][cap] (full evaluation)
+  const StepFlags* flags;
+  // sum of nc components of a (stride cap) over slot r's entries, in list order
+  __device__ __forceinline__ bool sum3(const double* a, int r, double out[3]) const {
+    out[0] = out[1] = out[2] = 0.0;
+    if (!off || !a || flags->overflow || flags->soverflow) return false;
+    const int e1 = (int)min((long long)off[r + 1], cap);
+    for (int e = max(off[r], 0); e < e1; e++) {
+      out[0] += a[e];
+      out[1] += a[cap + e];
+      out[2] += a[2 * cap + e];
+    }
+    return true;
+  }
 };
 
 // --------------------------------------------------------- k space
@@ -223,6 +268,16 @@ struct IntParams {
   void *k1m, *k1e, *m2, *e2, *th;   // th: [9][n] scaled noise
   // stage outputs (sorted order, T)
   const void *Br, *Bk, *Fr, *Fk, *ov;
+  // FP64 strong-pair terms: sv.B belongs to the evaluation that gave Br,
+  // sv.F and sv.P to the full evaluation (Fr, Ppart); sv.off null when off
+  StrongView sv;
+  // Reported field only (R = double in demag_si): FP64 unit moments of the
+  // evaluation (particle order) and the k-space self-interaction matrix
+  // kself = cflux sum_k e(k) n n^T (xx, yy, zz, xy, xz, yz; box units); the
+  // k-space sum holds -kself mu_i of each particle's own FP32 moment, which
+  // is moved to the FP64 moment.  mexact null: no correction.
+  const double* mexact;
+  double kself[6];
   SortedView s;
   const double* musum;       // [3] sum of mu' of the evaluated stage
   const double* Ppart;       // [n][3] per-particle pressure sums of the full real-space pass

@@ -147,6 +147,19 @@ RealParams real_params(md_ctx* c, void* B, void* F, void* ov) {
   p.nbr_off = c->nbr_off;
   p.nbr_cap = c->nbr_cap;
   p.flags = &c->sc->flags;
+  if (strong_active(c)) {
+    p.strong = 1;
+    p.strong_w4sq = c->strong_w4sq;
+    p.snbr = c->snbr;
+    p.snbr_cnt = c->snbr_cnt;
+    p.snbr_off = c->snbr_off;
+    p.scap = c->scap;
+    p.svals = B == c->Br2 ? c->svals2 : c->svals;
+    if (B != c->Br2) {  // full evaluation: the master moments
+      p.smm = c->mm;
+      p.smag = c->magMom_u;
+    }
+  }
   return p;
 }
 
@@ -284,6 +297,17 @@ IntParams int_params(md_ctx* c, double dt, const void* Br, const void* Bk) {
   p.Fr = c->Fr;
   p.Fk = c->Fk;
   p.ov = c->ov;
+  p.mexact = nullptr;
+  for (int q = 0; q < 6; q++) p.kself[q] = c->kself[q];
+  p.sv = StrongView{};
+  p.sv.flags = &c->sc->flags;
+  if (strong_active(c)) {
+    p.sv.off = c->snbr_off;
+    p.sv.cap = c->scap;
+    p.sv.B = Br == c->Br2 ? c->svals2 : c->svals;
+    p.sv.F = c->svals + 3 * c->scap;
+    p.sv.P = c->svals + 6 * c->scap;
+  }
   p.s = sorted_view(c);
   p.musum = c->sc->musum;
   p.obs_part = c->obs_part;
@@ -399,6 +423,84 @@ int alloc_nbr(md_ctx* c, long long cap) {
   return MD_OK;
 }
 
+bool strong_active(const md_ctx* c) {
+  return !fp64(c) && !c->cfg.ENABLE_COATING_POT && c->strong_w4sq > 0.f && c->scap > 0 && c->snbr_off;
+}
+
+int alloc_strong(md_ctx* c, long long cap) {
+  cap = std::min<long long>(cap, 0x7ffffffeLL);
+  if (cap <= c->scap) return MD_OK;
+  dfree(c, c->snbr);
+  dfree(c, c->svals);
+  dfree(c, c->svals2);
+  c->snbr = nullptr;
+  c->svals = c->svals2 = nullptr;
+  c->scap = 0;
+  int st = dalloc(c, &c->snbr, sizeof(int2) * (size_t)cap);
+  if (!st) st = dalloc(c, &c->svals, 9 * sizeof(double) * (size_t)cap);
+  if (!st) st = dalloc(c, &c->svals2, 3 * sizeof(double) * (size_t)cap);
+  if (st) return st;
+  c->scap = cap;
+  invalidate_graph(c);
+  return MD_OK;
+}
+
+// Threshold of the strong pairs in kernel units: the force weight
+// (|mu_i| |mu_j| / mu_min^2) (d_min / r)^4, d_min = 2 min rHydr (the scale
+// of the reference's relative error, src/interaction.cpp:180), exceeds
+// strong_theta  <=>  |mu_i|^2 |mu_j|^2 > w4sq r^8 with moments in mu_max
+// and r in box lengths.  A monodisperse system has no pair above theta >= 1.
+void update_strong(md_ctx* c) {
+  c->strong_w4sq = -1.f;
+  if (fp64(c) || !(c->strong_theta > 0) || !c->have_particles || c->props.magMom.empty()) return;
+  double mmin = 1e300, rhmin = 1e300;
+  for (size_t i = 0; i < c->props.magMom.size(); i++) {
+    mmin = std::min(mmin, c->props.magMom[i]);
+    rhmin = std::min(rhmin, c->props.rHydr[i]);
+  }
+  const double q = mmin / c->props.muMax, dl = c->L / (2.0 * rhmin);
+  const double w4 = c->strong_theta * q * q * dl * dl * dl * dl;
+  const double w4sq = w4 * w4;
+  c->strong_w4sq = w4sq < 3.0e38 ? (float)w4sq : -1.f;
+}
+
+// Expected entries of the strong list at uniform density: particles binned
+// by log moment (48 bins; per bin the largest moment and the smallest
+// hydrodynamic radius, so the estimate errs high), and per bin pair the
+// shell between contact and the distance where the weight falls to theta
+// (2 * 1.25e5 entries estimated vs 1.22e5 built for N = 32768, log-normal
+// sigma 0.2).
+double strong_estimate(const md_ctx* c) {
+  const std::vector<double>& m = c->props.magMom;
+  const std::vector<double>& rh = c->props.rHydr;
+  if (m.empty() || !(c->strong_theta > 0)) return 0;
+  double mmin = 1e300, mmax = 0, rhmin = 1e300;
+  for (size_t i = 0; i < m.size(); i++) {
+    mmin = std::min(mmin, m[i]);
+    mmax = std::max(mmax, m[i]);
+    rhmin = std::min(rhmin, rh[i]);
+  }
+  const int nb = 48;
+  const double span = std::log(mmax / mmin) * (1.0 + 1e-9) + 1e-12;
+  std::vector<double> cnt(nb, 0.0), mb(nb, 0.0), rb(nb, 1e300);
+  for (size_t i = 0; i < m.size(); i++) {
+    const int b = std::min(nb - 1, (int)(std::log(m[i] / mmin) / span * nb));
+    cnt[b] += 1;
+    mb[b] = std::max(mb[b], m[i]);
+    rb[b] = std::min(rb[b], rh[i]);
+  }
+  const double pi = 3.141592653589793, V = c->L * c->L * c->L, dmin = 2.0 * rhmin;
+  double tot = 0;
+  for (int a = 0; a < nb; a++)
+    for (int b = 0; b < nb; b++) {
+      if (cnt[a] == 0 || cnt[b] == 0) continue;
+      const double rs = dmin * std::pow(mb[a] * mb[b] / (mmin * mmin * c->strong_theta), 0.25);
+      const double rc = std::min(rs, c->rc * (1.0 + c->skin_frac)), cont = rb[a] + rb[b];
+      if (rc > cont) tot += cnt[a] * cnt[b] * 4.0 / 3.0 * pi * (rc * rc * rc - cont * cont * cont) / V;
+    }
+  return tot;
+}
+
 // After work on the stream: a neighbour list that did not fit was replaced by
 // the direct cell scan (results are correct); grow it for the next steps.
 static int handle_overflow(md_ctx* c, const StepFlags& f);
@@ -411,6 +513,17 @@ int check_overflow(md_ctx* c) {
 }
 
 static int handle_overflow(md_ctx* c, const StepFlags& f) {
+  if (f.soverflow && !f.overflow && strong_active(c)) {
+    // the strong list did not fit (or the last build did not classify):
+    // grow it if needed and classify again at the next step
+    int total = 0;
+    CK(c, cudaMemcpy(&total, c->snbr_off + c->n, sizeof(int), cudaMemcpyDeviceToHost));
+    if (total > c->scap || total < 0) {
+      const long long need = (total > 0 && total < 0x7fffffff) ? (long long)(total * 1.25) + 4LL * c->n : 2 * c->scap;
+      if (int st = alloc_strong(c, need)) return st;
+    }
+    if (int st = force_rebuild(c)) return st;
+  }
   if (!f.overflow) return MD_OK;
   int total = 0;
   CK(c, cudaMemcpy(&total, c->nbr_off + c->n, sizeof(int), cudaMemcpyDeviceToHost));
@@ -631,8 +744,15 @@ int md_ctx_create(const md_config* cfg, int64_t n, int precision, md_ctx** out) 
   if ((st = dalloc(c, &c->xbuild, 24 * N))) return fail(st);
   if ((st = dalloc(c, &c->Ppart, 24 * N))) return fail(st);
   if ((st = dalloc(c, &c->obs_part, 56 * (size_t)std::max(int_blocks((int)n), int_blocks_one((int)n))))) return fail(st);
+  if (!fp64(c)) {
+    if ((st = dalloc(c, &c->snbr_cnt, 4 * N)) || (st = dalloc(c, &c->snbr_off, 4 * (N + 1)))) return fail(st);
+    if (cudaMemsetAsync(c->snbr_off, 0, 4 * (N + 1), c->stream) != cudaSuccess)
+      return fail(set_err(nullptr, MD_ERR_CUDA, "initial memset failed"));
+  }
   if ((st = dalloc(c, &c->sc, sizeof(DevScalars)))) return fail(st);
+  static const int one = 1;
   if (cudaMemsetAsync(c->sc, 0, sizeof(DevScalars), c->stream) != cudaSuccess ||
+      cudaMemcpyAsync(&c->sc->flags.soverflow, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->xi, 0, 72 * N, c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->Ppart, 0, 24 * N, c->stream) != cudaSuccess)
     return fail(set_err(nullptr, MD_ERR_CUDA, "initial memset failed"));
@@ -924,6 +1044,22 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
   CK(c, cudaMemcpy(c->chunks, c->klist.chunks.data(), sizeof(int) * c->klist.chunks.size(), cudaMemcpyHostToDevice));
   if (int st = setup_tc(c)) return st;
   {
+    // k-space self-interaction: B_i holds -cflux sum_k e(k) (n . mu_i) n of
+    // each particle's own moment (the k list's e(k) covers the half space)
+    double K[6] = {0, 0, 0, 0, 0, 0};
+    for (size_t k = 0; k < c->klist.ek.size(); k++) {
+      if (!c->klist.kreal[k]) continue;
+      const double e = c->klist.ek[k], nx = c->klist.kx[k], ny = c->klist.ky[k], nz = c->klist.kz[k];
+      K[0] += e * nx * nx;
+      K[1] += e * ny * ny;
+      K[2] += e * nz * nz;
+      K[3] += e * nx * ny;
+      K[4] += e * nx * nz;
+      K[5] += e * ny * nz;
+    }
+    for (int q = 0; q < 6; q++) c->kself[q] = 4.0 * c->cfg.my_pi * K[q];
+  }
+  {
     // neighbour-list capacity: uniform-density estimate + margin (grown on overflow)
     const double rlb = rc / c->L * (1.0 + c->skin_frac);
     double est = (double)c->n * (double)c->n * 4.0 / 3.0 * 3.141592653589793 * rlb * rlb * rlb;
@@ -931,6 +1067,9 @@ int md_set_ewald(md_ctx* c, double alpha, double rc, int64_t kc) {
     int st = alloc_nbr(c, (long long)(1.3 * est) + 64LL * c->n);
     if (st) return st;
   }
+  update_strong(c);
+  if (c->strong_w4sq > 0.f && !c->cfg.ENABLE_COATING_POT)
+    if (int st = alloc_strong(c, 4096 + (long long)(2.0 * strong_estimate(c)))) return st;
   if (int st = force_rebuild(c)) return st;
   c->have_ewald = true;
   c->have_geometry = false;
@@ -964,7 +1103,19 @@ int md_compute_interactions(md_ctx* c, double* B, double* F, double* P3) {
   if (st) return st;
   if ((st = force_rebuild(c))) return st;
   c->launches = issue_interactions(c);
+  if (strong_active(c)) {
+    // a strong list that did not fit its estimate: grown, built again and
+    // evaluated again, so the returned result has its strong pairs in FP64
+    StepFlags f0;
+    CK(c, cudaMemcpyAsync(&f0, &c->sc->flags, sizeof f0, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (f0.soverflow && !f0.overflow) {
+      if ((st = handle_overflow(c, f0))) return st;
+      c->launches = issue_interactions(c);
+    }
+  }
   IntParams ip = int_params(c, 0.0, c->Br, c->Bk);
+  if (!fp64(c)) ip.mexact = c->mm;
   c->launches += launch_combine(c->stream, ip, c->Bout, c->Fout, 1, fp64(c));
   CK(c, cudaGetLastError());
   const size_t Bz = 24 * (size_t)c->n;
@@ -972,10 +1123,26 @@ int md_compute_interactions(md_ctx* c, double* B, double* F, double* P3) {
   if (F) CK(c, cudaMemcpyAsync(F, c->Fout, Bz, cudaMemcpyDeviceToHost, c->stream));
   std::vector<double> pp(3 * (size_t)c->n);
   CK(c, cudaMemcpyAsync(pp.data(), c->Ppart, 8 * pp.size(), cudaMemcpyDeviceToHost, c->stream));
+  StepFlags fl{};
+  int stotal = 0;
+  if (strong_active(c)) {
+    CK(c, cudaMemcpyAsync(&fl, &c->sc->flags, sizeof fl, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(&stotal, c->snbr_off + c->n, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  }
   CK(c, cudaStreamSynchronize(c->stream));
+  // pressure of the strong pairs: their FP64 terms, summed here
+  double sp3[3] = {0, 0, 0};
+  if (strong_active(c) && !fl.overflow && !fl.soverflow && stotal > 0 && stotal <= c->scap) {
+    std::vector<double> sp(3 * (size_t)stotal);
+    for (int q = 0; q < 3; q++)
+      CK(c, cudaMemcpy(sp.data() + (size_t)q * stotal, c->svals + (6 + q) * c->scap, 8 * (size_t)stotal,
+                       cudaMemcpyDeviceToHost));
+    for (int q = 0; q < 3; q++)
+      for (int e = 0; e < stotal; e++) sp3[q] += sp[(size_t)q * stotal + e];
+  }
   if ((st = check_overflow(c))) return st;
   if (P3) {
-    double s[3] = {0, 0, 0};
+    double s[3] = {sp3[0], sp3[1], sp3[2]};
     for (size_t b = 0; b < pp.size() / 3; b++)
       for (int q = 0; q < 3; q++) s[q] += pp[3 * b + q];
     const double sc = c->L * F_unit(c) / 2.0;
@@ -995,6 +1162,7 @@ int md_compute_field(md_ctx* c, const double* mm, double* B) {
   c->launches = launch_set_mu(c->stream, (int)c->n, c->tmpmm, c->magMom_u, c->rMag_u, s, fp64(c));
   c->launches += issue_field(c);
   IntParams ip = int_params(c, 0.0, c->Br2, c->Bk2);
+  if (!fp64(c)) ip.mexact = c->tmpmm;
   c->launches += launch_combine(c->stream, ip, c->Bout, nullptr, 0, fp64(c));
   CK(c, cudaGetLastError());
   if (B) CK(c, cudaMemcpyAsync(B, c->Bout, 24 * (size_t)c->n, cudaMemcpyDeviceToHost, c->stream));
@@ -1417,6 +1585,31 @@ int md_set_neighbor_skin(md_ctx* c, double skin_frac) {
   return force_rebuild(c);
 }
 
+int md_set_strong_pairs(md_ctx* c, double theta) {
+  if (!c || !(theta >= 0)) return set_err(c, MD_ERR_INVALID, "strong-pair threshold must be >= 0 (0: off)");
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->strong_theta = theta;
+  invalidate_graph(c);
+  if (!c->have_ewald) return MD_OK;
+  update_strong(c);
+  if (c->strong_w4sq > 0.f && !c->cfg.ENABLE_COATING_POT)
+    if (int st = alloc_strong(c, 4096 + (long long)(2.0 * strong_estimate(c)))) return st;
+  return force_rebuild(c);
+}
+
+int md_debug_strong_pairs(md_ctx* c, int64_t* entries) {
+  if (!c || !entries) return set_err(c, MD_ERR_INVALID, "null argument");
+  *entries = 0;
+  if (!strong_active(c)) return MD_OK;
+  CK(c, cudaStreamSynchronize(c->stream));
+  StepFlags f;
+  int total = 0;
+  CK(c, cudaMemcpy(&f, &c->sc->flags, sizeof f, cudaMemcpyDeviceToHost));
+  CK(c, cudaMemcpy(&total, c->snbr_off + c->n, sizeof(int), cudaMemcpyDeviceToHost));
+  *entries = (f.overflow || f.soverflow) ? -1 : total;
+  return MD_OK;
+}
+
 int md_debug_real_part(md_ctx* c, double* B, double* F) {
   if (!c || !B || !F) return set_err(c, MD_ERR_INVALID, "null argument");
   if (!c->have_geometry) return set_err(c, MD_ERR_INVALID, "call md_compute_interactions first");
@@ -1523,8 +1716,7 @@ int md_autotune_ewald(md_ctx* c, int ncand, double* alpha_out, double* rc_out, i
     for (int rep = 0; rep < 3; rep++) {
       CK(c, cudaEventRecord(e0, c->stream));
       issue_interactions(c);
-      launch_real(c->stream, real_params(c, c->Br2, nullptr, nullptr), false, fp64(c));
-      launch_kspace(c->stream, k_params(c, c->Bk2, nullptr), false, fp64(c));
+      issue_field(c);
       CK(c, cudaEventRecord(e1, c->stream));
       CK(c, cudaEventSynchronize(e1));
       float ms = 0;

@@ -135,6 +135,18 @@ struct md_ctx {
   // nm) is crossed only after ~1e4 steps and rebuilds stay rare.
   double skin_frac = 0.005;
   bool list_valid = false;  // a build for the current particles, grid and skin exists
+  // Strong pairs (mixed path, md_real.cu): list entries whose force weight
+  // (|mu_i| |mu_j| / mu_min^2) (2 rHydr_min / r)^4 exceeds strong_theta are
+  // evaluated in FP64; strong_w4sq is that threshold in kernel units
+  // (squared, for |mu_i|^2 |mu_j|^2 > w4sq r^8; < 0: off).
+  double kself[6] = {0, 0, 0, 0, 0, 0};  // k-space self-interaction matrix (IntParams::kself)
+  double strong_theta = 3.0;
+  float strong_w4sq = -1.f;
+  int2* snbr = nullptr;
+  int *snbr_cnt = nullptr, *snbr_off = nullptr;
+  double* svals = nullptr;   // [9][scap] FP64 B, F, P terms per entry (full evaluation)
+  double* svals2 = nullptr;  // [3][scap] FP64 B terms per entry (field-only evaluation)
+  long long scap = 0;
   // profiling: events between the kernel segments of a step
   bool prof = false;
   cudaEvent_t ev[MD_NSEG + 1] = {};
@@ -173,6 +185,11 @@ md::ObsParams obs_params(md_ctx* c, double dt);
 int check_ready(md_ctx* c, bool need_state);
 int force_rebuild(md_ctx* c);
 int alloc_nbr(md_ctx* c, long long cap);
+// Strong-pair path: on for the mixed path without coating potentials and
+// with a finite threshold; alloc_strong grows the strong list.
+bool strong_active(const md_ctx* c);
+int alloc_strong(md_ctx* c, long long cap);
+void update_strong(md_ctx* c);
 int check_overflow(md_ctx* c);
 int ensure_records(md_ctx* c, int64_t extra);
 int read_err_word(md_ctx* c);

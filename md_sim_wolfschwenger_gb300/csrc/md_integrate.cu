@@ -81,6 +81,8 @@ __device__ __forceinline__ void demag_si(const IntParams& p, int r, R b[3]) {
   const int n = p.n;
   const T* Br = (const T*)p.Br;
   const T* Bk = (const T*)p.Bk;
+  double sb[3];  // strong pairs (FP64 terms), mixed path
+  const bool hs = p.sv.sum3(p.sv.B, r, sb);
   const T4 mu = ((const T4*)p.s.mu)[r];
   if constexpr (std::is_same<R, float>::value) {
     // mixed integrator: the FP32 stage outputs combined in FP32 (FP64 runs
@@ -90,14 +92,34 @@ __device__ __forceinline__ void demag_si(const IntParams& p, int r, R b[3]) {
     const float cs = (float)p.cself, cu = (float)p.csurf, bu = (float)p.B_unit;
     const float mu3[3] = {(float)mu.x, (float)mu.y, (float)mu.z};
 #pragma unroll
-    for (int a = 0; a < 3; a++)
-      b[a] = (((float)Br[a * n + r] + (float)Bk[a * n + r]) + (cs * mu3[a] - cu * (float)p.musum[a])) * bu;
+    for (int a = 0; a < 3; a++) {
+      const float br = hs ? (float)Br[a * n + r] + (float)sb[a] : (float)Br[a * n + r];
+      b[a] = ((br + (float)Bk[a * n + r]) + (cs * mu3[a] - cu * (float)p.musum[a])) * bu;
+    }
   } else {
-    const double mu3[3] = {(double)mu.x, (double)mu.y, (double)mu.z};
+    double mu3[3] = {(double)mu.x, (double)mu.y, (double)mu.z};
+    double kfix[3] = {0.0, 0.0, 0.0};
+    if (std::is_same<R, double>::value && p.mexact) {
+      // FP64 moment of particle i (sorted slot r): the self term uses it, and
+      // the k-space sum's self-interaction -kself mu is moved from the moment
+      // it was evaluated with (the sorted view's) to this one
+      const int i = p.s.perm[r];
+      const double g = p.magMom_u[i];
+      const double me[3] = {p.mexact[i] * g, p.mexact[n + i] * g, p.mexact[2 * n + i] * g};
+      const double d[3] = {mu3[0] - me[0], mu3[1] - me[1], mu3[2] - me[2]};
+      const double* K = p.kself;
+      kfix[0] = K[0] * d[0] + K[3] * d[1] + K[4] * d[2];
+      kfix[1] = K[3] * d[0] + K[1] * d[1] + K[5] * d[2];
+      kfix[2] = K[4] * d[0] + K[5] * d[1] + K[2] * d[2];
+      mu3[0] = me[0];
+      mu3[1] = me[1];
+      mu3[2] = me[2];
+    }
 #pragma unroll
     for (int a = 0; a < 3; a++) {
       const double selfsurf = p.cself * mu3[a] - p.csurf * p.musum[a];
-      b[a] = (R)((((double)Br[a * n + r] + (double)Bk[a * n + r]) + selfsurf) * p.B_unit);
+      const double br = (double)Br[a * n + r] + sb[a];
+      b[a] = (R)(((br + ((double)Bk[a * n + r] + kfix[a])) + selfsurf) * p.B_unit);
     }
   }
 }
@@ -181,6 +203,12 @@ __device__ __forceinline__ void finish_particle(const IntParams& p, int i, int r
   acc[4] = p.Ppart[3 * i];
   acc[5] = p.Ppart[3 * i + 1];
   acc[6] = p.Ppart[3 * i + 2];
+  double sp[3], sf[3];  // strong pairs of the full evaluation (FP64 terms)
+  const bool hs = p.sv.sum3(p.sv.P, r, sp);
+  p.sv.sum3(p.sv.F, r, sf);
+  acc[4] += sp[0];
+  acc[5] += sp[1];
+  acc[6] += sp[2];
   const T nm = sqrt(mn[0] * mn[0] + mn[1] * mn[1] + mn[2] * mn[2]);
   const T ne = sqrt(en[0] * en[0] + en[1] * en[1] + en[2] * en[2]);
   const T* Fr = (const T*)p.Fr;
@@ -196,10 +224,11 @@ __device__ __forceinline__ void finish_particle(const IntParams& p, int i, int r
     p.mm[a * n + i] = (double)mf;
     p.ea[a * n + i] = (double)ef;
     T f;
+    const T fr = hs ? Fr[a * n + r] + (T)sf[a] : Fr[a * n + r];
     if constexpr (std::is_same<T, float>::value)
-      f = (Fr[a * n + r] + Fk[a * n + r]) * (float)p.F_unit + fth[a];
+      f = (fr + Fk[a * n + r]) * (float)p.F_unit + fth[a];
     else
-      f = (Fr[a * n + r] + Fk[a * n + r]) * p.F_unit + fth[a];
+      f = (fr + Fk[a * n + r]) * p.F_unit + fth[a];
     double x = p.pos[a * n + i] + (double)ov[a * n + r] * L + dtd * (double)(f * izt);
     if (x > half) x -= L;
     if (x < -half) x += L;
@@ -370,11 +399,13 @@ __global__ void k_combine(IntParams p, double* Bout, double* Fout, int apply_ove
   const int r = p.s.rank[i];
   double b[3];  // reported field: no rounding to the integrator's type
   demag_si<T, double>(p, r, b);
+  double sf[3];
+  p.sv.sum3(p.sv.F, r, sf);
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     if (Bout) Bout[a * n + i] = b[a];
-    if (Fout)
-      Fout[a * n + i] = ((double)((const T*)p.Fr)[a * n + r] + (double)((const T*)p.Fk)[a * n + r]) * p.F_unit;
+    if (Fout) Fout[a * n + i] = ((double)((const T*)p.Fr)[a * n + r] + sf[a] + (double)((const T*)p.Fk)[a * n + r]) *
+                                p.F_unit;
     if (apply_overlap) p.pos[a * n + i] += (double)((const T*)p.ov)[a * n + r] * p.L;
   }
 }
@@ -387,10 +418,13 @@ __global__ void k_real_part(IntParams p, double* Bout, double* Fout) {
   const int n = p.n;
   if (i >= n) return;
   const int r = p.s.rank[i];
+  double sb[3], sf[3];
+  p.sv.sum3(p.sv.B, r, sb);
+  p.sv.sum3(p.sv.F, r, sf);
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    Bout[a * n + i] = (double)((const T*)p.Br)[a * n + r] * p.B_unit;
-    Fout[a * n + i] = (double)((const T*)p.Fr)[a * n + r] * p.F_unit;
+    Bout[a * n + i] = ((double)((const T*)p.Br)[a * n + r] + sb[a]) * p.B_unit;
+    Fout[a * n + i] = ((double)((const T*)p.Fr)[a * n + r] + sf[a]) * p.F_unit;
   }
 }
 

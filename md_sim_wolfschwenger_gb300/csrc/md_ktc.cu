@@ -26,11 +26,12 @@
 // added into one accumulator (measured at N = 32768: 5.5e-6 relative error
 // of S with 392 particles per accumulator, 1.8e-6 with 128), so the
 // structure factor uses chunks of <= 512 particles (4 accumulators of <= 128
-// each, added in FP32) and sums the chunks with compensated FP32 sums (in
-// two levels); the scatter sums over the nx of a row in the MMA (<= 2 kc + 1 terms),
-// over the rows of a tile in FP32 and over tiles with compensated FP32 sums.
-// All sums have a
-// fixed order: results are deterministic.
+// each, added in FP32) and sums the chunks exactly (error-free FP32 pairs,
+// then FP64), like the reference's FP64 sums over particles; the scatter sums
+// over the nx of a row in the MMA
+// (<= 2 kc + 1 terms), over the rows of a tile in FP32 and over tiles with
+// compensated FP32 sums.  All sums have a fixed order: results are
+// deterministic.
 //
 // Kernels:
 //   k_tc_prep    once per step (positions are frozen across the step's
@@ -44,8 +45,8 @@
 //                dealt round-robin, one accumulator each, added in a fixed
 //                order at the end); mbarriers hand stages between the roles
 //                and tcgen05.commit releases the slots.
-//   k_sf_tc_reduce  compensated sum of the chunk partials, S(n) = C_U + nx C_V,
-//                e(n) S(n), and the scatter's W operand image (hi, lo) in
+//   k_sf_tc_reduce  exact sum of the chunk partials (TwoSum pairs, then
+//                FP64), S(n) = C_U + nx C_V and e(n) S(n) in FP64, and the scatter's W operand image (hi, lo) in
 //                the shared-memory layout the scatter copies in bulk.
 //   k_kscat_tc   128 particles per block, their X phases (the A operand, hi
 //                and lo) in tensor memory; W tiles of 128 columns stream in
@@ -489,19 +490,24 @@ __device__ __forceinline__ void w_put(float* img, int kp, int row, int k, float 
 }
 
 // Block per (M tile, column q): 64 rows x 8 groups of chunks, the groups
-// combined in a fixed order.  The chunk partials are summed with compensated
-// FP32 sums (Kahan; GB300's FP64 rate is ~1/64 of FP32), then the 8 group
-// sums and their compensations in one more compensated FP32 sum.
-__device__ __forceinline__ void kahan_f(float& s, float& c, float v) {
-  const float y = v - c, t = s + y;
-  c = (t - s) - y;
+// combined in a fixed order.  The chunk partials (FP32 tensor-memory sums of
+// <= 512 particles) are added exactly: within a group with error-free FP32
+// transformations (TwoSum: the running sum and its exact rounding errors;
+// GB300's FP64 rate is a small fraction of FP32, so a conversion and an FP64
+// addition per partial would cost more than the whole FP32 reduction), the
+// group sum (sum + compensation) and the groups in FP64, as are S(n) = C_U +
+// nx C_V and e(n) S(n); the W image is then split into its FP32 operands.
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float v) {
+  const float t = s + v;
+  const float bp = t - s;
+  c += (s - (t - bp)) + (v - bp);  // the exact rounding error of s + v (Knuth)
   s = t;
 }
 
 template <bool FULL>
 __global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
   using L = ScatLayout<FULL>;
-  __shared__ float red[8][8][64];  // [group][sum, compensation x 4 values][row]
+  __shared__ double red[8][4][64];  // [group][4 values][row]
   const int Q = 2 * p.kc + 1;
   const int mtile = blockIdx.x / Q, q = blockIdx.x - mtile * Q;
   const int rl = threadIdx.x & 63, grp = threadIdx.x >> 6;
@@ -517,39 +523,30 @@ __global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
 #pragma unroll 4
   for (int c = grp; c < p.tc_nchunk; c += 8) {
     const float* bc = b + (size_t)c * cstride;
-    kahan_f(su[0], cu[0], bc[(2 * q) * 128 + rl]);
-    kahan_f(su[1], cu[1], bc[(2 * q + 1) * 128 + rl]);
-    kahan_f(su[2], cu[2], bc[(2 * q) * 128 + 64 + rl]);
-    kahan_f(su[3], cu[3], bc[(2 * q + 1) * 128 + 64 + rl]);
+    two_sum_acc(su[0], cu[0], bc[(2 * q) * 128 + rl]);
+    two_sum_acc(su[1], cu[1], bc[(2 * q + 1) * 128 + rl]);
+    two_sum_acc(su[2], cu[2], bc[(2 * q) * 128 + 64 + rl]);
+    two_sum_acc(su[3], cu[3], bc[(2 * q + 1) * 128 + 64 + rl]);
   }
 #pragma unroll
-  for (int v = 0; v < 4; v++) {
-    red[grp][2 * v][rl] = su[v];
-    red[grp][2 * v + 1][rl] = cu[v];
-  }
+  for (int v = 0; v < 4; v++) red[grp][v][rl] = (double)su[v] + (double)cu[v];
   __syncthreads();
   if (grp != 0) return;
-  // the groups' sums and compensations in one more compensated FP32 sum
-  float acc[4], cmp[4];
-#pragma unroll
-  for (int v = 0; v < 4; v++) acc[v] = cmp[v] = 0.f;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
   for (int g8 = 0; g8 < 8; g8++)
 #pragma unroll
-    for (int v = 0; v < 4; v++) {
-      kahan_f(acc[v], cmp[v], red[g8][2 * v][rl]);
-      kahan_f(acc[v], cmp[v], -red[g8][2 * v + 1][rl]);
-    }
-  const float ur = acc[0] - cmp[0], ui = acc[1] - cmp[1], vr = acc[2] - cmp[2], vi = acc[3] - cmp[3];
+    for (int v = 0; v < 4; v++) acc[v] += red[g8][v][rl];
   const int r = mtile * 64 + rl;
   if (r >= p.tc_rows) return;
   const int kk = p.tc_kmap[r * Q + q];
   if (kk < 0) return;
+  const double nxd = (double)(q - p.kc);
+  const double srd = fma(nxd, acc[2], acc[0]), sid = fma(nxd, acc[3], acc[1]);
+  p.S[kk] = make_double2(srd, sid);
+  const double ed = p.ek[kk];
+  const float er = (float)(ed * srd), ei = (float)(ed * sid);
   const float nx = (float)(q - p.kc);  // small integer: its powers below are exact
-  const float sr = fmaf(nx, vr, ur), si = fmaf(nx, vi, ui);
-  p.S[kk] = make_double2((double)sr, (double)si);
-  const float e = (float)p.ek[kk];
-  const float er = e * sr, ei = e * si;
   const int tt = r / L::RT, sl = r - tt * L::RT;
   const int kp = p.tc_kp;
   float* img = p.tc_w + (size_t)tt * 2 * kScCols * kp;

@@ -217,12 +217,15 @@ __host__ __device__ constexpr float erfc_c(double c) { return (float)(c * 1.4426
 
 // Pairs A and B: fixed-point pair vectors (dxf..), r2f = |d_fix|^2, the
 // neighbour moments ma, mb; inA, inB: the pair is within rc.  Pairs outside
-// get a harmless distance and weight 0.  Same formulas as pair_terms, with
-// the field sums of the field-only pass as two FMAs per component.
+// get a harmless distance and weight 0.  wA, wB: the pair's Ewald field,
+// force and pressure go into the sums (in range and not a strong pair, whose
+// terms the FP64 kernels add; the overlap push follows inA, inB).  Same
+// formulas as pair_terms, with the field sums of the field-only pass as two
+// FMAs per component.
 template <bool FULL>
 __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dxf, float2 dyf, float2 dzf, float2 r2f,
-                                            bool inA, bool inB, float rc2_fix, const float4& mi, const float4& ma,
-                                            const float4& mb, Acc<float>& a, Acc2& a2) {
+                                            bool inA, bool inB, bool wA, bool wB, float rc2_fix, const float4& mi,
+                                            const float4& ma, const float4& mb, Acc<float>& a, Acc2& a2) {
   const float sc = 2.3283064365386963e-10f;  // 2^-32 (exact scaling)
   r2f = pk(inA ? r2f.x : rc2_fix, inB ? r2f.y : rc2_fix);
   a.np += (int)inA + (int)inB;
@@ -280,7 +283,7 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
   if constexpr (FULL) {
     // field + force: packed coefficients, then each pair assembled in scalar
     // code (as pair_terms), which keeps fewer values live
-    const float2 w = pk(inA ? 1.f : 0.f, inB ? 1.f : 0.f);
+    const float2 w = pk(wA ? 1.f : 0.f, wB ? 1.f : 0.f);
     const float2 a1 = mul2(fma2(mul2(erfcv, ire2), ire, t), w);
     const float2 tw = mul2(t, w);
     const float2 a2c = fma2(mul2(pk1(3.f), a1), ire2, mul2(pk1(K.al2x2), tw));
@@ -316,7 +319,7 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
     // -a1, and a2 r^2 = (3 a1 ire2 + 2 alpha^2 t w) r2f 2^-64
     const float2 mjx = pk(ma.x, mb.x), mjy = pk(ma.y, mb.y), mjz = pk(ma.z, mb.z);
     const float2 d2 = fma2(mjz, uz, fma2(mjy, uy, mul2(mjx, ux)));
-    const float2 wn = pk(inA ? -1.f : 0.f, inB ? -1.f : 0.f);
+    const float2 wn = pk(wA ? -1.f : 0.f, wB ? -1.f : 0.f);
     const float2 a1n = mul2(fma2(mul2(erfcv, ire2), ire, t), wn);
     const float2 a2s = fma2(mul2(pk1(K.ka2n), a1n), ire2, mul2(pk1(K.kt2n), mul2(t, wn)));
     const float2 c1 = mul2(mul2(a2s, d2), r2f);
@@ -454,6 +457,10 @@ __device__ __forceinline__ void scan_rows(const RealParams& p, int k, int lane, 
 // ------------------------------------------------------- neighbour list
 
 // Count (FILL = false) or write (FILL = true) the neighbours within rc + skin.
+// On the mixed path with strong pairs on, each neighbour is also classified
+// (|mu_k|^2 |mu_j|^2 > strong_w4sq r^8 at this build): strong entries carry
+// the sign bit in the Verlet list and are copied, as (k, j), into the
+// strong list (unless that list overflowed in the count).
 template <typename T, bool FILL>
 __device__ __forceinline__ void nbr_build(const RealParams& p, int bx) {
   if (!p.flags->rebuild) return;
@@ -462,26 +469,49 @@ __device__ __forceinline__ void nbr_build(const RealParams& p, int bx) {
   const int k = bx * kRealWarps + wib;
   if (k >= p.n) return;
   const Self<T> me = load_self<T, false>(p, k);
-  int cnt = 0;
+  constexpr bool F32 = std::is_same<T, float>::value;
+  const bool cls = F32 && p.strong;
+  const float4* gmu = (const float4*)p.s.mu;
+  float mi2 = 0.f;
+  if (cls) {
+    const float4 m = gmu[k];
+    mi2 = m.x * m.x + m.y * m.y + m.z * m.z;
+  }
+  const bool sfill = FILL && cls && !p.flags->soverflow;
+  int cnt = 0, scnt = 0;
   int* out = FILL ? p.nbr + p.nbr_off[k] : nullptr;
-  scan_rows<T>(p, k, lane, me, p.rl2, [&](bool in, int j, float, float, float) {
+  int2* sout = sfill ? p.snbr + p.snbr_off[k] : nullptr;
+  scan_rows<T>(p, k, lane, me, p.rl2, [&](bool in, int j, float dx, float dy, float dz) {
+    bool st = false;
+    if (cls && in) {
+      const float4 mj = gmu[j];
+      const float r2 = dx * dx + dy * dy + dz * dz, r4 = r2 * r2;
+      st = mi2 * (mj.x * mj.x + mj.y * mj.y + mj.z * mj.z) > p.strong_w4sq * (r4 * r4);
+    }
     const unsigned mask = __ballot_sync(kFull, in);
-    if (FILL && in) out[cnt + __popc(mask & lanemask_lt())] = j;
+    const unsigned smask = __ballot_sync(kFull, st);
+    if (FILL && in) out[cnt + __popc(mask & lanemask_lt())] = (sfill && st) ? (int)((unsigned)j | 0x80000000u) : j;
+    if (sfill && st) sout[scnt + __popc(smask & lanemask_lt())] = make_int2(k, j);
     cnt += __popc(mask);
+    scnt += __popc(smask);
   });
-  if (!FILL && lane == 0) p.nbr_cnt[k] = cnt;
+  if (!FILL && lane == 0) {
+    p.nbr_cnt[k] = cnt;
+    if (cls) p.snbr_cnt[k] = scnt;
+  }
 }
 
-// Exclusive scan of the counts (one block); flags overflow.
-__device__ __forceinline__ void nbr_scan(const RealParams& p) {
-  StepFlags* flags = p.flags;
-  if (!flags->rebuild) return;
+// Exclusive scan of cnt[0, n) into off[0, n] by one block (every thread
+// calls it); returns the total to every thread.  Offsets saturate at
+// INT_MAX (the list is then flagged as overflowing).
+__device__ __forceinline__ long long block_scan_counts(const int* cnt, int* off, int n) {
   __shared__ long long wsum[32];
-  const int t = threadIdx.x, nt = blockDim.x, n = p.n;
+  __shared__ long long total;
+  const int t = threadIdx.x, nt = blockDim.x;
   const int per = (n + nt - 1) / nt;
   const int b = t * per, e = min(n, b + per);
   long long local = 0;
-  for (int i = b; i < e; i++) local += p.nbr_cnt[i];
+  for (int i = b; i < e; i++) local += cnt[i];
   const int lane = t & 31, w = t >> 5;
   long long incl = local;
 #pragma unroll
@@ -504,12 +534,129 @@ __device__ __forceinline__ void nbr_scan(const RealParams& p) {
   __syncthreads();
   long long run = wsum[w] + incl - local;
   for (int i = b; i < e; i++) {
-    p.nbr_off[i] = (int)min(run, (long long)0x7fffffff);
-    run += p.nbr_cnt[i];
+    off[i] = (int)min(run, (long long)0x7fffffff);
+    run += cnt[i];
   }
   if (t == nt - 1) {
-    p.nbr_off[n] = (int)min(run, (long long)0x7fffffff);
-    flags->overflow = run > p.nbr_cap ? 1 : 0;
+    off[n] = (int)min(run, (long long)0x7fffffff);
+    total = run;
+  }
+  __syncthreads();
+  const long long r = total;
+  __syncthreads();  // the shared scratch is reused by a second call
+  return r;
+}
+
+// Offsets of the Verlet list (and of the strong list); flags overflow.
+__device__ __forceinline__ void nbr_scan(const RealParams& p) {
+  StepFlags* flags = p.flags;
+  if (!flags->rebuild) return;
+  const long long tot = block_scan_counts(p.nbr_cnt, p.nbr_off, p.n);
+  long long stot = 0;
+  if (p.strong) stot = block_scan_counts(p.snbr_cnt, p.snbr_off, p.n);
+  if (threadIdx.x == 0) {
+    flags->overflow = tot > p.nbr_cap ? 1 : 0;
+    // a build that did not classify leaves the strong list unusable until the
+    // next build that does (the FP64 kernels then contribute nothing)
+    flags->soverflow = p.strong ? (stot > p.scap ? 1 : 0) : 1;
+  }
+}
+
+// ------------------------------------------------------------ strong pairs
+//
+// The FP32 pair maths rounds every pair term to ~1e-7 of its size.  In a
+// polydisperse system the reference's error scale is the contact force of
+// the smallest particles, and near-contact pairs of large particles carry
+// terms of ~10-100 such contact forces, so those few pairs (~0.2 % of the
+// list at N = 32768, log-normal sigma 0.2) hold most of the FP32 error.  They
+// are classified at each list build by the force weight |mu_i| |mu_j| / r^4
+// and evaluated in FP64 with the reference's formula
+// (src/interaction.cpp:396-417), one thread per entry of the strong list.
+// The FP32 passes do this work themselves: the warps of k_real take the
+// strong list in chunks of 32 entries, spread evenly over the grid, before
+// their own particle, so the FP64 pipe (a small fraction of the FP32 rate on
+// GB300, otherwise idle here) works under the FP32 pair loop of the other
+// warps.  Each entry's terms go to svals; the integrator adds a particle's
+// entries in list order (deterministic).  The FP32 pass keeps the overlap
+// push of these pairs; the distance is clamped to contact here too.
+template <bool FULL>
+__device__ __forceinline__ void strong_entry(const RealParams& p, int e) {
+  const int2 ij = p.snbr[e];
+  if ((unsigned)ij.x >= (unsigned)p.n || (unsigned)ij.y >= (unsigned)p.n) return;  // never after a build
+  const size_t cap = (size_t)p.scap;
+  const float4* gmu = (const float4*)p.s.mu;
+  const int4 xi = p.s.xi[ij.x], xj = p.s.xi[ij.y];
+  const float4 fi = gmu[ij.x], fj = gmu[ij.y];
+  const double sc = 2.3283064365386963e-10;  // 2^-32
+  // wrapping differences of the fixed-point coordinates: the exact minimum image
+  const double dx = (double)(int)((unsigned)xj.x - (unsigned)xi.x) * sc;
+  const double dy = (double)(int)((unsigned)xj.y - (unsigned)xi.y) * sc;
+  const double dz = (double)(int)((unsigned)xj.z - (unsigned)xi.z) * sc;
+  const double r2 = dx * dx + dy * dy + dz * dz;
+  double ire = rsqrt(r2), r = r2 * ire;
+  const double ux = dx * ire, uy = dy * ire, uz = dz * ire;
+  const double dcont = (double)fi.w + (double)fj.w + p.cont_eps;
+  if (r < dcont) {
+    r = dcont;
+    ire = 1.0 / r;
+  }
+  const double ire2 = ire * ire, re2 = r * r;
+  const double ex = exp(-p.al2 * re2);
+  const double t = p.c2a * ex * ire2;
+  const double a1 = erfc(p.alpha * r) * ire2 * ire + t;
+  const double a2 = 3.0 * a1 * ire2 + 2.0 * p.al2 * t;
+  double mix = fi.x, miy = fi.y, miz = fi.z, mjx = fj.x, mjy = fj.y, mjz = fj.z;
+  if (p.smm) {  // the master moments in FP64 (the sorted view holds them rounded to FP32)
+    const int n = p.n, pi = p.s.perm[ij.x], pj = p.s.perm[ij.y];
+    const double gi = p.smag[pi], gj = p.smag[pj];
+    mix = p.smm[pi] * gi;
+    miy = p.smm[n + pi] * gi;
+    miz = p.smm[2 * n + pi] * gi;
+    mjx = p.smm[pj] * gj;
+    mjy = p.smm[n + pj] * gj;
+    mjz = p.smm[2 * n + pj] * gj;
+  }
+  const double d2 = mjx * ux + mjy * uy + mjz * uz;
+  const double c1 = a2 * d2 * re2;
+  double* sv = p.svals;
+  sv[e] = c1 * ux - a1 * mjx;
+  sv[cap + e] = c1 * uy - a1 * mjy;
+  sv[2 * cap + e] = c1 * uz - a1 * mjz;
+  if constexpr (FULL) {
+    const double a3 = 5.0 * a2 * ire2 + 4.0 * p.al4 * t;
+    const double d1 = mix * ux + miy * uy + miz * uz;
+    const double m12 = mix * mjx + miy * mjy + miz * mjz;
+    const double s1 = (a2 * m12 - a3 * d1 * d2 * re2) * r;
+    const double s2 = a2 * r;
+    const double vx = s1 * ux + s2 * (d2 * mix + d1 * mjx);
+    const double vy = s1 * uy + s2 * (d2 * miy + d1 * mjy);
+    const double vz = s1 * uz + s2 * (d2 * miz + d1 * mjz);
+    sv[3 * cap + e] = -vx;
+    sv[4 * cap + e] = -vy;
+    sv[5 * cap + e] = -vz;
+    sv[6 * cap + e] = r * ux * vy;
+    sv[7 * cap + e] = r * ux * vz;
+    sv[8 * cap + e] = r * uy * vz;
+  }
+}
+
+// The chunks of the strong list that warp k (one warp per particle) takes:
+// with C chunks of 32 entries and n warps, every stride-th warp, stride =
+// n / C, takes one chunk (or each warp several when C > n).
+template <bool FULL>
+__device__ __forceinline__ void strong_chunks(const RealParams& p, int k, int lane) {
+  const StepFlags* fl = p.flags;
+  if (fl->overflow || fl->soverflow) return;
+  const int total = (int)min((long long)p.snbr_off[p.n], p.scap);
+  const int chunks = (total + 31) >> 5;
+  if (chunks == 0) return;
+  const int n = p.n;
+  const int stride = max(1, n / chunks);
+  if (k % stride) return;
+  const int step = (n + stride - 1) / stride;
+  for (int c = k / stride; c < chunks; c += step) {
+    const int e = c * 32 + lane;
+    if (e < total) strong_entry<FULL>(p, e);
   }
 }
 
@@ -523,6 +670,9 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = bx * NW + wib;
   if (k >= p.n) return;  // whole warp; no block-level synchronisation below
+  if constexpr (F32 && !COAT) {
+    if (p.strong && !p.flags->overflow) strong_chunks<FULL>(p, k, lane);
+  }
   Acc<T> a;
   Acc2 a2;  // packed sums (mixed path list loop)
   const T4 mi = ((const T4*)p.s.mu)[k];
@@ -575,11 +725,15 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
       // two batches of 32 entries per iteration, all gathers issued first;
       // the list indices of the next iteration are loaded one ahead, so a
       // gather waits on one memory round trip instead of two
+      // entries with the sign bit set are strong pairs (FP64 kernels) when
+      // the context evaluates them there, ordinary ones otherwise
+      const int sflag = p.strong ? (int)0x80000000u : 0;
       int ja_n = lane < cnt ? lst[lane] : k, jb_n = 32 + lane < cnt ? lst[32 + lane] : k;
       for (int t0 = 0; t0 < cnt; t0 += 64) {
         const int ta = t0 + lane, tb = t0 + 32 + lane;
         const bool va = ta < cnt, vb = tb < cnt;
-        const int ja = ja_n, jb = jb_n;
+        const bool sta = (ja_n & sflag) != 0, stb = (jb_n & sflag) != 0;
+        const int ja = ja_n & 0x7fffffff, jb = jb_n & 0x7fffffff;
         ja_n = ta + 64 < cnt ? lst[ta + 64] : k;
         jb_n = tb + 64 < cnt ? lst[tb + 64] : k;
         const int4 sa = p.s.xi[ja], sb = p.s.xi[jb];
@@ -594,7 +748,8 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
           const bool inA = va && r2f.x < rc2_fix, inB = vb && r2f.y < rc2_fix;
           // unconditional: nearly every iteration has a pair in range, and
           // entries out of range carry weight 0
-          pair_terms2<FULL>(p.pk, wdc, dxf, dyf, dzf, r2f, inA, inB, rc2_fix, mi, ma, mb, a, a2);
+          pair_terms2<FULL>(p.pk, wdc, dxf, dyf, dzf, r2f, inA, inB, inA && !sta, inB && !stb, rc2_fix, mi, ma,
+                            mb, a, a2);
         } else {
           if (va) eval_loaded(sa, ma);
           if (vb) eval_loaded(sb, mb);
@@ -603,7 +758,7 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
     } else {
       int jn = lane < cnt ? lst[lane] : 0;
       for (int t0 = 0; t0 < cnt; t0 += 32) {
-        const int j = jn;
+        const int j = jn & 0x7fffffff;
         const bool valid = t0 + lane < cnt;
         if (t0 + 32 + lane < cnt) jn = lst[t0 + 32 + lane];
         if (valid) eval(j);
@@ -671,6 +826,17 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
   }
 }
 
+static int num_sms() {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
+  }
+  return nsm;
+}
+
+
 // ------------------------------------------------------------ entry points
 
 // Grid-stride over the particle blocks: most steps do not rebuild, and a
@@ -708,12 +874,7 @@ __global__ void __launch_bounds__(kRealWarps * 32, COAT ? 2 : 4) k_real_packed(c
 int real_blocks(int n) { return (n + kRealWarps - 1) / kRealWarps; }
 
 int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64) {
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
-  }
+  const int nsm = num_sms();
   const int nblk = real_blocks(p.n);
   dim3 grid(std::min(nblk, 8 * nsm)), block(kRealWarps * 32);
   if (fp64)

@@ -322,6 +322,18 @@ class Simulation:
         """Skin of the real-space neighbour list as a fraction of rc."""
         self._ck(self.L.md_set_neighbor_skin(self.h, float(skin_frac)))
 
+    def set_strong_pairs(self, theta):
+        """Mixed path: pairs above theta contact forces of the smallest
+        particles ((|mu_i||mu_j|/mu_min^2)(2 rHydr_min/r)^4) are evaluated in
+        FP64 (default 3; 0 turns it off)."""
+        self._ck(self.L.md_set_strong_pairs(self.h, float(theta)))
+
+    def strong_pairs(self):
+        """Entries of the strong-pair list of the last build (0: off, -1: not in use)."""
+        v = C.c_int64()
+        self._ck(self.L.md_debug_strong_pairs(self.h, C.byref(v)))
+        return v.value
+
     def neighbor_capacity(self, cap=0):
         """Entries of the last neighbour list; cap > 0 caps the capacity (test hook)."""
         used = C.c_int64()
