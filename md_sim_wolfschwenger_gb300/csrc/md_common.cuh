@@ -167,28 +167,45 @@ struct RealParams {
 };
 
 // The FP64 strong-pair terms of one evaluation, as the integrator reads
-// them: per sorted slot r, entries snbr_off[r] .. snbr_off[r + 1] of each
-// component array.  off == nullptr: the path is off; the flags say whether
-// the list of the last build is in use.
+// them.  The real-space kernel stores, per 32-entry chunk of the strong list
+// and owner particle, the owner's field and force sums at its first entry in
+// the chunk, and the chunk's pressure sum at the chunk's first entry.  Slot
+// r (entries off[r] .. off[r + 1]) thus adds its partials at off[r] and at
+// every chunk start inside its range, in that fixed order; the pressure
+// partial of a chunk belongs to the owner of the chunk's first entry.
+// off == nullptr: the path is off; the flags say whether the list of the
+// last build is in use.
 struct StrongView {
   const int* off;
   long long cap;
-  const double* B;  // [3][cap]
-  const double* F;  // [3][cap] (full evaluation)
-  const double* P;  // [3][cap] (full evaluation)
+  const double* B;  // [3][cap] (field of the evaluation)
+  const double* F;  // [3][cap] (force, full evaluation)
+  const double* P;  // [3][cap] (pressure, full evaluation)
   const StepFlags* flags;
-  // sum of nc components of a (stride cap) over slot r's entries, in list order
-  __device__ __forceinline__ bool sum3(const double* a, int r, double out[3]) const {
-    out[0] = out[1] = out[2] = 0.0;
-    if (!off || !a || flags->overflow || flags->soverflow) return false;
-    const int e1 = (int)min((long long)off[r + 1], cap);
-    for (int e = max(off[r], 0); e < e1; e++) {
-      out[0] += a[e];
-      out[1] += a[cap + e];
-      out[2] += a[2 * cap + e];
+  __device__ __forceinline__ bool usable() const { return off && !flags->overflow && !flags->soverflow; }
+  // sums of the 3-component arrays a (and b when given) over slot r's
+  // partials; pc: the pressure partials of the chunks slot r starts
+  __device__ __forceinline__ bool sums(int r, const double* a, double oa[3], const double* b = nullptr,
+                                       double* ob = nullptr, const double* pc = nullptr, double* op = nullptr) const {
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      oa[q] = 0.0;
+      if (ob) ob[q] = 0.0;
+      if (op) op[q] = 0.0;
+    }
+    if (!usable() || !a) return false;
+    const int e0 = max(off[r], 0), e1 = (int)min((long long)off[r + 1], cap);
+    for (int e = e0; e < e1; e = (e & ~31) + 32) {
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        oa[q] += a[q * cap + e];
+        if (b) ob[q] += b[q * cap + e];
+        if (pc && (e & 31) == 0) op[q] += pc[q * cap + e];
+      }
     }
     return true;
   }
+  __device__ __forceinline__ bool sum3(const double* a, int r, double out[3]) const { return sums(r, a, out); }
 };
 
 // --------------------------------------------------------- k space

@@ -1130,7 +1130,8 @@ int md_compute_interactions(md_ctx* c, double* B, double* F, double* P3) {
     CK(c, cudaMemcpyAsync(&stotal, c->snbr_off + c->n, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   }
   CK(c, cudaStreamSynchronize(c->stream));
-  // pressure of the strong pairs: their FP64 terms, summed here
+  // pressure of the strong pairs: the FP64 partial of each 32-entry chunk
+  // (stored at the chunk's first entry), summed here
   double sp3[3] = {0, 0, 0};
   if (strong_active(c) && !fl.overflow && !fl.soverflow && stotal > 0 && stotal <= c->scap) {
     std::vector<double> sp(3 * (size_t)stotal);
@@ -1138,7 +1139,7 @@ int md_compute_interactions(md_ctx* c, double* B, double* F, double* P3) {
       CK(c, cudaMemcpy(sp.data() + (size_t)q * stotal, c->svals + (6 + q) * c->scap, 8 * (size_t)stotal,
                        cudaMemcpyDeviceToHost));
     for (int q = 0; q < 3; q++)
-      for (int e = 0; e < stotal; e++) sp3[q] += sp[(size_t)q * stotal + e];
+      for (int e = 0; e < stotal; e += 32) sp3[q] += sp[(size_t)q * stotal + e];
   }
   if ((st = check_overflow(c))) return st;
   if (P3) {

@@ -75,14 +75,23 @@ __device__ __forceinline__ void rk(const IntParams& p, const T m[3], const T e[3
 // Demagnetising field of particle i (sorted slot r) in SI: the real- and
 // k-space sums and the self and surface terms combined in FP64, then
 // returned in the integrator's type T.
+// sbs: the strong-pair field sums of slot r when the caller has them already.
 template <typename T, typename R = T>
-__device__ __forceinline__ void demag_si(const IntParams& p, int r, R b[3]) {
+__device__ __forceinline__ void demag_si(const IntParams& p, int r, R b[3], const double* sbs = nullptr) {
   using T4 = typename V4<T>::t;
   const int n = p.n;
   const T* Br = (const T*)p.Br;
   const T* Bk = (const T*)p.Bk;
   double sb[3];  // strong pairs (FP64 terms), mixed path
-  const bool hs = p.sv.sum3(p.sv.B, r, sb);
+  bool hs;
+  if (sbs) {
+    sb[0] = sbs[0];
+    sb[1] = sbs[1];
+    sb[2] = sbs[2];
+    hs = true;
+  } else {
+    hs = p.sv.sum3(p.sv.B, r, sb);
+  }
   const T4 mu = ((const T4*)p.s.mu)[r];
   if constexpr (std::is_same<R, float>::value) {
     // mixed integrator: the FP32 stage outputs combined in FP32 (FP64 runs
@@ -196,16 +205,28 @@ __device__ __forceinline__ void heun1(const IntParams& p, int bx) {
 // step moves a particle far less than L / 2), so they equal the FP64
 // round(.../L) of the reference; the displacement since the list build only
 // feeds the rebuild test and is FP32.
+// sfp: the strong-pair force and pressure sums of slot r (6 values) when the
+// caller has them already.
 template <typename T>
 __device__ __forceinline__ void finish_particle(const IntParams& p, int i, int r, const T mn[3], const T en[3],
-                                                const T fth[3], double acc[7], float& disp2) {
+                                                const T fth[3], double acc[7], float& disp2,
+                                                const double* sfp = nullptr) {
   const int n = p.n;
   acc[4] = p.Ppart[3 * i];
   acc[5] = p.Ppart[3 * i + 1];
   acc[6] = p.Ppart[3 * i + 2];
   double sp[3], sf[3];  // strong pairs of the full evaluation (FP64 terms)
-  const bool hs = p.sv.sum3(p.sv.P, r, sp);
-  p.sv.sum3(p.sv.F, r, sf);
+  bool hs;
+  if (sfp) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      sf[q] = sfp[q];
+      sp[q] = sfp[3 + q];
+    }
+    hs = true;
+  } else {
+    hs = p.sv.sums(r, p.sv.F, sf, nullptr, nullptr, p.sv.P, sp);
+  }
   acc[4] += sp[0];
   acc[5] += sp[1];
   acc[6] += sp[2];
@@ -298,7 +319,11 @@ __device__ __forceinline__ void heun2(const IntParams& p, int bx) {
       bth[a] = th[(3 + a) * n + i];
       fth[a] = th[(6 + a) * n + i];
     }
-    demag_si<T>(p, r, bd);
+    // strong-pair partials: the field of this (field-only) evaluation, the
+    // force and pressure of the step's full evaluation, in one pass
+    double sb[3], sfp[6];
+    const bool hs = p.sv.sums(r, p.sv.B, sb, p.sv.F, sfp, p.sv.P, sfp + 3);
+    demag_si<T>(p, r, bd, hs ? sb : nullptr);
     const T bz = (T)ext_field_z(p, *p.time);
     T km[3], ke[3];
     rk<T>(p, m2, e2, bd, bz, bth, tau, (T)p.velEa1[i], (T)p.velEa2[i], km, ke);
@@ -309,7 +334,7 @@ __device__ __forceinline__ void heun2(const IntParams& p, int bx) {
       en[a] = e[a] + dt * (h * k1e[a] + h * ke[a]);
       mn[a] = m[a] + dt * (h * k1m[a] + h * km[a]);
     }
-    finish_particle<T>(p, i, r, mn, en, fth, acc, disp2);
+    finish_particle<T>(p, i, r, mn, en, fth, acc, disp2, hs ? sfp : nullptr);
   }
   step_block_sums(p, bx, acc, disp2);
 }

@@ -579,11 +579,42 @@ __device__ __forceinline__ void nbr_scan(const RealParams& p) {
 // warps.  Each entry's terms go to svals; the integrator adds a particle's
 // entries in list order (deterministic).  The FP32 pass keeps the overlap
 // push of these pairs; the distance is clamped to contact here too.
+// g1(s) = erfc(s) + (2 s / sqrt(pi)) exp(-s^2), the factor of 1/r^3 in the
+// pair coefficient a1 (s = alpha r).  From its power series for s <= 1.5:
+// g1 = 1 - (4 / sqrt(pi)) s^3 sum_k (-1)^k s^2k / (k! (2k + 3)), 18 terms
+// (relative error < 3e-10 at s = 1.5, at the FP64 rounding level below
+// s = 1), one branch-free polynomial instead of erfc's range branches;
+// beyond, with erfc.  ex = exp(-s^2).
+__device__ __forceinline__ double ewald_g1(double s, double ex) {
+  const double x = s * s;
+  if (x <= 2.25) {
+    double q = -7.598533119852758e-17;
+    q = fma(q, x, 1.3655649521106815e-15);
+    q = fma(q, x, -2.317322342975702e-14);
+    q = fma(q, x, 3.7002405153966856e-13);
+    q = fma(q, x, -5.537601323041936e-12);
+    q = fma(q, x, 7.732132217728926e-11);
+    q = fma(q, x, -1.0020843354176688e-09);
+    q = fma(q, x, 1.1981443140863431e-08);
+    q = fma(q, x, -1.3122532963802806e-07);
+    q = fma(q, x, 1.3053467000835422e-06);
+    q = fma(q, x, -1.1671335200746965e-05);
+    q = fma(q, x, 9.259259259259259e-05);
+    q = fma(q, x, -0.000641025641025641);
+    q = fma(q, x, 0.003787878787878788);
+    q = fma(q, x, -0.018518518518518517);
+    q = fma(q, x, 0.07142857142857142);
+    q = fma(q, x, -0.2);
+    q = fma(q, x, 0.3333333333333333);
+    return fma(-2.256758334191025 * s * x, q, 1.0);  // 4 / sqrt(pi)
+  }
+  return erfc(s) + 1.1283791670955126 * s * ex;  // 2 / sqrt(pi)
+}
+
+// The FP64 terms of strong entry (i, j): v[0..2] field, and for FULL
+// v[3..5] force, v[6..8] pressure.
 template <bool FULL>
-__device__ __forceinline__ void strong_entry(const RealParams& p, int e) {
-  const int2 ij = p.snbr[e];
-  if ((unsigned)ij.x >= (unsigned)p.n || (unsigned)ij.y >= (unsigned)p.n) return;  // never after a build
-  const size_t cap = (size_t)p.scap;
+__device__ __forceinline__ void strong_entry(const RealParams& p, int2 ij, double v[9]) {
   const float4* gmu = (const float4*)p.s.mu;
   const int4 xi = p.s.xi[ij.x], xj = p.s.xi[ij.y];
   const float4 fi = gmu[ij.x], fj = gmu[ij.y];
@@ -603,7 +634,7 @@ __device__ __forceinline__ void strong_entry(const RealParams& p, int e) {
   const double ire2 = ire * ire, re2 = r * r;
   const double ex = exp(-p.al2 * re2);
   const double t = p.c2a * ex * ire2;
-  const double a1 = erfc(p.alpha * r) * ire2 * ire + t;
+  const double a1 = ewald_g1(p.alpha * r, ex) * ire2 * ire;  // = erfc(alpha r) / r^3 + t
   const double a2 = 3.0 * a1 * ire2 + 2.0 * p.al2 * t;
   double mix = fi.x, miy = fi.y, miz = fi.z, mjx = fj.x, mjy = fj.y, mjz = fj.z;
   if (p.smm) {  // the master moments in FP64 (the sorted view holds them rounded to FP32)
@@ -618,10 +649,9 @@ __device__ __forceinline__ void strong_entry(const RealParams& p, int e) {
   }
   const double d2 = mjx * ux + mjy * uy + mjz * uz;
   const double c1 = a2 * d2 * re2;
-  double* sv = p.svals;
-  sv[e] = c1 * ux - a1 * mjx;
-  sv[cap + e] = c1 * uy - a1 * mjy;
-  sv[2 * cap + e] = c1 * uz - a1 * mjz;
+  v[0] = c1 * ux - a1 * mjx;
+  v[1] = c1 * uy - a1 * mjy;
+  v[2] = c1 * uz - a1 * mjz;
   if constexpr (FULL) {
     const double a3 = 5.0 * a2 * ire2 + 4.0 * p.al4 * t;
     const double d1 = mix * ux + miy * uy + miz * uz;
@@ -631,18 +661,23 @@ __device__ __forceinline__ void strong_entry(const RealParams& p, int e) {
     const double vx = s1 * ux + s2 * (d2 * mix + d1 * mjx);
     const double vy = s1 * uy + s2 * (d2 * miy + d1 * mjy);
     const double vz = s1 * uz + s2 * (d2 * miz + d1 * mjz);
-    sv[3 * cap + e] = -vx;
-    sv[4 * cap + e] = -vy;
-    sv[5 * cap + e] = -vz;
-    sv[6 * cap + e] = r * ux * vy;
-    sv[7 * cap + e] = r * ux * vz;
-    sv[8 * cap + e] = r * uy * vz;
+    v[3] = -vx;
+    v[4] = -vy;
+    v[5] = -vz;
+    v[6] = r * ux * vy;
+    v[7] = r * ux * vz;
+    v[8] = r * uy * vz;
   }
 }
 
 // The chunks of the strong list that warp k (one warp per particle) takes:
 // with C chunks of 32 entries and n warps, every stride-th warp, stride =
-// n / C, takes one chunk (or each warp several when C > n).
+// n / C, takes one chunk (or each warp several when C > n).  A chunk's
+// entries are grouped by owner particle (list order); the field and force
+// terms are added per owner within the chunk (segmented warp sum, fixed
+// order) and stored at the owner's first entry in the chunk, so a particle
+// has one partial per chunk it spans.  The pressure, needed only as a total,
+// is added over the whole chunk and stored at the chunk's first entry.
 template <bool FULL>
 __device__ __forceinline__ void strong_chunks(const RealParams& p, int k, int lane) {
   const StepFlags* fl = p.flags;
@@ -654,9 +689,42 @@ __device__ __forceinline__ void strong_chunks(const RealParams& p, int k, int la
   const int stride = max(1, n / chunks);
   if (k % stride) return;
   const int step = (n + stride - 1) / stride;
+  const size_t cap = (size_t)p.scap;
+  constexpr int NS = FULL ? 6 : 3;  // components summed per owner
   for (int c = k / stride; c < chunks; c += step) {
     const int e = c * 32 + lane;
-    if (e < total) strong_entry<FULL>(p, e);
+    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int owner = -1 - lane;  // lanes past the end: segments of their own
+    if (e < total) {
+      const int2 ij = p.snbr[e];
+      if ((unsigned)ij.x < (unsigned)n && (unsigned)ij.y < (unsigned)n) {  // always, after a build
+        owner = ij.x;
+        strong_entry<FULL>(p, ij, v);
+      }
+    }
+    // segmented suffix sums: lane l ends with the sum over [l, end of its run]
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int ow = __shfl_down_sync(kFull, owner, o);
+      const bool same = lane + o < 32 && ow == owner;
+#pragma unroll
+      for (int q = 0; q < NS; q++) {
+        const double t = __shfl_down_sync(kFull, v[q], o);
+        if (same) v[q] += t;
+      }
+    }
+    const int prev = __shfl_up_sync(kFull, owner, 1);
+    if (e < total && (lane == 0 || prev != owner)) {
+#pragma unroll
+      for (int q = 0; q < NS; q++) p.svals[q * cap + e] = v[q];
+    }
+    if constexpr (FULL) {
+#pragma unroll
+      for (int q = 6; q < 9; q++) {
+        const double t = warp_sum(v[q]);
+        if (lane == 0) p.svals[q * cap + e] = t;
+      }
+    }
   }
 }
 
@@ -847,8 +915,13 @@ __global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build(RealParams p, int
   for (int bx = blockIdx.x; bx < nblk; bx += gridDim.x) nbr_build<T, FILL>(p, bx);
 }
 __global__ void __launch_bounds__(1024) k_nbr_scan(RealParams p) { nbr_scan(p); }
+// The FP32 passes without coating keep the occupancy of their pair loops
+// (field: 9 blocks of 4 warps per SM, 56 registers; field + force: 7 blocks,
+// 72 registers): the FP64 strong-pair code in the same kernel must not
+// raise the register count.
 template <typename T, bool FULL, bool COAT>
-__global__ void __launch_bounds__(((FULL && COAT) ? kRealWarps : kFieldWarps) * 32) k_real(RealParams p) {
+__global__ void __launch_bounds__(((FULL && COAT) ? kRealWarps : kFieldWarps) * 32,
+                                  (std::is_same<T, float>::value && !COAT) ? (FULL ? 7 : 9) : 1) k_real(RealParams p) {
   real_eval<T, FULL, COAT, (FULL && COAT) ? kRealWarps : kFieldWarps>(p, blockIdx.x);
 }
 
