@@ -95,6 +95,16 @@ def workload_state(n, seed):
     return workloads.state(dict(W, n=n), seed)
 
 
+def bench_config(n, ws):
+    """The `config` object of the JSON line: the workload alone, identical in
+    both arms (per-run quantities such as the box length and the Ewald split
+    of the drawn system are reported under "system")."""
+    return {"workload": W["desc"], "n": n, "replicas_per_gpu": 1,
+            "parallelism": f"replicas x{ws}" if ws > 1 else "single instance",
+            "l2": "GPU arm: L2 flushed between timed steps (256 MiB write), step time from CUDA events on the "
+                  "library's stream; CPU arm: wall clock per step"}
+
+
 def oracle_ini(n, seed):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import ref_io
@@ -227,35 +237,59 @@ def cpu_baseline_port(n, sysd, ewald, seed, threads=1, steps=1):
 
 
 def run_reference(args):
+    """The reference's algorithm on the host cores: the C restatement of its
+    step (oracle/md_oracle.c: all-pairs list, FP64 real- and k-space Ewald
+    sums in the reference's loops, Heun step), one instance of the workload
+    with the pair list and Ewald sums spread over every host thread.  The
+    system (seeded log-normal radii, random sequential addition in index
+    order, uniform orientations) and the Ewald split (the library's cost
+    model over the reference's error model, restated in oracle.py) come from
+    oracle code only: this arm loads nothing of the CUDA library."""
     rank, ws, _ = dist_init()
     if rank != 0:
         return
-    n = args.n
-    sysd = workload_state(n, 1)
-    from md_sim_wolfschwenger_gb300 import MD_PREC_MIXED
-    import ctypes as C
-    import md_sim_wolfschwenger_gb300 as m
-    cfg = workload_config(n, 1)
-    a, r, k, ef, et, lb = (C.c_double(), C.c_double(), C.c_int64(), C.c_double(), C.c_double(), C.c_double())
-    P = lambda x: x.ctypes.data_as(C.POINTER(C.c_double))
-    m._lib.check(m.lib().md_ewald_params_host(C.byref(cfg.c), n, P(sysd[0]), P(sysd[1]), -1.0, C.byref(a),
-                                                C.byref(r), C.byref(k), C.byref(ef), C.byref(et), C.byref(lb)))
-    del MD_PREC_MIXED
-    threads = max(1, min(os.cpu_count() or 1, 16))
-    warm, steps = min(args.warmup, 1), max(1, min(args.steps, 3))
-    if warm:
-        cpu_baseline_port(n, sysd, (a.value, r.value, k.value), 7, threads=threads, steps=warm)
-    times, _ = cpu_baseline_port(n, sysd, (a.value, r.value, k.value), 7, threads=threads, steps=steps)
-    total = sum(times)
-    value = threads * n * steps / total
-    sample = (f"{steps} timed step(s) (+{warm} warm-up) of the full N={n} workload on each of {threads} "
-              f"concurrent single-threaded replicas; all-pairs list and FP64 Ewald as the reference")
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    n, seed = args.n, 1
+    rng = np.random.default_rng(1000 + seed)
+    rMag = W["median"] * np.exp(W["sigma"] * rng.standard_normal(n)) if W["sigma"] > 0 else np.full(n, W["median"])
+    rHydr = rMag + 5e-9
+    d = O.derive(oracle_ini(n, seed))
+    d["vis"] = 1e-3
+    d["ENABLE_THERM_TORQUE"] = d["ENABLE_THERM_FIELD"] = d["ENABLE_THERM_FORCE"] = True
+    d["magDamp"], d["satMag"], d["anisEn"] = 0.1, 4.8e5, 1.1e4
+    L = O.box_length(rHydr, W["phi"], d["my_pi"])
+    t0 = time.perf_counter()
+    pos = O.rsa_fast(n, L, rHydr, 7 + seed)
+    mm = rng.standard_normal((3, n))
+    mm /= np.linalg.norm(mm, axis=0)
+    ea = rng.standard_normal((3, n))
+    ea /= np.linalg.norm(ea, axis=0)
+    alpha, rc, kc = O.cost_model_rc(d, rMag, rHydr, L)
+    setup_s = time.perf_counter() - t0
+    threads = max(1, os.cpu_count() or 1)
+    o = O.Oracle(d, rMag, rHydr, L, alpha, rc, kc, vis=1e-3, overlap_mode=1)
+    o.set_threads(threads)
+    o.set_state(pos, mm, ea)
+    for _ in range(args.warmup):
+        o.step(1e-12, 2, None, seed)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step(1e-12, 2, None, seed)
+    total = time.perf_counter() - t0
+    pairs = o.pairs()
+    o.close()
+    value = n * args.steps / total
+    sample = (f"{args.steps} timed steps (+{args.warmup} warm-up) of one N={n} instance, the pair list and the Ewald "
+              f"sums spread over {threads} host threads; all-pairs list and FP64 Ewald in the reference's loops")
     line = {"impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
-            "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1e3 * total / steps,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": {"workload": W["desc"], "n": n,
-                                                     "ewald": {"alpha_L": a.value * lb.value,
-                                                               "rc_over_L": r.value / lb.value, "kc": k.value}},
+            "data": "synthetic (seeded log-normal radii, random sequential addition, moments and easy axes "
+                    "independent and uniform on the sphere)",
+            "config": bench_config(n, ws),
+            "system": {"lBox_m": L, "ewald": {"alpha_L": alpha * L, "rc_over_L": rc / L, "kc": kc, "pairs": pairs},
+                       "setup_s": setup_s},
             "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -693,14 +727,12 @@ def run_ours(args):
                               "surface terms, positions, reductions"),
                 "data": "synthetic (seeded log-normal radii, random sequential addition, moments and easy axes "
                         "independent and uniform on the sphere)",
-                "config": {"workload": W["desc"], "n": n, "lBox_m": L, "replicas_per_gpu": 1,
-                           "parallelism": f"replicas x{ws}" if ws > 1 else "single instance",
+                "config": bench_config(n, ws),
+                "system": {"lBox_m": L,
                            "ewald": {"alpha_L": alpha * L, "rc_over_L": rc / L, "kc": kc,
                                      "pred_force_err_rel_contact": errF, "pred_torque_err_rel_contact": errT,
                                      "pairs": pairs, "k_vectors": nk_real,
-                                     "strong_pair_entries_fp64": strong},
-                           "l2": "flushed between timed steps (256 MiB write); step time from CUDA events on the "
-                                 "library's stream around each step's graph launch"},
+                                     "strong_pair_entries_fp64": strong}},
                 "e2e": e2e, "roofline": roofline, "segments": segs,
                 "continuous": {"ms_per_step": cont_ms, "value": ws * n / (cont_ms * 1e-3),
                                "note": "graph replays back to back without L2 flush"},

@@ -297,6 +297,17 @@ int md_set_neighbor_skin(md_ctx* ctx, double skin_frac);
  * the FP64 path, with coating potentials on, or on a system without pairs
  * above theta (monodisperse: none for theta >= 1). */
 int md_set_strong_pairs(md_ctx* ctx, double theta);
+/* Limit of every mbarrier wait in the tensor-core kernels, in SM clock
+ * cycles (default 2e9, about a second).  A wait that reaches it gives up;
+ * the kernel frees its tensor memory and returns, and the call reports
+ * MD_ERR_CUDA ("a pipeline wait gave up").  No counterpart in the
+ * reference (it has no GPU code). */
+int md_set_wait_limit(md_ctx* ctx, int64_t cycles);
+/* Test hook for that error path: one warp takes tensor memory and waits on
+ * an mbarrier that is signalled only when `arrive` is nonzero, with the
+ * given limit; returns MD_ERR_CUDA when the wait gave up (the context stays
+ * usable), MD_OK otherwise. */
+int md_debug_wait_probe(md_ctx* ctx, int arrive, int64_t cycles);
 /* Entries of the strong-pair list of the last build (each ordered pair
  * once); 0 when the path is off, -1 while the list is not in use. */
 int md_debug_strong_pairs(md_ctx* ctx, int64_t* entries);
@@ -491,7 +502,8 @@ int md_export_records_txt(const char* dir, const double* obs, int64_t count, dou
  * the Ewald structure factor S(n) = sum_j (n . mu_j) exp(2 pi i n . r_j / L)
  * (FP64) with caller-owned device buffers and no allocation of its own: its
  * scratch is one file-scope device array of md_noalloc_scratch_bytes()
- * (about 2.6 MB) that every GPU loading the library holds until exit.
+ * (2,430,592 bytes) that every GPU loading the library holds until exit.
+ *   n:        1 .. 2^30 particles.
  *   pos, mom: device pointers, N x 3 column-major FP64 (positions in m,
  *             moment vectors in A m^2);  out5: device pointer with room for
  *             nk x 5 doubles {nx, ny, nz, Sc, Ss}, the k vectors of the
@@ -501,8 +513,11 @@ int md_export_records_txt(const char* dir, const double* obs, int64_t count, dou
  *             asynchronous on it.
  * kc above MD_NOALLOC_MAX_KC is rejected with MD_ERR_INVALID.  The first
  * call on a device looks up the array's device address (make it before any
- * stream capture).  All calls share the array and it keeps the last call's
- * contents, so calls whose work overlaps on the GPU race: serialise them. */
+ * stream capture); the address is kept for the process, so do not call it
+ * on a device after cudaDeviceReset.  All calls share the array and it keeps
+ * the last call's contents, so calls whose work overlaps on the GPU race:
+ * serialise them.  Launch failures are read from each launch's own return
+ * code; an error left pending by earlier work is not consumed here. */
 #define MD_NOALLOC_MAX_KC 16
 size_t md_noalloc_scratch_bytes(void);
 int md_structure_factor_noalloc(const double* pos, const double* mom, int64_t n, double lBox, int64_t kc,

@@ -132,6 +132,8 @@ def lib():
         "md_debug_pairs": (C.c_int, [V, PI64]),
         "md_debug_real_part": (C.c_int, [V, P, P]),
         "md_set_neighbor_skin": (C.c_int, [V, C.c_double]),
+        "md_set_wait_limit": (C.c_int, [V, I64]),
+        "md_debug_wait_probe": (C.c_int, [V, C.c_int, I64]),
         "md_set_strong_pairs": (C.c_int, [V, C.c_double]),
         "md_debug_strong_pairs": (C.c_int, [V, PI64]),
         "md_debug_neighbor_capacity": (C.c_int, [V, I64, PI64]),

@@ -254,6 +254,7 @@ struct KParams {
   int tc_scat_smem;      // dynamic shared memory of the scatter launch
   int tc_yz;             // the scatter stages the Y, Z phases in shared memory
   int tc_sfa, tc_sfb;    // structure-factor ring slots (generated, copied)
+  long long tc_wait;     // SM clock cycles after which an mbarrier wait gives up
   int* err;              // device error word (kErrTcWait on a wait that gave up)
 };
 

@@ -247,6 +247,7 @@ KParams k_params(md_ctx* c, void* B, void* F) {
   p.tc_yz = c->tcs.yz;
   p.tc_sfa = c->tcs.sfa;
   p.tc_sfb = c->tcs.sfb;
+  p.tc_wait = c->tc_wait;
   p.err = &c->sc->err;
   return p;
 }
@@ -1609,6 +1610,21 @@ int md_debug_strong_pairs(md_ctx* c, int64_t* entries) {
   CK(c, cudaMemcpy(&total, c->snbr_off + c->n, sizeof(int), cudaMemcpyDeviceToHost));
   *entries = (f.overflow || f.soverflow) ? -1 : total;
   return MD_OK;
+}
+
+int md_set_wait_limit(md_ctx* c, int64_t cycles) {
+  if (!c || cycles < 1000) return set_err(c, MD_ERR_INVALID, "wait limit must be >= 1000 cycles");
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->tc_wait = cycles;
+  invalidate_graph(c);
+  return MD_OK;
+}
+
+int md_debug_wait_probe(md_ctx* c, int arrive, int64_t cycles) {
+  if (!c || cycles < 1000) return set_err(c, MD_ERR_INVALID, "wait limit must be >= 1000 cycles");
+  launch_tc_wait_probe(c->stream, &c->sc->err, arrive ? 1 : 0, cycles);
+  CK(c, cudaGetLastError());
+  return read_err_word(c);
 }
 
 int md_debug_real_part(md_ctx* c, double* B, double* F) {

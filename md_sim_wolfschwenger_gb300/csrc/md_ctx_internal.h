@@ -116,6 +116,7 @@ struct md_ctx {
   // tensor-core k space (mixed path; md_ktc.cu): engine choice, k rows and
   // their buffers (tc_rows = 0 while the engine is off)
   int kengine = MD_KSPACE_AUTO;
+  long long tc_wait = 2000000000LL;  // mbarrier wait limit of the tensor-core kernels (SM cycles)
   int tc_rows = 0;
   TcShape tcs{};
   int2* tc_row = nullptr;

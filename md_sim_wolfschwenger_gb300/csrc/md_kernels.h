@@ -85,6 +85,9 @@ size_t kspace_tc_tblk_entries(int kc, int nsb);  // per-step Y, Z blocks (float2
 // Per-step operand images (after the phase tables), then per evaluation.
 int launch_kspace_tc_prep(cudaStream_t st, const KParams& p);
 int launch_kspace_tc(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* ev = nullptr);
+// One warp waits on an mbarrier that gets an arrival only when `arrive` is
+// set; a wait that gives up after `limit` cycles sets kErrTcWait in *err.
+int launch_tc_wait_probe(cudaStream_t st, int* err, int arrive, long long limit);
 // Per-particle phase tables (once per step; positions are frozen across the
 // two Heun stages).
 int launch_phase_tables(cudaStream_t st, const KParams& p, bool fp64);

@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
       int q = 0, ph = 0;  // slot and phase parity of stage s
       for (int s = 0; s + kSfB < nstage && ok; s++) {
         // the copied slot of stage s takes stage s + kSfB once stage s's MMAs are done
-        ok = mbar_wait_abort(&bt_empty[q], ph, &abort_flag);
+        ok = mbar_wait_abort(&bt_empty[q], ph, &abort_flag, p.tc_wait);
         if (!ok) break;
         issue_copy(s + kSfB, q);
         issued = s + kSfB + 1;
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
       }
       // no copy may still be in flight at the exit: the last copy of each slot has landed
       for (int u = issued - kSfB > 0 ? issued - kSfB : 0; u < issued; u++)
-        mbar_wait(&full_bt[u % kSfB], (u / kSfB) & 1);
+        mbar_wait(&full_bt[u % kSfB], (u / kSfB) & 1, p.tc_wait);
     }
   } else if (warp > kSfGenWarps) {
     // MMA issuer is: stages is, is + kSfIssuers, ...
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
       // its phase parity, copied slot qb of stage s
       int qa = is, pha = 0, qb = is % kSfB;
       for (int s = is; s < nstage && ok; s += kSfIssuers) {
-        ok = mbar_wait_abort(&full_a[qa], pha, &abort_flag);
+        ok = mbar_wait_abort(&full_a[qa], pha, &abort_flag, p.tc_wait);
         if (!ok) break;
         tc_fence_after();
         // descriptors of the slots' tiles; k step ks (16 elements) starts 256 B (16 address units) further
@@ -388,8 +388,8 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
     // generated slot for stage s is the one of stage s - kSfA (parity pha ^ 1)
     int qa = 0, pha = 0, qb = 0, phb = 0;
     for (int s = 0; s < nstage; s++) {
-      bool w = mbar_wait_abort(&full_bt[qb], phb, &abort_flag);
-      if (w && s >= kSfA) w = mbar_wait_abort(&a_empty[qa], pha ^ 1, &abort_flag);
+      bool w = mbar_wait_abort(&full_bt[qb], phb, &abort_flag, p.tc_wait);
+      if (w && s >= kSfA) w = mbar_wait_abort(&a_empty[qa], pha ^ 1, &abort_flag, p.tc_wait);
       w = __all_sync(kFull, w);
       if (!w) {
         if (lane == 0) {
@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
   if (warp < 8) {
     // every issuer's MMAs are complete (each issuer committed once at its end)
     bool w = true;
-    for (int q = 0; q < kSfIssuers; q++) w = w && mbar_wait_abort(&dfull[q], 0, &abort_flag);
+    for (int q = 0; q < kSfIssuers; q++) w = w && mbar_wait_abort(&dfull[q], 0, &abort_flag, p.tc_wait);
     w = __all_sync(kFull, w);
     tc_fence_after();
     const bool good = w && !abort_flag && nstage > 0;
@@ -667,7 +667,7 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
       }
       for (int t = 0; t + NST < NT && ok; t++) {
         // the stage of tile t takes tile t + NST once tile t's MMAs are done
-        ok = mbar_wait_abort(&sfree_bar[t % NST], (t / NST) & 1, &abort_flag);
+        ok = mbar_wait_abort(&sfree_bar[t % NST], (t / NST) & 1, &abort_flag, p.tc_wait);
         if (!ok) break;
         const int u = t + NST;
         mbar_expect_tx(&full_bar[u % NST], tbytes);
@@ -680,7 +680,7 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
       }
       // no copy may still be in flight at the exit: the last copy of each stage has landed
       for (int u = issued - NST > 0 ? issued - NST : 0; u < issued; u++)
-        mbar_wait(&full_bar[u % NST], (u / NST) & 1);
+        mbar_wait(&full_bar[u % NST], (u / NST) & 1, p.tc_wait);
     }
   } else if (warp > kScEpiWarps) {
     // MMA issuer 0 or 1: tiles t = is, is + 2, ...
@@ -692,8 +692,8 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
       bool ok = true;
       int k = 0, last = -1;
       for (int t = is; t < NT && ok; t += 2, k++) {
-        ok = mbar_wait_abort(&full_bar[t % NST], (t / NST) & 1, &abort_flag);
-        if (ok && k >= 1) ok = mbar_wait_abort(&dfree_bar[is], (k - 1) & 1, &abort_flag);
+        ok = mbar_wait_abort(&full_bar[t % NST], (t / NST) & 1, &abort_flag, p.tc_wait);
+        if (ok && k >= 1) ok = mbar_wait_abort(&dfree_bar[is], (k - 1) & 1, &abort_flag, p.tc_wait);
         if (!ok) break;
         tc_fence_after();
         const uint64_t dbh = tc_desc(smem_u32(stage0 + (t % NST) * tbytes), 128, sbo);
@@ -713,7 +713,7 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
         abort_flag = 1;
         atomicOr(p.err, kErrTcWait);
       }
-      if (last >= 0) mbar_wait(&dfull_bar[is], last & 1);  // this issuer's MMAs are done
+      if (last >= 0) mbar_wait(&dfull_bar[is], last & 1, p.tc_wait);  // this issuer's MMAs are done
     }
   } else {
     const float4 mu = act ? ((const float4*)p.s.mu)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -747,7 +747,7 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
       const int is = t & 1, k = t >> 1;
       float2 Pn[L::RQ];
       if (t + 1 < NT) fetch(t + 1, Pn);  // in flight during this tile's wait and arithmetic
-      bool w = mbar_wait_abort(&dfull_bar[is], k & 1, &abort_flag);
+      bool w = mbar_wait_abort(&dfull_bar[is], k & 1, &abort_flag, p.tc_wait);
       w = __all_sync(kFull, w);
       if (!w) {
         if (lane == 0) {
@@ -935,6 +935,42 @@ int launch_kspace_tc(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* 
     k_kscat_tc<false><<<nb, kScThreads, sm2, st>>>(p);
   }
   return 3;
+}
+
+// ------------------------------------------------------ bounded-wait probe
+
+// The error path of a wait that gives up, on its own: one warp takes tensor
+// memory, waits on an mbarrier (phase 0) that gets its arrival only when
+// `arrive` is set, and when the wait gives up records kErrTcWait and still
+// frees its tensor memory -- the steps of every wait in the kernels above.
+// Tests run it with a short limit and no arrival (a barrier nothing
+// signals), then check that the context reports the error and keeps working.
+__global__ void __launch_bounds__(32) k_tc_wait_probe(int* err, int arrive, long long limit) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tslot;
+  const int lane = threadIdx.x;
+  if (lane == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+  tmem_alloc(&tslot, 32);
+  tc_fence_before();
+  __syncwarp();
+  tc_fence_after();
+  const uint32_t tmem = tslot;
+  if (arrive && lane == 0) mbar_arrive(&bar);
+  __syncwarp();
+  const bool ok = mbar_wait(&bar, 0, limit);
+  if (!ok && lane == 0) atomicOr(err, kErrTcWait);
+  __syncwarp();
+  tc_fence_before();
+  tmem_free(tmem, 32);
+}
+
+int launch_tc_wait_probe(cudaStream_t st, int* err, int arrive, long long limit) {
+  k_tc_wait_probe<<<1, 32, 0, st>>>(err, arrive, limit);
+  return 1;
 }
 
 }  // namespace md

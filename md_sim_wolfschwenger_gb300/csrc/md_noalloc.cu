@@ -7,8 +7,9 @@
 // S(n) = sum_j (n . mu_j) exp(2 pi i n . r_j / L) -- the quantity that
 // CompDipInteractEwaldF / CompDipFieldEwaldF accumulate -- with caller-owned
 // inputs and outputs and a fixed scratch area that lives in a file-scope
-// __device__ array of this library (kNoAllocScratchBytes, about 2.5 MB).
-// Every GPU that loads the library holds that array until the process exits.
+// __device__ array of this library (md_noalloc_scratch_bytes(): 2,430,592
+// bytes for kc <= 16).  Every GPU that loads the library holds that array
+// until the process exits.
 //
 // The array's name is a host-side stand-in in host code, not a device
 // address.  Its device address is obtained once per device with
@@ -16,7 +17,14 @@
 // that device; make that first call before any stream capture.  Every call
 // shares the one array, which keeps the contents of the last call, so calls
 // whose work overlaps on the GPU (different streams, different host threads)
-// race on it; serialise them.
+// race on it; serialise them.  The looked-up address is kept for the life
+// of the process: after a cudaDeviceReset of that device the library's
+// module (and the array) may be loaded elsewhere, so do not call this entry
+// point on a device that was reset.
+//
+// A launch error is checked on each launch's own return code
+// (cudaLaunchKernel), so an error left pending by the caller's earlier work
+// is neither consumed nor reported here.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -69,17 +77,18 @@ __global__ void k_noalloc_klist(Scratch* s, int kc) {
 
 // Partial sums over one particle chunk for each k (FP64, direct sincos of the
 // full phase with the configuration's pi, as EvalSinCos's tables represent).
-__global__ void k_noalloc_partial(Scratch* s, const double* __restrict__ pos, const double* __restrict__ mom, int n,
-                                  int nk, double two_pi_over_L) {
+// Indices are 64-bit: 2 n + j exceeds INT_MAX for n above ~7e8.
+__global__ void k_noalloc_partial(Scratch* s, const double* __restrict__ pos, const double* __restrict__ mom,
+                                  long long n, int nk, double two_pi_over_L) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
   if (k >= nk) return;
-  const int per = (n + kChunks - 1) / kChunks;
-  const int j0 = c * per, j1 = min(n, j0 + per);
+  const long long per = (n + kChunks - 1) / kChunks;
+  const long long j0 = c * per, j1 = min(n, j0 + per);
   const int4 q = s->klist[k];
   const double nx = q.x, ny = q.y, nz = q.z;
   double sc = 0, ss = 0;
-  for (int j = j0; j < j1; j++) {
+  for (long long j = j0; j < j1; j++) {
     const double ph = two_pi_over_L * (nx * pos[j] + ny * pos[n + j] + nz * pos[2 * n + j]);
     double sn, cs;
     sincos(ph, &sn, &cs);
@@ -138,11 +147,27 @@ extern "C" int md_structure_factor_noalloc(const double* pos, const double* mom,
     s = g_addr[dev];
   }
   cudaStream_t st = (cudaStream_t)stream;
-  k_noalloc_klist<<<1, 1, 0, st>>>(s, (int)kc);
-  dim3 g1((nk + 127) / 128, kChunks);
-  k_noalloc_partial<<<g1, 128, 0, st>>>(s, pos, mom, (int)n, nk, 2.0 * my_pi / lBox);
-  k_noalloc_reduce<<<(nk + 127) / 128, 128, 0, st>>>(s, nk, out5);
-  if (cudaGetLastError() != cudaSuccess) return MD_ERR_CUDA;
+  // each launch's own return code (a failed launch's error is then cleared
+  // from the runtime's last-error state, which holds nothing of the caller's)
+  auto launched = [](cudaError_t e) {
+    if (e == cudaSuccess) return true;
+    cudaGetLastError();
+    return false;
+  };
+  int kci = (int)kc;
+  void* a1[] = {&s, &kci};
+  if (!launched(cudaLaunchKernel((const void*)k_noalloc_klist, dim3(1), dim3(1), a1, 0, st))) return MD_ERR_CUDA;
+  long long nl = n;
+  int nki = nk;
+  double w = 2.0 * my_pi / lBox;
+  void* a2[] = {&s, (void*)&pos, (void*)&mom, &nl, &nki, &w};
+  if (!launched(cudaLaunchKernel((const void*)k_noalloc_partial, dim3((nk + 127) / 128, kChunks), dim3(128), a2, 0,
+                                 st)))
+    return MD_ERR_CUDA;
+  const Scratch* cs = s;
+  void* a3[] = {(void*)&cs, &nki, (void*)&out5};
+  if (!launched(cudaLaunchKernel((const void*)k_noalloc_reduce, dim3((nk + 127) / 128), dim3(128), a3, 0, st)))
+    return MD_ERR_CUDA;
   if (nk_out) *nk_out = nk;
   return MD_OK;
 }

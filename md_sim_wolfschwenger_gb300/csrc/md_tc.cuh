@@ -10,8 +10,9 @@
 // One kind::tf32 MMA consumes K = 8 elements (two core matrices along K), so
 // the k-th step starts 256 B * k after the tile.
 //
-// Every mbarrier wait is bounded: after kWaitCycles it gives up and the
-// caller records an error (no wait can hang the GPU).
+// Every mbarrier wait is bounded: after a limit of SM clock cycles (a kernel
+// parameter, kWaitCycles by default) it gives up and the caller records an
+// error (no wait can hang the GPU).
 #pragma once
 #include <cuda_fp16.h>
 
@@ -19,7 +20,7 @@
 
 namespace md {
 
-// A wait gives up after kWaitCycles SM clock cycles (about a second).
+// Default limit of a wait: 2e9 SM clock cycles (about a second).
 constexpr long long kWaitCycles = 2000000000LL;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -181,24 +182,25 @@ __device__ __forceinline__ bool mbar_try_sleep(uint32_t a, uint32_t parity) {
 }
 
 // Waits for the phase with the given parity to complete; false after
-// kWaitCycles.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// `limit` SM clock cycles.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit) {
   const uint32_t a = smem_u32(bar);
   if (mbar_try(a, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_sleep(a, parity))
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 
 // As mbar_wait, but also gives up as soon as *abort is set (another role of
 // the block failed).
-__device__ __forceinline__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, volatile int* abort) {
+__device__ __forceinline__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, volatile int* abort,
+                                                long long limit) {
   const uint32_t a = smem_u32(bar);
   if (mbar_try(a, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_sleep(a, parity)) {
-    if (*abort || clock64() - t0 > kWaitCycles) return false;
+    if (*abort || clock64() - t0 > limit) return false;
   }
   return true;
 }

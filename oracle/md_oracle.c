@@ -1,5 +1,6 @@
 /* md_oracle.c -- TEST INFRASTRUCTURE ONLY.  CPU restatement (FP64, one thread
- * per context) of the reference's LLG + Brownian-dynamics time step.  See
+ * per context unless orc_set_threads asks for more) of the reference's LLG +
+ * Brownian-dynamics time step.  See
  * md_oracle.h.  Each function names the reference lines it restates
  * (paths relative to the MD_Sim_Wolfschwenger repository).  The loop order
  * and the arithmetic order of the reference are kept so that the two agree
@@ -9,6 +10,8 @@
 #include "md_oracle.h"
 
 #include <math.h>
+#include <stdint.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
@@ -37,6 +40,10 @@ struct orc_ctx {
   double Pxy, Pxz, Pyz;
   double t, last_seconds;
   int64_t step;
+  /* threads of the pair list and the Ewald sums (orc_set_threads): private
+   * accumulators per thread, [T][6 N] (B then F), pressure [T][3] */
+  int nthreads;
+  double *tacc, *tP;
 };
 
 #define AX(a, i, c, n) (a)[(int64_t)(c) * (n) + (i)]
@@ -100,7 +107,53 @@ void orc_destroy(orc_ctx* c) {
   free(c->ebuf);
   free(c->pidx);
   free(c->psr);
+  free(c->tacc);
+  free(c->tP);
   free(c);
+}
+
+/* Threads for the pair list and the Ewald sums (the bench's CPU arm on all
+ * host cores).  t > 1 needs the Jacobi overlap push (overlap_mode 1): the
+ * sequential push of the reference depends on the loop order.  Results
+ * equal the one-thread ones up to the order of the final additions. */
+int orc_set_threads(orc_ctx* c, int t) {
+  if (t < 1 || t > 256) return 1;
+  if (t > 1 && c->cfg.overlap_mode != 1) return 2;
+  free(c->tacc);
+  free(c->tP);
+  c->tacc = c->tP = NULL;
+  c->nthreads = t;
+  if (t > 1) {
+    c->tacc = zalloc((int64_t)t * 6 * c->n);
+    c->tP = zalloc(3 * (int64_t)t);
+  }
+  return 0;
+}
+
+typedef struct {
+  orc_ctx* c;
+  int t;
+  int64_t a, b;   /* range of rows, pairs or k vectors */
+  double *B, *F;  /* private accumulators (N x 3 each) */
+  int field_only;
+  /* pair list: private list */
+  int64_t np, cap;
+  double *pvec, *plen, *jac;
+  int32_t* pidx;
+  unsigned char* psr;
+} orc_job;
+
+static void run_jobs(orc_job* jobs, int T, void* (*fn)(void*)) {
+  pthread_t th[256];
+  int started[256] = {0};
+  for (int t = 1; t < T; t++) started[t] = pthread_create(&th[t], NULL, fn, &jobs[t]) == 0;
+  fn(&jobs[0]);
+  for (int t = 1; t < T; t++) {
+    if (started[t])
+      pthread_join(th[t], NULL);
+    else
+      fn(&jobs[t]);  /* no thread: run it here */
+  }
 }
 
 /* InitParticleProps derived quantities (simulation.cpp:204-210). */
@@ -166,6 +219,12 @@ static void philox4x32_10(uint32_t ctr[4], uint32_t k0, uint32_t k1) {
 
 /* 9 standard normals for particle i at step s: counter {i, block, s_lo, s_hi},
  * key {seed_lo, seed_hi}; uniforms (x + 0.5) 2^-32; Box-Muller pairs. */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  philox4x32_10(c, key[0], key[1]);
+  for (int q = 0; q < 4; q++) out[q] = c[q];
+}
+
 void orc_philox_normals(uint64_t seed, uint64_t step, int64_t n, double* xi) {
   const double twopi = 6.283185307179586476925286766559;
   for (int64_t i = 0; i < n; i++) {
@@ -262,10 +321,16 @@ static void list_push(orc_ctx* c, double r, const double v[3], int32_t i1, int32
   c->psr[p] = (unsigned char)sr;
 }
 
+static void pair_list_threads(orc_ctx* c);
+
 /* CompInteractVecs + ApplyBoundaryCondVec (interaction.cpp:88-155): all pairs,
  * minimum image, list of pairs with r < rCutLR, and the overlap push of the
  * cores (in place and sequential for overlap_mode 0, Jacobi for 1). */
 static void pair_list(orc_ctx* c) {
+  if (c->nthreads > 1) {
+    pair_list_threads(c);
+    return;
+  }
   int64_t n = c->n;
   double L = c->cfg.lBox, h = L / 2, rc = c->cfg.rCutLR, rsr = c->cfg.rCutSR;
   int jac = c->cfg.overlap_mode == 1;
@@ -306,15 +371,112 @@ static void pair_list(orc_ctx* c) {
     for (int64_t k = 0; k < 3 * n; k++) c->pos[k] += c->jac[k];
 }
 
+/* The pair list over rows [a, b) of the all-pairs loop into a private list
+ * (Jacobi overlap push into a private displacement array). */
+static void* pair_rows(void* arg) {
+  orc_job* j = (orc_job*)arg;
+  orc_ctx* c = j->c;
+  int64_t n = c->n;
+  double L = c->cfg.lBox, h = L / 2, rc = c->cfg.rCutLR, rsr = c->cfg.rCutSR;
+  for (int64_t i1 = j->a; i1 < j->b; i1++) {
+    for (int64_t i2 = i1 + 1; i2 < n; i2++) {
+      double v[3];
+      for (int a = 0; a < 3; a++) {
+        double d = AX(c->pos, i2, a, n) - AX(c->pos, i1, a, n);
+        d -= L * (double)(d > h);
+        d += L * (double)(d < -h);
+        v[a] = d;
+      }
+      double r = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      if (r < rc) {
+        if (j->np == j->cap) {
+          int64_t nc = j->cap ? 2 * j->cap : 4096;
+          j->pvec = (double*)realloc(j->pvec, (size_t)nc * 3 * sizeof(double));
+          j->plen = (double*)realloc(j->plen, (size_t)nc * sizeof(double));
+          j->pidx = (int32_t*)realloc(j->pidx, (size_t)nc * 2 * sizeof(int32_t));
+          j->psr = (unsigned char*)realloc(j->psr, (size_t)nc);
+          j->cap = nc;
+        }
+        int64_t p = j->np++;
+        j->plen[p] = r;
+        for (int a = 0; a < 3; a++) j->pvec[3 * p + a] = v[a] / r;
+        j->pidx[2 * p] = (int32_t)i1;
+        j->pidx[2 * p + 1] = (int32_t)i2;
+        j->psr[p] = (unsigned char)(r < rsr);
+        double dCont = c->rMag[i1] + c->rMag[i2] + 1e-10;
+        if (r < dCont) {
+          double d = dCont - r;
+          for (int a = 0; a < 3; a++) {
+            double u = j->pvec[3 * p + a];
+            AX(j->jac, i1, a, n) -= 0.5 * d * u;
+            AX(j->jac, i2, a, n) += 0.5 * d * u;
+          }
+          j->plen[p] = dCont;
+        }
+      }
+    }
+  }
+  return NULL;
+}
+
+/* pair_list on T threads: rows split into ranges of equal candidate counts,
+ * the private lists concatenated in row order (the one-thread list order). */
+static void pair_list_threads(orc_ctx* c) {
+  int T = c->nthreads;
+  int64_t n = c->n;
+  orc_job jobs[256];
+  memset(jobs, 0, sizeof jobs);
+  double total = 0.5 * (double)n * (double)(n - 1);
+  int64_t row = 0;
+  for (int t = 0; t < T; t++) {
+    jobs[t].c = c;
+    jobs[t].t = t;
+    jobs[t].a = row;
+    double target = total * (double)(t + 1) / T;
+    while (row < n && (double)(row + 1) * (double)(n - 1) - 0.5 * (double)(row + 1) * (double)row < target) row++;
+    if (t == T - 1) row = n;
+    jobs[t].b = row;
+    jobs[t].jac = c->tacc + (int64_t)t * 6 * n;
+    memset(jobs[t].jac, 0, (size_t)(3 * n) * sizeof(double));
+  }
+  run_jobs(jobs, T, pair_rows);
+  int64_t total_pairs = 0;
+  for (int t = 0; t < T; t++) total_pairs += jobs[t].np;
+  if (total_pairs > c->cap) {
+    c->pvec = (double*)realloc(c->pvec, (size_t)total_pairs * 3 * sizeof(double));
+    c->plen = (double*)realloc(c->plen, (size_t)total_pairs * sizeof(double));
+    c->pidx = (int32_t*)realloc(c->pidx, (size_t)total_pairs * 2 * sizeof(int32_t));
+    c->psr = (unsigned char*)realloc(c->psr, (size_t)total_pairs);
+    c->cap = total_pairs;
+  }
+  c->pairs = 0;
+  for (int t = 0; t < T; t++) {
+    const int64_t m = jobs[t].np, o = c->pairs;
+    if (m) {
+      memcpy(c->pvec + 3 * o, jobs[t].pvec, (size_t)m * 3 * sizeof(double));
+      memcpy(c->plen + o, jobs[t].plen, (size_t)m * sizeof(double));
+      memcpy(c->pidx + 2 * o, jobs[t].pidx, (size_t)m * 2 * sizeof(int32_t));
+      memcpy(c->psr + o, jobs[t].psr, (size_t)m);
+    }
+    c->pairs += m;
+    free(jobs[t].pvec);
+    free(jobs[t].plen);
+    free(jobs[t].pidx);
+    free(jobs[t].psr);
+  }
+  for (int t = 0; t < T; t++)
+    for (int64_t k = 0; k < 3 * n; k++) c->pos[k] += jobs[t].jac[k];
+}
+
 static inline double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
 /* CompDipInteractEwaldR + EvalPressTensLR (interaction.cpp:383-422,
  * postprocessing.cpp:195-200); field only when F == NULL
  * (CompDipFieldEwaldR, interaction.cpp:555-582). */
-static void ewald_real(orc_ctx* c, double* B, double* F) {
+static void ewald_real_range(orc_ctx* c, double* B, double* F, int64_t p0, int64_t p1, double* P) {
   int64_t n = c->n;
   double al = c->cfg.alpha, al2 = c->alpha2, al4 = c->alpha4, fe = c->cfg.facEwald;
-  for (int64_t p = 0; p < c->pairs; p++) {
+  for (int64_t p = p0; p < p1; p++) {
     int64_t i1 = c->pidx[2 * p], i2 = c->pidx[2 * p + 1];
     double r = c->plen[p], r2 = r * r;
     double t = 2.0 * al * exp(-al2 * r2) * c->cfg.irPi / r2;
@@ -338,9 +500,9 @@ static void ewald_real(orc_ctx* c, double* B, double* F) {
         AX(F, i1, a, n) -= v1[a];
         AX(F, i2, a, n) += v1[a];
       }
-      c->Pxy += r * u[0] * v1[1];
-      c->Pxz += r * u[0] * v1[2];
-      c->Pyz += r * u[1] * v1[2];
+      P[0] += r * u[0] * v1[1];
+      P[1] += r * u[0] * v1[2];
+      P[2] += r * u[1] * v1[2];
     } else {
       for (int a = 0; a < 3; a++) {
         AX(B, i1, a, n) += fe * (a2 * dot2 * u[a] * r2 - a1 * m2[a]);
@@ -350,16 +512,67 @@ static void ewald_real(orc_ctx* c, double* B, double* F) {
   }
 }
 
+static void* real_job(void* arg) {
+  orc_job* j = (orc_job*)arg;
+  double* P = j->c->tP + 3 * j->t;
+  P[0] = P[1] = P[2] = 0;
+  ewald_real_range(j->c, j->B, j->F, j->a, j->b, P);
+  return NULL;
+}
+
+/* Adds the private accumulators of T jobs in thread order. */
+static void reduce_jobs(orc_ctx* c, orc_job* jobs, int T, double* B, double* F) {
+  int64_t n3 = 3 * c->n;
+  for (int t = 0; t < T; t++)
+    for (int64_t k = 0; k < n3; k++) {
+      B[k] += jobs[t].B[k];
+      if (F) F[k] += jobs[t].F[k];
+    }
+}
+
+static void ewald_real(orc_ctx* c, double* B, double* F) {
+  if (c->nthreads <= 1) {
+    double P[3] = {c->Pxy, c->Pxz, c->Pyz};
+    ewald_real_range(c, B, F, 0, c->pairs, P);
+    c->Pxy = P[0];
+    c->Pxz = P[1];
+    c->Pyz = P[2];
+    return;
+  }
+  int T = c->nthreads;
+  int64_t n = c->n;
+  orc_job jobs[256];
+  memset(jobs, 0, sizeof jobs);
+  for (int t = 0; t < T; t++) {
+    jobs[t].c = c;
+    jobs[t].t = t;
+    jobs[t].a = c->pairs * t / T;
+    jobs[t].b = c->pairs * (t + 1) / T;
+    jobs[t].B = c->tacc + (int64_t)t * 6 * n;
+    jobs[t].F = F ? jobs[t].B + 3 * n : NULL;
+    memset(jobs[t].B, 0, (size_t)(6 * n) * sizeof(double));
+  }
+  run_jobs(jobs, T, real_job);
+  reduce_jobs(c, jobs, T, B, F);
+  for (int t = 0; t < T; t++) {
+    c->Pxy += c->tP[3 * t];
+    c->Pxz += c->tP[3 * t + 1];
+    c->Pyz += c->tP[3 * t + 2];
+  }
+}
+
 /* CompDipInteractEwaldF (interaction.cpp:429-514); field only when F == NULL
  * (CompDipFieldEwaldF, interaction.cpp:588-672).  Includes self and surface terms. */
-static void ewald_kspace(orc_ctx* c, double* B, double* F) {
-  int64_t n = c->n, nc = c->cfg.nc;
+static void ewald_kspace_range(orc_ctx* c, double* B, double* F, int64_t k0, int64_t k1) {
+  int64_t n = c->n, nc = c->cfg.nc, kidx = -1;
   for (int64_t nz = 0; nz <= nc; nz++)
     for (int64_t ny = -nc; ny <= nc; ny++)
       for (int64_t nx = -nc; nx <= nc; nx++) {
         double kv[3] = {(double)nx, (double)ny, (double)nz};
         double lenSqr = dot3(kv, kv);
         if (lenSqr == 0 || lenSqr > c->nc2) continue;
+        kidx++;
+        if (kidx < k0 || kidx >= k1) continue;
         double e = 2.0 * exp(-c->w * lenSqr) / lenSqr;
         if (nz == 0) e *= 0.5;
         double sumC = 0, sumS = 0;
@@ -390,6 +603,41 @@ static void ewald_kspace(orc_ctx* c, double* B, double* F) {
           }
         }
       }
+}
+
+static void* kspace_job(void* arg) {
+  orc_job* j = (orc_job*)arg;
+  ewald_kspace_range(j->c, j->B, j->F, j->a, j->b);
+  return NULL;
+}
+
+static void ewald_kspace(orc_ctx* c, double* B, double* F) {
+  int64_t n = c->n;
+  if (c->nthreads <= 1) {
+    ewald_kspace_range(c, B, F, 0, INT64_MAX);
+  } else {
+    int64_t nk = 0, nc = c->cfg.nc;
+    for (int64_t nz = 0; nz <= nc; nz++)
+      for (int64_t ny = -nc; ny <= nc; ny++)
+        for (int64_t nx = -nc; nx <= nc; nx++) {
+          double l = (double)(nx * nx + ny * ny + nz * nz);
+          if (l > 0 && l <= c->nc2) nk++;
+        }
+    int T = c->nthreads;
+    orc_job jobs[256];
+    memset(jobs, 0, sizeof jobs);
+    for (int t = 0; t < T; t++) {
+      jobs[t].c = c;
+      jobs[t].t = t;
+      jobs[t].a = nk * t / T;
+      jobs[t].b = nk * (t + 1) / T;
+      jobs[t].B = c->tacc + (int64_t)t * 6 * n;
+      jobs[t].F = F ? jobs[t].B + 3 * n : NULL;
+      memset(jobs[t].B, 0, (size_t)(6 * n) * sizeof(double));
+    }
+    run_jobs(jobs, T, kspace_job);
+    reduce_jobs(c, jobs, T, B, F);
+  }
   for (int64_t i = 0; i < n; i++)
     for (int a = 0; a < 3; a++)
       AX(B, i, a, n) += c->cSelf * AX(c->mom, i, a, n) - c->cSurf * c->momSum[a];
@@ -831,3 +1079,47 @@ int orc_ewald_for_rc(double rc, double M, double fAl, double lBox, double n, dou
 
 int64_t orc_pairs(const orc_ctx* c) { return c->pairs; }
 double orc_last_seconds(const orc_ctx* c) { return c->last_seconds; }
+
+/* InitCoordsFromSketch's random sequential addition (simulation.cpp:241-264)
+ * in index order: candidate uniform in [-(L/2 - rHydr_i), L/2 - rHydr_i]^3,
+ * rejected if it overlaps a placed hydrodynamic sphere (periodic distances),
+ * with a seeded splitmix64 generator instead of EigenRand's.  pos: N x 3
+ * column-major.  Returns 0, or 1 if a particle found no place. */
+static uint64_t sm64(uint64_t* x) {
+  uint64_t z = (*x += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+static double sm64_unit(uint64_t* x) { return (double)(sm64(x) >> 11) * (1.0 / 9007199254740992.0); }
+
+int orc_rsa(int64_t n, double lBox, const double* rHydr, uint64_t seed, int64_t max_tries, double* pos) {
+  uint64_t st = seed;
+  double L = lBox;
+  for (int64_t i = 0; i < n; i++) {
+    int placed = 0;
+    for (int64_t t = 0; t < max_tries && !placed; t++) {
+      double x[3];
+      for (int a = 0; a < 3; a++) x[a] = (2.0 * sm64_unit(&st) - 1.0) * (L / 2.0 - rHydr[i]);
+      placed = 1;
+      const double h = L / 2.0;
+      for (int64_t j = 0; j < i && placed; j++) {
+        const double s = rHydr[i] + rHydr[j];
+        double r2 = 0;
+        int far = 0;
+        for (int a = 0; a < 3 && !far; a++) {
+          double d = AX(pos, j, a, n) - x[a];
+          d -= L * (double)(d > h);
+          d += L * (double)(d < -h);
+          far = d > s || d < -s;
+          r2 += d * d;
+        }
+        if (!far && r2 < s * s) placed = 0;
+      }
+      if (placed)
+        for (int a = 0; a < 3; a++) AX(pos, i, a, n) = x[a];
+    }
+    if (!placed) return 1;
+  }
+  return 0;
+}

@@ -87,6 +87,8 @@ void orc_thermal(orc_ctx* c, double dt, int noise_mode, const double* xi, uint64
 
 /* Philox4x32-10 normals: 9 per particle per step, layout as uploaded xi. */
 void orc_philox_normals(uint64_t seed, uint64_t step, int64_t n, double* xi);
+/* One Philox4x32-10 block (Salmon et al., SC'11): counter ctr, key key. */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
 /* Ewald error model (interaction.cpp:330-347).  Returns the real-space and
  * k-space RMS force errors divided by F_contact, minus errTol/sqrt(2). */
@@ -100,6 +102,12 @@ int orc_ewald_for_rc(double rc, double M, double fAl, double lBox, double n, dou
                      double my_pi, double errTol, double* alpha, double* kc);
 
 int64_t orc_pairs(const orc_ctx* c);
+/* Threads of the pair list and the Ewald sums (default 1); t > 1 needs
+ * overlap_mode 1.  Returns 0, or nonzero for a bad request. */
+int orc_set_threads(orc_ctx* c, int t);
+/* Random sequential addition in index order (InitCoordsFromSketch,
+ * simulation.cpp:241-264) with a seeded splitmix64 generator. */
+int orc_rsa(int64_t n, double lBox, const double* rHydr, uint64_t seed, int64_t max_tries, double* pos);
 double orc_last_seconds(const orc_ctx* c);
 
 #ifdef __cplusplus

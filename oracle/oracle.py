@@ -32,7 +32,7 @@ def build(force=False) -> str:
                 os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "md_oracle.h"))):
             os.makedirs(BUILD, exist_ok=True)
             tmp = LIB + f".{os.getpid()}.tmp"
-            subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-o", tmp, src, "-lm"])
+            subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-pthread", "-o", tmp, src, "-lm"])
             os.replace(tmp, LIB)
     return LIB
 
@@ -82,6 +82,11 @@ def lib():
         L.orc_pairs.argtypes = [C.c_void_p]
         L.orc_last_seconds.restype = C.c_double
         L.orc_last_seconds.argtypes = [C.c_void_p]
+        L.orc_set_threads.restype = C.c_int
+        L.orc_set_threads.argtypes = [C.c_void_p, C.c_int]
+        L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.orc_rsa.restype = C.c_int
+        L.orc_rsa.argtypes = [C.c_int64, C.c_double, P, C.c_uint64, C.c_int64, P]
         _lib = L
     return _lib
 
@@ -283,11 +288,25 @@ class Oracle:
                                  C.byref(att))
         return dtv.value, used.value, att.value, obs
 
+    def set_threads(self, t):
+        """Threads of the pair list and the Ewald sums (t > 1 needs overlap_mode 1)."""
+        if self.L.orc_set_threads(self.h, int(t)) != 0:
+            raise ValueError(f"orc_set_threads({t}) refused")
+
     def last_seconds(self):
         return self.L.orc_last_seconds(self.h)
 
     def pairs(self):
         return self.L.orc_pairs(self.h)
+
+
+def philox_block(ctr, key):
+    """One Philox4x32-10 block: four 32-bit counter words, two key words."""
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().orc_philox4x32_10(c, k, o)
+    return [int(v) for v in o]
 
 
 def philox_normals(seed, step, n):
@@ -342,3 +361,37 @@ def random_state(n, lBox, rHydr, rng, min_gap=0.0, rot=2):
         el2 = 2.0 * np.arcsin(np.sqrt(rng.uniform(0, 1, n)))
         mm = np.stack([np.sin(el2) * np.cos(az2), np.sin(el2) * np.sin(az2), np.cos(el2)])
     return np.ascontiguousarray(pos.T), mm, ea
+
+
+def rsa_fast(n, lBox, rHydr, seed, max_tries=100000):
+    """(3, N) positions by random sequential addition in index order (the C
+    restatement orc_rsa of InitCoordsFromSketch, simulation.cpp:241-264)."""
+    rH = np.ascontiguousarray(rHydr, dtype=np.float64)
+    pos = np.zeros((3, n))
+    if lib().orc_rsa(n, lBox, _p(rH), int(seed), int(max_tries), _p(pos)) != 0:
+        raise RuntimeError("random sequential addition failed: volume fraction too high")
+    return pos
+
+
+def cost_model_rc(d, rMag, rHydr, lBox, kc_tc=25):
+    """The Ewald split the library's cost model picks (restated for the CPU
+    arm of the benchmark, which must not load the library): every rc = 0.08 L
+    .. 0.5 L in steps of 0.005 L, alpha and kc from the reference's error
+    model (ewald_for_rc), cost = N (9.5 n_pairs + c_k n_k) with c_k = 1.7 for
+    kc <= kc_tc (tensor-core k space) else 2.5.  Returns (alpha, rc, kc)."""
+    n = len(rMag)
+    best = None
+    for q in range(85):
+        x = 0.08 + 0.005 * q
+        try:
+            a, kc, _ = ewald_for_rc(d, rMag, rHydr, lBox, x * lBox)
+        except ValueError:
+            continue
+        if kc > 64:
+            continue
+        nr = n * 4.0 / 3.0 * math.pi * x ** 3
+        nk = 2.0 * math.pi / 3.0 * kc ** 3
+        cost = n * (9.5 * nr + (1.7 if kc <= kc_tc else 2.5) * nk)
+        if best is None or cost < best[0]:
+            best = (cost, a, x * lBox, kc)
+    return best[1:]

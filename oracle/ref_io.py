@@ -152,3 +152,14 @@ def parse_out(raw, n, nsteps, dump_level, adaptive=False):
     o["elapsed"] = take(1)[0]
     assert p == raw.size, (p, raw.size)
     return o
+
+
+def reference_root():
+    """Root of the reference sources the harness was built from (recorded by
+    oracle/build_ref.sh in oracle/_ref/reference_root), or None."""
+    f = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref", "reference_root")
+    try:
+        root = open(f).read().strip()
+    except OSError:
+        return None
+    return root if os.path.isdir(root) else None

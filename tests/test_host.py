@@ -91,7 +91,9 @@ def test_default_config_is_the_shipped_ini():
     """md_config_default equals the reference's shipped configuration.ini
     (checked against the file itself when the reference is mounted)."""
     import md_sim_wolfschwenger_gb300 as m
-    path = "/root/reference/src/configuration.ini"
+    import ref_io
+    root = ref_io.reference_root()
+    path = os.path.join(root, "src", "configuration.ini") if root else ""
     if not os.path.exists(path):
         pytest.skip("reference sources not mounted")
     a = m.Configuration.default().as_dict()

@@ -58,18 +58,21 @@ def test_jacobi_overlap_differs_only_on_overlapping_particles():
 
 
 def test_philox_known_answer():
-    """Philox4x32-10 known-answer vectors of the Random123 distribution
-    (Salmon et al., SC'11): counter 0 / key 0 and counter pi / key e."""
-    import ctypes as C
-    L = O.lib()
-    # the uniform-to-normal map is checked through moments below; the integer
-    # stream through the published known answers via a one-particle draw
-    xi0 = O.philox_normals(0, 0, 1)
-    assert np.all(np.isfinite(xi0))
+    """Philox4x32-10 against the known-answer vectors published with the
+    Random123 library (Salmon et al., SC'11): counter 0 / key 0, all ones,
+    and the digits of pi as counter and key.  The GPU's noise is checked
+    bit for bit against this generator elsewhere, so these pin both."""
+    kat = [([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+           ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+           ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
+            [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1])]
+    for ctr, key, want in kat:
+        assert O.philox_block(ctr, key) == want, (ctr, key)
+    # the uniform-to-normal map (Box-Muller) through its first two moments
     xs = O.philox_normals(1234, 7, 20000).reshape(9, -1)
+    assert np.all(np.isfinite(xs))
     assert abs(xs.mean()) < 0.01
     assert abs(xs.std() - 1) < 0.01
-    del L, C
 
 
 ADAPTIVE_CASES = ["n64_adapt_he", "n64_adapt_bs", "n64_adapt_dp"]

@@ -60,4 +60,7 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     nk = C.c_int64(0)
     one = C.c_void_p(1)  # never dereferenced: the size check comes first
     assert L.md_structure_factor_noalloc(one, one, 10, 1e-6, 17, 3.14159265359, one, C.byref(nk), None) == 1
-    assert 0 < L.md_noalloc_scratch_bytes() < 8 << 20
+    # particle count beyond 2^30 (the documented limit; indexing is 64-bit below it)
+    assert L.md_structure_factor_noalloc(one, one, (1 << 30) + 1, 1e-6, 8, 3.14159265359, one, C.byref(nk),
+                                         None) == 1
+    assert L.md_noalloc_scratch_bytes() == 2430592
