@@ -73,9 +73,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison")
     p.add_argument("--sweep-replicas", type=int, default=256, help="field-sweep sample: replicas (0 skips it)")
-    p.add_argument("--sweep-steps", type=int, default=100, help="field-sweep sample: steps per replica")
-    p.add_argument("--serve-requests", type=int, default=256, help="served-stream sample: requests (0 skips it)")
-    p.add_argument("--serve-step-scale", type=float, default=0.01,
+    p.add_argument("--sweep-steps", type=int, default=1000, help="field-sweep sample: steps per replica")
+    p.add_argument("--serve-requests", type=int, default=4096, help="served stream: requests (0 skips it)")
+    p.add_argument("--serve-step-scale", type=float, default=0.02,
                    help="served-stream sample: factor on the drawn step counts (1e3..1e5 log-uniform)")
     p.add_argument("--stress-steps", type=int, default=20, help="stress-instance sample: steps (0 skips it)")
     p.add_argument("--autotune", type=int, default=0, help="candidate cutoffs timed (0: the cost-model choice, the same one the reference arm uses)")
@@ -528,7 +528,7 @@ def serve_sample(nreq, step_scale, plain_sample=8):
                                            "sample": f"{len(idx)} requests of the stream, each alone on the "
                                                      f"FP64 path (MD_PREC_FP64), a few steps each"},
             "vs_plain_fp64": (value / plain) if plain else None,
-            "sample": f"first {nreq} requests of the stream (Poisson 200/s; N log-uniform 128..16384; volume "
+            "sample": f"{'all' if nreq >= 4096 else 'first'} {nreq} requests of the stream (Poisson 200/s; N log-uniform 128..16384; volume "
                       f"fraction 0.02..0.15; steps log-uniform 1e3..1e5 scaled by {step_scale}; sinusoidal "
                       f"field 10..30 mT, 10..100 kHz); 150 GB budget, realtime admission, mixed precision"}
 
@@ -612,6 +612,9 @@ def run_ours(args):
     serial_ms = sum(seg_mean.values())
     pairs = sim.pairs()
     strong = sim.strong_pairs()
+    ring, waves, chunk = sim.kspace_tiling()
+    kspace = {"tensor_cores": bool(sim.kspace_tensor_cores()), "sf_ring_option": ring, "sf_chunk_waves": waves,
+              "sf_chunk_particles": chunk, "chosen_by": "autotuner" if args.autotune > 0 else "defaults"}
     nk_real = len(sim.debug_structure_factor())
     clk = clocks.stop()  # sampled over both timed runs
 
@@ -732,7 +735,8 @@ def run_ours(args):
                            "ewald": {"alpha_L": alpha * L, "rc_over_L": rc / L, "kc": kc,
                                      "pred_force_err_rel_contact": errF, "pred_torque_err_rel_contact": errT,
                                      "pairs": pairs, "k_vectors": nk_real,
-                                     "strong_pair_entries_fp64": strong}},
+                                     "strong_pair_entries_fp64": strong},
+                           "kspace": kspace},
                 "e2e": e2e, "roofline": roofline, "segments": segs,
                 "continuous": {"ms_per_step": cont_ms, "value": ws * n / (cont_ms * 1e-3),
                                "note": "graph replays back to back without L2 flush"},

@@ -200,9 +200,21 @@ int md_set_ewald(md_ctx* ctx, double alpha, double rc, int64_t kc);
 int md_set_kspace_engine(md_ctx* ctx, int engine);
 /* *tensor_cores = 1 when the current Ewald parameters use the tensor cores. */
 int md_kspace_engine_active(const md_ctx* ctx, int* tensor_cores);
+/* Tiling of the tensor-core structure factor (no counterpart in the
+ * reference; the autotuner's knobs): ring = the operand-ring option (0..5,
+ * deeper rings first; -1: the deepest that fits shared memory), waves = the
+ * multiple (1..4) of the chunk count that fills whole waves of resident
+ * blocks (more, smaller particle chunks).  The same sums, to the kernels'
+ * precision (smaller chunks add fewer terms per tensor-memory accumulator). */
+int md_set_kspace_tiling(md_ctx* ctx, int ring, int waves);
+/* The tiling in use; chunk = particles per structure-factor chunk (0 when
+ * the tensor cores are off). */
+int md_get_kspace_tiling(const md_ctx* ctx, int* ring, int* waves, int* chunk);
 /* Times candidate cut-offs on the device and sets the fastest that meets
  * the error model; the GPU counterpart of the timing sweep of
- * CompEwaldParams (src/interaction.cpp:185-296). */
+ * CompEwaldParams (src/interaction.cpp:185-296).  At the chosen cut-off it
+ * also times the k-space engines and the tensor-core tilings
+ * (md_set_kspace_tiling) on the mixed path and keeps the fastest. */
 int md_autotune_ewald(md_ctx* ctx, int ncand, double* alpha, double* rc, int64_t* kc,
                       double* best_ms);
 

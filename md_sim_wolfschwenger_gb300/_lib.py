@@ -114,6 +114,8 @@ def lib():
         "md_set_ewald": (C.c_int, [V, C.c_double, C.c_double, I64]),
         "md_set_kspace_engine": (C.c_int, [V, C.c_int]),
         "md_kspace_engine_active": (C.c_int, [V, C.POINTER(C.c_int)]),
+        "md_set_kspace_tiling": (C.c_int, [V, C.c_int, C.c_int]),
+        "md_get_kspace_tiling": (C.c_int, [V, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "md_ewald_params_host": (C.c_int, [C.POINTER(MdConfig), I64, P, P, C.c_double, P, P, PI64, P, P, P]),
         "md_autotune_ewald": (C.c_int, [V, C.c_int, P, P, PI64, P]),
         "md_compute_interactions": (C.c_int, [V, P, P, P]),

@@ -582,7 +582,7 @@ static int setup_tc(md_ctx* c) {
     if (c->klist.kreal[k]) kmap[(size_t)rowid[{c->klist.kz[k], c->klist.ky[k]}] * Q + c->klist.kx[k] + kc] = k;
   int nsm = 148;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
-  const md::TcShape t = md::kspace_tc_shape(kc, (int)c->n, R, nsm);
+  const md::TcShape t = md::kspace_tc_shape(kc, (int)c->n, R, nsm, c->tc_ring, c->tc_waves);
   void* old[] = {c->tc_row, c->tc_rowd, c->tc_kmap, c->tc_part, c->tc_wfull, c->tc_wfield, c->tc_bimg, c->tc_tblk};
   for (void* q : old) dfree(c, q);
   c->tc_row = nullptr;
@@ -1095,6 +1095,25 @@ int md_set_kspace_engine(md_ctx* c, int engine) {
 int md_kspace_engine_active(const md_ctx* c, int* tensor_cores) {
   if (!c || !tensor_cores) return MD_ERR_INVALID;
   *tensor_cores = c->tc_rows > 0 ? 1 : 0;
+  return MD_OK;
+}
+
+int md_set_kspace_tiling(md_ctx* c, int ring, int waves) {
+  if (!c || ring < -1 || ring > 5 || waves < 1 || waves > 4) return set_err(c, MD_ERR_INVALID, "bad k-space tiling");
+  invalidate_graph(c);
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->tc_ring = ring;
+  c->tc_waves = waves;
+  c->have_geometry = false;  // the per-step operands come with the next full evaluation
+  if (c->have_ewald) return setup_tc(c);
+  return MD_OK;
+}
+
+int md_get_kspace_tiling(const md_ctx* c, int* ring, int* waves, int* chunk) {
+  if (!c) return MD_ERR_INVALID;
+  if (ring) *ring = c->tc_ring;
+  if (waves) *waves = c->tc_waves;
+  if (chunk) *chunk = c->tc_rows > 0 ? c->tcs.chunk : 0;
   return MD_OK;
 }
 
@@ -1748,10 +1767,69 @@ int md_autotune_ewald(md_ctx* c, int ncand, double* alpha_out, double* rc_out, i
       bk = k;
     }
   }
+  if (best >= 1e300) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return set_err(c, MD_ERR_INVALID, "no candidate cutoff met the error model");
+  }
+  if ((st = md_set_ewald(c, ba, brc, bk))) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return st;
+  }
+  // at the chosen cutoff: the k-space engine and, on the tensor cores, the
+  // structure factor's ring option and chunk count (waves), timed the same way
+  if (!fp64(c)) {
+    struct Cand {
+      int engine, ring, waves;
+    };
+    std::vector<Cand> cands;
+    const int eng0 = c->kengine;
+    if (md::kspace_tc_supported((int)bk) && eng0 != MD_KSPACE_SIMT) {
+      int ro[6];
+      const int nr = md::kspace_tc_ring_options((int)bk, ro, 6);
+      for (int q = 0; q < nr && q < 3; q++)
+        for (int w = 1; w <= 2; w++) cands.push_back({MD_KSPACE_AUTO, ro[q], w});
+      cands.push_back({MD_KSPACE_SIMT, -1, 1});
+    }
+    double bms = 1e300;
+    Cand bc{eng0, c->tc_ring, c->tc_waves};
+    for (const Cand& cd : cands) {
+      c->kengine = cd.engine;
+      c->tc_ring = cd.ring;
+      c->tc_waves = cd.waves;
+      if (setup_tc(c) != MD_OK) continue;
+      invalidate_graph(c);
+      float msum = 0;
+      for (int rep = 0; rep < 3; rep++) {
+        CK(c, cudaEventRecord(e0, c->stream));
+        issue_interactions(c);
+        issue_field(c);
+        CK(c, cudaEventRecord(e1, c->stream));
+        CK(c, cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0) msum += ms;
+      }
+      if (msum / 2 < bms) {
+        bms = msum / 2;
+        bc = cd;
+      }
+    }
+    c->kengine = bc.engine;
+    c->tc_ring = bc.ring;
+    c->tc_waves = bc.waves;
+    if ((st = setup_tc(c))) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return st;
+    }
+    invalidate_graph(c);
+    c->have_geometry = false;
+    if (bms < 1e300) best = std::min(best, bms);
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (best >= 1e300) return set_err(c, MD_ERR_INVALID, "no candidate cutoff met the error model");
-  if ((st = md_set_ewald(c, ba, brc, bk))) return st;
   if (alpha_out) *alpha_out = ba;
   if (rc_out) *rc_out = brc;
   if (kc_out) *kc_out = bk;
@@ -1763,7 +1841,12 @@ int md_autotune_ewald(md_ctx* c, int ncand, double* alpha_out, double* rc_out, i
 // volume fraction in steps of 0.01.
 namespace {
 std::mutex g_tune_mu;
-std::map<std::pair<int, int>, double> g_tune;  // bucket -> rc / L
+// bucket -> tuned choices: rc / L, k-space engine, structure-factor ring option, chunk waves
+struct TuneEntry {
+  double x;
+  int engine, ring, waves;
+};
+std::map<std::pair<int, int>, TuneEntry> g_tune;
 std::pair<int, int> tune_key(int64_t n, double volFrac) {
   return {(int)std::floor(2.0 * std::log2((double)n)), (int)std::lround(volFrac * 100.0)};
 }
@@ -1773,10 +1856,12 @@ int md_autotune_ewald_cached(md_ctx* c, double volFrac, double* alpha, double* r
   if (!c || !c->have_particles || !c->have_state) return set_err(c, MD_ERR_INVALID, "particles or state not set");
   const auto key = tune_key(c->n, volFrac);
   double x = -1;
+  TuneEntry te{-1, MD_KSPACE_AUTO, -1, 1};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
-    if (it != g_tune.end()) x = it->second;
+    if (it != g_tune.end()) te = it->second;
+    x = te.x;
   }
   if (hit) *hit = x > 0;
   if (x > 0) {
@@ -1784,6 +1869,11 @@ int md_autotune_ewald_cached(md_ctx* c, double volFrac, double* alpha, double* r
     double a = 0, kr = 0;
     if (mdh::ewald_for_rc(c->cfg, m, x * c->L, &a, &kr)) {
       const int64_t k = std::max<int64_t>(1, (int64_t)std::floor(kr + 0.5));
+      if (!fp64(c)) {
+        c->kengine = te.engine;
+        c->tc_ring = te.ring;
+        c->tc_waves = te.waves;
+      }
       int st = md_set_ewald(c, a, x * c->L, k);
       if (st == MD_OK) {
         if (alpha) *alpha = a;
@@ -1800,7 +1890,7 @@ int md_autotune_ewald_cached(md_ctx* c, double volFrac, double* alpha, double* r
   if (st) return st;
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = r / c->L;
+    g_tune[key] = TuneEntry{r / c->L, c->kengine, c->tc_ring, c->tc_waves};
   }
   if (alpha) *alpha = a;
   if (rc) *rc = r;
@@ -1813,8 +1903,10 @@ int md_tune_cache_save(const char* path) {
   FILE* f = std::fopen(path, "w");
   if (!f) return set_err(nullptr, MD_ERR_INVALID, "cannot write %s", path);
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  std::fprintf(f, "# n_bucket(2*log2 N) volfrac_bucket(x100) rc_over_L\n");
-  for (const auto& kv : g_tune) std::fprintf(f, "%d %d %.17g\n", kv.first.first, kv.first.second, kv.second);
+  std::fprintf(f, "# n_bucket(2*log2 N) volfrac_bucket(x100) rc_over_L kspace_engine sf_ring sf_waves\n");
+  for (const auto& kv : g_tune)
+    std::fprintf(f, "%d %d %.17g %d %d %d\n", kv.first.first, kv.first.second, kv.second.x, kv.second.engine,
+                 kv.second.ring, kv.second.waves);
   std::fclose(f);
   return MD_OK;
 }
@@ -1826,9 +1918,17 @@ int md_tune_cache_load(const char* path) {
   char line[256];
   std::lock_guard<std::mutex> lk(g_tune_mu);
   while (std::fgets(line, sizeof line, f)) {
-    int a = 0, b = 0;
+    int a = 0, b = 0, eng = MD_KSPACE_AUTO, ring = -1, waves = 1;
     double x = 0;
-    if (line[0] != '#' && std::sscanf(line, "%d %d %lf", &a, &b, &x) == 3 && x > 0 && x <= 0.5) g_tune[{a, b}] = x;
+    const int got = line[0] == '#' ? 0 : std::sscanf(line, "%d %d %lf %d %d %d", &a, &b, &x, &eng, &ring, &waves);
+    if (got >= 3 && x > 0 && x <= 0.5) {
+      if (got < 6 || eng < MD_KSPACE_AUTO || eng > MD_KSPACE_TC || ring < -1 || ring > 5 || waves < 1 || waves > 4) {
+        eng = MD_KSPACE_AUTO;  // a line with the cutoff only: default k-space choices
+        ring = -1;
+        waves = 1;
+      }
+      g_tune[{a, b}] = TuneEntry{x, eng, ring, waves};
+    }
   }
   std::fclose(f);
   return MD_OK;

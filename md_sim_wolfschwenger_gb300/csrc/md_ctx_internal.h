@@ -117,6 +117,7 @@ struct md_ctx {
   // their buffers (tc_rows = 0 while the engine is off)
   int kengine = MD_KSPACE_AUTO;
   long long tc_wait = 2000000000LL;  // mbarrier wait limit of the tensor-core kernels (SM cycles)
+  int tc_ring = -1, tc_waves = 1;     // structure-factor ring option and chunk-count multiplier (tuning)
   int tc_rows = 0;
   TcShape tcs{};
   int2* tc_row = nullptr;

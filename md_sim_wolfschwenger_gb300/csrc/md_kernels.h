@@ -73,7 +73,10 @@ struct TcShape {
 };
 bool kspace_tc_supported(int kc);
 int kspace_tc_max_kc();  // largest supported kc
-TcShape kspace_tc_shape(int kc, int n, int rows, int nsm);
+// ring: structure-factor ring option (-1: the deepest that fits); waves:
+// multiplier of the wave-filling chunk count (1 .. 4).
+TcShape kspace_tc_shape(int kc, int n, int rows, int nsm, int ring = -1, int waves = 1);
+int kspace_tc_ring_options(int kc, int* opts_out, int cap);
 size_t kspace_tc_image_floats(int kc, int nt);  // scatter operand image of nt tiles
 // Scatter row descriptors: R rows padded to whole tiles of both shapes;
 // (ny, nz, Y offset, Z offset bits) per row into out[kspace_tc_rows_pad(R)],

@@ -135,10 +135,17 @@ struct SfLayout {
 // issuers, an issuer could pass the wait one phase early and read a slot
 // that still held stage s - na.)  The copied ring is waited on only by the
 // copy producer and the generators, which take every stage in order.
-static SfLayout sf_layout(int kc) {
+// ring >= 0 picks option `ring` of the list when it fits (a tuning choice);
+// otherwise the deepest option that fits.
+constexpr int kSfRingOpts = 6;
+static SfLayout sf_layout(int kc, int ring = -1) {
   const int ns = tc_ns(kc), k1 = kc + 1;
-  const int opts[6][2] = {{8, 6}, {8, 5}, {8, 4}, {4, 4}, {4, 3}, {4, 2}};
+  const int opts[kSfRingOpts][2] = {{8, 6}, {8, 5}, {8, 4}, {4, 4}, {4, 3}, {4, 2}};
   static_assert(8 % kSfIssuers == 0 && 4 % kSfIssuers == 0, "generated ring depths: multiples of the issuers");
+  if (ring >= 0 && ring < kSfRingOpts) {
+    SfLayout l(ns, k1, opts[ring][0], opts[ring][1]);
+    if ((size_t)l.bytes <= kSmemLimit) return l;
+  }
   for (const auto& o : opts) {
     SfLayout l(ns, k1, o[0], o[1]);
     if ((size_t)l.bytes <= kSmemLimit) return l;
@@ -146,6 +153,16 @@ static SfLayout sf_layout(int kc) {
   return SfLayout(ns, k1, 4, 1);
 }
 static size_t sf_smem(int kc) { return (size_t)sf_layout(kc).bytes; }
+
+// Ring options of the structure factor that fit for kc (tuning candidates).
+int kspace_tc_ring_options(int kc, int* opts_out, int cap) {
+  const int ns = tc_ns(kc), k1 = kc + 1;
+  const int opts[kSfRingOpts][2] = {{8, 6}, {8, 5}, {8, 4}, {4, 4}, {4, 3}, {4, 2}};
+  int m = 0;
+  for (int q = 0; q < kSfRingOpts; q++)
+    if ((size_t)SfLayout(ns, k1, opts[q][0], opts[q][1]).bytes <= kSmemLimit && m < cap) opts_out[m++] = q;
+  return m;
+}
 // Scatter shared memory: nst W-tile stages | (yz) the Y, Z phases of the
 // block's particles [2 (kc + 1)][128] float2.
 static size_t scat_smem(int kc, int nst, int /*rows*/, bool yz = false) {
@@ -854,7 +871,7 @@ int kspace_tc_max_kc() {
   return k;
 }
 
-TcShape kspace_tc_shape(int kc, int n, int rows, int nsm) {
+TcShape kspace_tc_shape(int kc, int n, int rows, int nsm, int ring, int wave_mult) {
   TcShape s{};
   s.ns = tc_ns(kc);
   s.kp = tc_kp(kc);
@@ -871,16 +888,17 @@ TcShape kspace_tc_shape(int kc, int n, int rows, int nsm) {
   s.rt_full = ScatLayout<true>::RT;
   s.rt_field = ScatLayout<false>::RT;
   s.nsb = (n + kSfSC - 1) / kSfSC;
-  const SfLayout sl = sf_layout(kc);
+  const SfLayout sl = sf_layout(kc, ring);
   s.sfa = sl.na;
   s.sfb = sl.nb;
   // structure-factor grid: M tiles x chunks of <= kSfMaxChunk particles, the chunk
-  // count filling whole waves of resident blocks
-  int res = (int)((228 * 1024) / (sf_smem(kc) + 4096));
+  // count filling whole waves of resident blocks (times `waves`: more, smaller
+  // chunks, a tuning choice)
+  int res = (int)((228 * 1024) / ((size_t)sl.bytes + 4096));
   res = std::max(1, std::min(res, 2));
   const long slots = (long)nsm * res;
   const long nch_min = std::max(1L, ((long)n + kSfMaxChunk - 1) / kSfMaxChunk);
-  const long waves = std::max(1L, ((long)s.mt * nch_min + slots - 1) / slots);
+  const long waves = std::max(1L, ((long)s.mt * nch_min + slots - 1) / slots) * std::max(1, std::min(wave_mult, 4));
   long nch = std::max(nch_min, waves * slots / (long)std::max(1, s.mt));
   nch = std::min<long>(nch, std::max(1L, ((long)n + kSfSC - 1) / kSfSC));
   s.chunk = (int)((((long)n + nch - 1) / nch + kSfSC - 1) / kSfSC * kSfSC);
@@ -915,7 +933,7 @@ int launch_kspace_tc_prep(cudaStream_t st, const KParams& p) {
 }
 
 int launch_kspace_tc(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* ev) {
-  const size_t sm1 = sf_smem(p.kc);
+  const size_t sm1 = (size_t)SfLayout(p.tc_ns, p.kc + 1, p.tc_sfa, p.tc_sfb).bytes;
   cudaFuncSetAttribute(k_sf_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   k_sf_tc<<<dim3(p.tc_mt, p.tc_nchunk), kSfThreads, sm1, st>>>(p);
   if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);

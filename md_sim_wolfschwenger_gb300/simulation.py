@@ -191,6 +191,17 @@ class Simulation:
         code = {"auto": 0, "simt": 1, "tc": 2}[engine]
         self._ck(self.L.md_set_kspace_engine(self.h, code))
 
+    def set_kspace_tiling(self, ring=-1, waves=1):
+        """Tensor-core structure factor tiling: ring option (-1: deepest that
+        fits) and the chunk-count multiple (1..4)."""
+        self._ck(self.L.md_set_kspace_tiling(self.h, int(ring), int(waves)))
+
+    def kspace_tiling(self):
+        """(ring, waves, particles per structure-factor chunk)."""
+        r, w, ch = C.c_int(), C.c_int(), C.c_int()
+        self._ck(self.L.md_get_kspace_tiling(self.h, C.byref(r), C.byref(w), C.byref(ch)))
+        return r.value, w.value, ch.value
+
     def kspace_tensor_cores(self):
         """True when the current Ewald parameters run the k space on the tensor cores."""
         v = C.c_int()

@@ -145,3 +145,47 @@ def test_tc_small_and_ragged(n, kc):
     # with a handful of particles the k-space (periodic image) field is most
     # of the field, so the engines' FP32-level differences weigh more
     assert O.rms_rel(Bt, Bs, bAl) < 5e-6 and O.rms_rel(Ft, Fs, fAl) < 5e-6
+
+
+def test_tiling_options_give_the_same_sums():
+    """Every tensor-core tiling the autotuner may pick (structure-factor ring
+    option, chunk-count multiple) computes the same k-space sums: field and
+    force against the FP64 path within the mixed budget, and against each
+    other to the tensor cores' accumulation error."""
+    ini, g = random_system(3000, seed=17, rc_frac=0.25)
+    fAl, bAl, _ = scales(ini, g)
+    ref = gpu_system(ini, g, 0)
+    B0, F0, _ = ref.CompInteractions()
+    base = None
+    for ring in (-1, 0, 3, 4, 5):
+        for waves in (1, 2):
+            sim = gpu_system(ini, g, 1)
+            sim.set_kspace_tiling(ring, waves)
+            assert sim.kspace_tensor_cores()
+            B, F, _ = sim.CompInteractions()
+            assert O.rms_rel(B, B0, bAl) < TOL_MIXED and O.rms_rel(F, F0, fAl) < TOL_MIXED, (ring, waves)
+            if base is None:
+                base = (B, F)
+            else:
+                assert O.rms_rel(B, base[0], bAl) < 1e-6 and O.rms_rel(F, base[1], fAl) < 1e-6, (ring, waves)
+            sim.close()
+
+
+def test_autotune_keeps_tiling_in_cache():
+    """The autotuner's k-space choices (engine, ring, waves) are cached with
+    the cut-off and applied again on a hit."""
+    import md_sim_wolfschwenger_gb300 as m
+    m.tune_cache_clear()
+    ini, g = random_system(2048, seed=19, rc_frac=0.3)
+    a = gpu_system(ini, g, 1)
+    r1 = m.autotune_ewald_cached(a, 0.05)
+    assert not r1[3]
+    t1, e1 = a.kspace_tiling()[:2], a.kspace_tensor_cores()
+    ini2, g2 = random_system(2048, seed=20, rc_frac=0.3)
+    b = gpu_system(ini2, g2, 1)
+    r2 = m.autotune_ewald_cached(b, 0.05)
+    assert r2[3]
+    assert b.kspace_tiling()[:2] == t1 and b.kspace_tensor_cores() == e1
+    B, F, _ = b.CompInteractions()
+    assert np.all(np.isfinite(B)) and np.all(np.isfinite(F))
+    m.tune_cache_clear()

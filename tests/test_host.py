@@ -204,3 +204,20 @@ def test_tune_cache_file_round_trip(tmp_path):
     m.tune_cache_save(q)
     assert q.read_text().splitlines()[1:] == ["24 5 0.25", "26 10 0.3125"]
     m.tune_cache_clear()
+
+
+def test_tune_cache_file_round_trip(tmp_path):
+    """The tuning cache file keeps, per (N, volume fraction) bucket, the
+    cut-off and the k-space choices (engine, ring option, chunk waves); a line
+    with the cut-off only (an older file) loads with default choices."""
+    import md_sim_wolfschwenger_gb300 as m
+    src = tmp_path / "in.txt"
+    src.write_text("# header\n30 5 0.245 1 3 2\n28 10 0.3\n26 12 0.9 0 0 1\n")
+    m.tune_cache_clear()
+    m.tune_cache_load(src)
+    out = tmp_path / "out.txt"
+    m.tune_cache_save(out)
+    m.tune_cache_clear()
+    rows = [ln.split() for ln in out.read_text().splitlines() if not ln.startswith("#")]
+    got = {(int(r[0]), int(r[1])): (float(r[2]), int(r[3]), int(r[4]), int(r[5])) for r in rows}
+    assert got == {(30, 5): (0.245, 1, 3, 2), (28, 10): (0.3, 0, -1, 1)}  # rc > 0.5 L is refused
