@@ -235,8 +235,13 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
   float2 r = mul2(rfx, pk1(sc));
   const float2 dcont = pk(wdc + ma.w, wdc + mb.w);
   const bool ovA = inA && r.x < dcont.x, ovB = inB && r.y < dcont.y;
+  // the pair vector in box units is (dxf, dyf, dzf) * gsc: 2^-32, or, for a
+  // pair clamped to contact, the unit vector times the contact distance
+  float2 gsc = pk1(sc);
   if (ovA || ovB) {  // rare: clamp overlapping pairs to contact
     const float s32 = 4294967296.0f;
+    if (ovA) gsc.x = irf.x * dcont.x;
+    if (ovB) gsc.y = irf.y * dcont.y;
     if (ovA) {
       if constexpr (FULL) {
         const float h = 0.5f * (dcont.x - r.x);
@@ -282,38 +287,40 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
   const float2 t = mul2(mul2(pk1(K.c2a), e), ire2);
   if constexpr (FULL) {
     // field + force: packed coefficients, then each pair assembled in scalar
-    // code (as pair_terms), which keeps fewer values live
+    // code (as pair_terms), which keeps fewer values live.  The assembly uses
+    // the pair vector d = r u itself: B = a2 (mj.d) d - a1 mj, F_ij = (a2 m12
+    // - a3 (mi.d)(mj.d)) d + a2 ((mj.d) mi + (mi.d) mj), P += d_x F_y, ...
+    // (no normalisation, fewer products of r)
     const float2 w = pk(wA ? 1.f : 0.f, wB ? 1.f : 0.f);
     const float2 a1 = mul2(fma2(mul2(erfcv, ire2), ire, t), w);
     const float2 tw = mul2(t, w);
     const float2 a2c = fma2(mul2(pk1(3.f), a1), ire2, mul2(pk1(K.al2x2), tw));
     const float2 a3 = fma2(mul2(pk1(5.f), a2c), ire2, mul2(pk1(K.al4x4), tw));
-    const float2 re2 = mul2(r, r);
-    auto assemble = [&](float a1s, float a2s, float a3s, float rs, float re2s, float uxs, float uys, float uzs,
-                        const float4& mj) {
+    const float2 dvx = mul2(dxf, gsc), dvy = mul2(dyf, gsc), dvz = mul2(dzf, gsc);
+    auto assemble = [&](float a1s, float a2s, float a3s, float dx, float dy, float dz, const float4& mj) {
       // dot products in scalar code: packed, they would first pair up the
       // two neighbours' moment components
-      const float d1s = mi.x * uxs + mi.y * uys + mi.z * uzs;
-      const float d2s = mj.x * uxs + mj.y * uys + mj.z * uzs;
-      const float c1 = a2s * d2s * re2s;
-      a.b0 = fmaf(c1, uxs, fmaf(-a1s, mj.x, a.b0));
-      a.b1 = fmaf(c1, uys, fmaf(-a1s, mj.y, a.b1));
-      a.b2 = fmaf(c1, uzs, fmaf(-a1s, mj.z, a.b2));
-      const float m12 = mi.x * mj.x + mi.y * mj.y + mi.z * mj.z;
-      const float s1 = (a2s * m12 - a3s * d1s * d2s * re2s) * rs;
-      const float s2 = a2s * rs;
-      const float vx = s1 * uxs + s2 * (d2s * mi.x + d1s * mj.x);
-      const float vy = s1 * uys + s2 * (d2s * mi.y + d1s * mj.y);
-      const float vz = s1 * uzs + s2 * (d2s * mi.z + d1s * mj.z);
+      const float D1 = fmaf(mi.z, dz, fmaf(mi.y, dy, mi.x * dx));
+      const float D2 = fmaf(mj.z, dz, fmaf(mj.y, dy, mj.x * dx));
+      const float e2 = a2s * D2;
+      a.b0 = fmaf(e2, dx, fmaf(-a1s, mj.x, a.b0));
+      a.b1 = fmaf(e2, dy, fmaf(-a1s, mj.y, a.b1));
+      a.b2 = fmaf(e2, dz, fmaf(-a1s, mj.z, a.b2));
+      const float m12 = fmaf(mi.z, mj.z, fmaf(mi.y, mj.y, mi.x * mj.x));
+      const float t1 = fmaf(-a3s * D1, D2, a2s * m12);
+      const float e1 = a2s * D1;
+      const float vx = fmaf(t1, dx, fmaf(e2, mi.x, e1 * mj.x));
+      const float vy = fmaf(t1, dy, fmaf(e2, mi.y, e1 * mj.y));
+      const float vz = fmaf(t1, dz, fmaf(e2, mi.z, e1 * mj.z));
       a.f0 -= vx;
       a.f1 -= vy;
       a.f2 -= vz;
-      a.p0 += rs * uxs * vy;
-      a.p1 += rs * uxs * vz;
-      a.p2 += rs * uys * vz;
+      a.p0 = fmaf(dx, vy, a.p0);
+      a.p1 = fmaf(dx, vz, a.p1);
+      a.p2 = fmaf(dy, vz, a.p2);
     };
-    assemble(a1.x, a2c.x, a3.x, r.x, re2.x, ux.x, uy.x, uz.x, ma);
-    assemble(a1.y, a2c.y, a3.y, r.y, re2.y, ux.y, uy.y, uz.y, mb);
+    assemble(a1.x, a2c.x, a3.x, dvx.x, dvy.x, dvz.x, ma);
+    assemble(a1.y, a2c.y, a3.y, dvx.y, dvy.y, dvz.y, mb);
   } else {
     // B += a2 (mj.u) r^2 u - a1 mj, with the weight negated (wn = -w): a1n =
     // -a1, and a2 r^2 = (3 a1 ire2 + 2 alpha^2 t w) r2f 2^-64
