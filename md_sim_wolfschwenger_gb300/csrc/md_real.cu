@@ -230,25 +230,25 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
   r2f = pk(inA ? r2f.x : rc2_fix, inB ? r2f.y : rc2_fix);
   a.np += (int)inA + (int)inB;
   float2 irf = pk(rsqrt_ftz(r2f.x), rsqrt_ftz(r2f.y));  // 1 / r_fix
-  const float2 ux = mul2(dxf, irf), uy = mul2(dyf, irf), uz = mul2(dzf, irf);
   float2 rfx = mul2(r2f, irf);  // r_fix
   float2 r = mul2(rfx, pk1(sc));
   const float2 dcont = pk(wdc + ma.w, wdc + mb.w);
   const bool ovA = inA && r.x < dcont.x, ovB = inB && r.y < dcont.y;
-  // the pair vector in box units is (dxf, dyf, dzf) * gsc: 2^-32, or, for a
-  // pair clamped to contact, the unit vector times the contact distance
-  float2 gsc = pk1(sc);
   if (ovA || ovB) {  // rare: clamp overlapping pairs to contact
     const float s32 = 4294967296.0f;
-    if (ovA) gsc.x = irf.x * dcont.x;
-    if (ovB) gsc.y = irf.y * dcont.y;
+    // push along the unit vector d / r; then the pair vector itself is
+    // rescaled to the contact length, which the assembly below uses
     if (ovA) {
       if constexpr (FULL) {
-        const float h = 0.5f * (dcont.x - r.x);
-        a.o0 -= h * ux.x;
-        a.o1 -= h * uy.x;
-        a.o2 -= h * uz.x;
+        const float h = 0.5f * (dcont.x - r.x) * irf.x;
+        a.o0 -= h * dxf.x;
+        a.o1 -= h * dyf.x;
+        a.o2 -= h * dzf.x;
       }
+      const float g = dcont.x * s32 * irf.x;
+      dxf.x *= g;
+      dyf.x *= g;
+      dzf.x *= g;
       r.x = dcont.x;
       rfx.x = dcont.x * s32;
       irf.x = rcp_ftz(rfx.x);
@@ -256,11 +256,15 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
     }
     if (ovB) {
       if constexpr (FULL) {
-        const float h = 0.5f * (dcont.y - r.y);
-        a.o0 -= h * ux.y;
-        a.o1 -= h * uy.y;
-        a.o2 -= h * uz.y;
+        const float h = 0.5f * (dcont.y - r.y) * irf.y;
+        a.o0 -= h * dxf.y;
+        a.o1 -= h * dyf.y;
+        a.o2 -= h * dzf.y;
       }
+      const float g = dcont.y * s32 * irf.y;
+      dxf.y *= g;
+      dyf.y *= g;
+      dzf.y *= g;
       r.y = dcont.y;
       rfx.y = dcont.y * s32;
       irf.y = rcp_ftz(rfx.y);
@@ -296,7 +300,7 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
     const float2 tw = mul2(t, w);
     const float2 a2c = fma2(mul2(pk1(3.f), a1), ire2, mul2(pk1(K.al2x2), tw));
     const float2 a3 = fma2(mul2(pk1(5.f), a2c), ire2, mul2(pk1(K.al4x4), tw));
-    const float2 dvx = mul2(dxf, gsc), dvy = mul2(dyf, gsc), dvz = mul2(dzf, gsc);
+    const float2 dvx = mul2(dxf, pk1(sc)), dvy = mul2(dyf, pk1(sc)), dvz = mul2(dzf, pk1(sc));  // box units
     auto assemble = [&](float a1s, float a2s, float a3s, float dx, float dy, float dz, const float4& mj) {
       // dot products in scalar code: packed, they would first pair up the
       // two neighbours' moment components
@@ -322,17 +326,18 @@ __device__ __forceinline__ void pair_terms2(const PairK& K, float wdc, float2 dx
     assemble(a1.x, a2c.x, a3.x, dvx.x, dvy.x, dvz.x, ma);
     assemble(a1.y, a2c.y, a3.y, dvx.y, dvy.y, dvz.y, mb);
   } else {
-    // B += a2 (mj.u) r^2 u - a1 mj, with the weight negated (wn = -w): a1n =
-    // -a1, and a2 r^2 = (3 a1 ire2 + 2 alpha^2 t w) r2f 2^-64
+    // B += a2 (mj.d) d - a1 mj with d the pair vector in fixed-point units
+    // (a2 (mj.u) r^2 u), the weight negated (wn = -w): a1n = -a1, and the
+    // 2^-64 of the fixed-point units folded into a2s
     const float2 mjx = pk(ma.x, mb.x), mjy = pk(ma.y, mb.y), mjz = pk(ma.z, mb.z);
-    const float2 d2 = fma2(mjz, uz, fma2(mjy, uy, mul2(mjx, ux)));
+    const float2 d2 = fma2(mjz, dzf, fma2(mjy, dyf, mul2(mjx, dxf)));
     const float2 wn = pk(wA ? -1.f : 0.f, wB ? -1.f : 0.f);
     const float2 a1n = mul2(fma2(mul2(erfcv, ire2), ire, t), wn);
     const float2 a2s = fma2(mul2(pk1(K.ka2n), a1n), ire2, mul2(pk1(K.kt2n), mul2(t, wn)));
-    const float2 c1 = mul2(mul2(a2s, d2), r2f);
-    a2.b0 = fma2(c1, ux, fma2(a1n, mjx, a2.b0));
-    a2.b1 = fma2(c1, uy, fma2(a1n, mjy, a2.b1));
-    a2.b2 = fma2(c1, uz, fma2(a1n, mjz, a2.b2));
+    const float2 c1 = mul2(a2s, d2);
+    a2.b0 = fma2(c1, dxf, fma2(a1n, mjx, a2.b0));
+    a2.b1 = fma2(c1, dyf, fma2(a1n, mjy, a2.b1));
+    a2.b2 = fma2(c1, dzf, fma2(a1n, mjz, a2.b2));
   }
 }
 
