@@ -55,6 +55,7 @@ struct md_batch {
   Task* d_tasks = nullptr;
   size_t task_cap = 0;
   Packed n256{}, sort{}, real{}, phase{}, sk{}, red{}, sc{};
+  WorkQ* d_wq = nullptr;  // one work queue per task table (persistent packed launches)
   int kcmax = 0, np = 64;
   bool coat = false;
   int64_t launches_per_step = 0;
@@ -175,6 +176,17 @@ int pack(md_batch* b) {
   }
   for (Packed* pk : {&b->n256, &b->sort, &b->real, &b->phase, &b->sk, &b->red, &b->sc})
     pk->tasks = b->d_tasks + reinterpret_cast<size_t>(pk->tasks);
+  if (!b->d_wq) {
+    cudaError_t e = cudaMalloc(&b->d_wq, sizeof(WorkQ) * 7);
+    if (e == cudaSuccess) e = cudaMemset(b->d_wq, 0, sizeof(WorkQ) * 7);
+    if (e != cudaSuccess) return set_err(nullptr, MD_ERR_NOMEM, "work queues: %s", cudaGetErrorString(e));
+  }
+  {
+    // launches over one table run in stream order (never two at once), so a
+    // queue per table suffices
+    int q = 0;
+    for (Packed* pk : {&b->n256, &b->sort, &b->real, &b->phase, &b->sk, &b->red, &b->sc}) pk->wq = b->d_wq + q++;
+  }
   int st;
   if ((st = upload(b->d_tasks, tasks, b->stream))) return st;
   if ((st = upload_params(b))) return st;
@@ -322,7 +334,7 @@ int md_batch_destroy(md_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
   void* arrays[] = {b->d_cell, b->d_rfull, b->d_rfield, b->d_kfull, b->d_kfield, b->d_i1, b->d_i2, b->d_obs,
-                    b->d_status, b->d_tasks};
+                    b->d_status, b->d_tasks, b->d_wq};
   for (void* p : arrays)
     if (p) cudaFree(p);
   if (b->ev0) cudaEventDestroy(b->ev0);

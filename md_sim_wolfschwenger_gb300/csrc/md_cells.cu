@@ -20,6 +20,9 @@
 // Roofline: HBM/L2 bound, ~60 B per particle of algorithmic traffic
 // (pos 24 B read, cell id 4+4 B, sorted views 16+16+16 B written, index
 // arrays 8 B) plus 8 B per cell.
+#include <map>
+#include <mutex>
+
 #include "md_common.cuh"
 #include "md_kernels.h"
 
@@ -209,34 +212,62 @@ __global__ void k_step_begin_packed(const CellParams* __restrict__ ps, int R) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < R) step_begin(ps[r].flags, ps[r].half_skin);
 }
+// Packed kernels are persistent: their blocks stride over the task table,
+// finishing one task before the next (the barrier keeps a task's shared
+// memory until every thread of the block is done with it).
 __global__ void __launch_bounds__(kCellThreads) k_cell_assign_packed(const CellParams* __restrict__ ps,
-                                                                     const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const CellParams p = ps[t.rep];
-  cell_assign(p, t.blk);
+                                                                     const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
+      cell_assign(ps[t.rep], t.blk);
+  });
 }
 __global__ void __launch_bounds__(1024) k_cell_scan_packed(const CellParams* __restrict__ ps) {
   const CellParams p = ps[blockIdx.x];
   cell_scan(p);
 }
 __global__ void __launch_bounds__(kCellThreads) k_cell_scatter_packed(const CellParams* __restrict__ ps,
-                                                                      const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const CellParams p = ps[t.rep];
-  cell_scatter(p, t.blk);
+                                                                      const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
+      cell_scatter(ps[t.rep], t.blk);
+  });
 }
 __global__ void __launch_bounds__(kCellThreads) k_cell_sort_packed(const CellParams* __restrict__ ps,
-                                                                   const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const CellParams p = ps[t.rep];
-  cell_sort(p, t.blk);
+                                                                   const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
+      cell_sort(ps[t.rep], t.blk);
+  });
 }
 template <typename T>
 __global__ void __launch_bounds__(kCellThreads) k_sorted_fill_packed(const CellParams* __restrict__ ps,
-                                                                     const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const CellParams p = ps[t.rep];
-  sorted_fill<T>(p, t.blk);
+                                                                     const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
+      sorted_fill<T>(ps[t.rep], t.blk);
+  });
+}
+
+int persistent_grid(const void* fn, int threads, size_t smem, int ntask) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, std::pair<int, size_t>>, int> cache;
+  int per = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_pair(fn, std::make_pair(threads, smem));
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      per = it->second;
+    } else {
+      int dev = 0, nsm = 0, occ = 0;
+      cudaGetDevice(&dev);
+      if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem) != cudaSuccess || occ <= 0) {
+        cudaGetLastError();
+        occ = 1;
+      }
+      per = occ * nsm;
+      cache[key] = per;
+    }
+  }
+  return std::max(1, std::min(per, ntask));
 }
 
 // -------------------------------------------------------- other kernels
@@ -316,21 +347,21 @@ int launch_step_begin_packed(cudaStream_t st, const CellParams* ps, int R) {
 int launch_cells_packed(cudaStream_t st, const CellParams* ps, int R, const Packed& n256, const Packed& sort) {
   int l = 0;
   if (n256.n) {
-    k_cell_assign_packed<<<n256.n, kCellThreads, 0, st>>>(ps, n256.tasks);
+    k_cell_assign_packed<<<persistent_grid((const void*)k_cell_assign_packed, kCellThreads, 0, n256.n), kCellThreads, 0, st>>>(ps, n256.tasks, n256.n, n256.wq);
     l++;
   }
   k_cell_scan_packed<<<R, 1024, 0, st>>>(ps);
   l++;
   if (n256.n) {
-    k_cell_scatter_packed<<<n256.n, kCellThreads, 0, st>>>(ps, n256.tasks);
+    k_cell_scatter_packed<<<persistent_grid((const void*)k_cell_scatter_packed, kCellThreads, 0, n256.n), kCellThreads, 0, st>>>(ps, n256.tasks, n256.n, n256.wq);
     l++;
   }
   if (sort.n) {
-    k_cell_sort_packed<<<sort.n, kCellThreads, 0, st>>>(ps, sort.tasks);
+    k_cell_sort_packed<<<persistent_grid((const void*)k_cell_sort_packed, kCellThreads, 0, sort.n), kCellThreads, 0, st>>>(ps, sort.tasks, sort.n, sort.wq);
     l++;
   }
   if (n256.n) {
-    k_sorted_fill_packed<float><<<n256.n, kCellThreads, 0, st>>>(ps, n256.tasks);
+    k_sorted_fill_packed<float><<<persistent_grid((const void*)k_sorted_fill_packed<float>, kCellThreads, 0, n256.n), kCellThreads, 0, st>>>(ps, n256.tasks, n256.n, n256.wq);
     l++;
   }
   return l;

@@ -81,6 +81,39 @@ struct Task {
   int rep, blk;
 };
 
+// Work queue of one persistent packed launch: blocks claim tasks in turn
+// (atomic ticket), and the last block to finish resets the counters for the
+// next launch (the next replay of the step graph).  Which block runs a task
+// does not change the task's result.
+struct WorkQ {
+  unsigned next, done;
+};
+
+// Task loop of a persistent packed kernel: body(t) for every task claimed by
+// this block; SYNC adds a block barrier after each task (kernels whose tasks
+// use shared memory).
+template <bool SYNC, typename F>
+__device__ __forceinline__ void for_tasks(const Task* __restrict__ tk, int ntask, WorkQ* wq, F&& body) {
+  __shared__ int s_task;
+  for (;;) {
+    if (threadIdx.x == 0) s_task = (int)atomicAdd(&wq->next, 1u);
+    __syncthreads();
+    const int q = s_task;
+    __syncthreads();  // every thread has read the ticket before thread 0 takes the next
+    if (q >= ntask) break;
+    body(tk[q]);
+    if (SYNC) __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&wq->done, 1u) == gridDim.x - 1) {  // all blocks have stopped claiming
+      wq->next = 0;
+      wq->done = 0;
+      __threadfence();
+    }
+  }
+}
+
 // ------------------------------------------------------- real space
 // FP32 loop constants of the packed pair terms (mixed path), computed once on
 // the host: the pair loop reads them from the kernel parameters, so nothing

@@ -397,17 +397,18 @@ __global__ void __launch_bounds__(kIntThreads) k_heun2_obs(IntParams p, ObsParam
   if (threadIdx.x == 0) *done = 0;
 }
 
+// persistent: blocks stride over the task table (see md_cells.cu)
 __global__ void __launch_bounds__(kIntThreads, 4) k_heun1_packed(const IntParams* __restrict__ ps,
-                                                             const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const IntParams p = ps[t.rep];
-  heun1<float>(p, t.blk);
+                                                             const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<false>(tk, ntask, wq, [&](const Task& t) {
+      heun1<float>(ps[t.rep], t.blk);
+  });
 }
 __global__ void __launch_bounds__(kIntThreads, 4) k_heun2_packed(const IntParams* __restrict__ ps,
-                                                             const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const IntParams p = ps[t.rep];
-  heun2<float>(p, t.blk);
+                                                             const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
+      heun2<float>(ps[t.rep], t.blk);
+  });
 }
 __global__ void __launch_bounds__(256) k_obs_packed(const ObsParams* __restrict__ ps) {
   const ObsParams p = ps[blockIdx.x];
@@ -647,13 +648,13 @@ int launch_obs(cudaStream_t st, const ObsParams& p) {
 
 int launch_heun1_packed(cudaStream_t st, const IntParams* ps, const Packed& n256) {
   if (!n256.n) return 0;
-  k_heun1_packed<<<n256.n, kIntThreads, 0, st>>>(ps, n256.tasks);
+  k_heun1_packed<<<persistent_grid((const void*)k_heun1_packed, kIntThreads, 0, n256.n), kIntThreads, 0, st>>>(ps, n256.tasks, n256.n, n256.wq);
   return 1;
 }
 
 int launch_heun2_packed(cudaStream_t st, const IntParams* ps, const Packed& n256) {
   if (!n256.n) return 0;
-  k_heun2_packed<<<n256.n, kIntThreads, 0, st>>>(ps, n256.tasks);
+  k_heun2_packed<<<persistent_grid((const void*)k_heun2_packed, kIntThreads, 0, n256.n), kIntThreads, 0, st>>>(ps, n256.tasks, n256.n, n256.wq);
   return 1;
 }
 

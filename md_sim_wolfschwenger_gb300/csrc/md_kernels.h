@@ -15,7 +15,13 @@ namespace md {
 struct Packed {
   const Task* tasks;
   int n;
+  WorkQ* wq;  // work queue of the persistent launches over this table (zeroed)
 };
+
+// Grid of a persistent packed launch: the blocks that one wave of kernel
+// `fn` keeps resident (occupancy x SMs), at most ntask; its blocks stride
+// over the task table.
+int persistent_grid(const void* fn, int threads, size_t smem, int ntask);
 
 // Blocks of one system per kernel shape (task-table construction).
 int cell_blocks(int n);                 // cell assign/scatter/fill, integrator

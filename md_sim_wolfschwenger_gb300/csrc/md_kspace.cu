@@ -420,31 +420,34 @@ __global__ void __launch_bounds__(NP * kScatterParts) k_kscatter(KParams p) {
   kscatter<T, NP, FULL>(p, blockIdx.x, p.kc);
 }
 
+// persistent: blocks stride over the task table (see md_cells.cu)
 __global__ void __launch_bounds__(kPhaseThreads) k_phase_tables_packed(const KParams* __restrict__ ps,
-                                                                       const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const KParams p = ps[t.rep];
-  phase_tables<float>(p, t.blk);
+                                                                       const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<false>(tk, ntask, wq, [&](const Task& t) {
+      phase_tables<float>(ps[t.rep], t.blk);
+  });
 }
 __global__ void __launch_bounds__(kSkThreads, 6) k_sk_packed(const KParams* __restrict__ ps,
-                                                              const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const KParams p = ps[t.rep];
-  const int nsb = (p.nseg + kSkThreads - 1) / kSkThreads;
-  sk_body<float>(p, t.blk % nsb, t.blk / nsb);
+                                                              const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
+      const KParams p = ps[t.rep];
+      const int nsb = (p.nseg + kSkThreads - 1) / kSkThreads;
+      sk_body<float>(p, t.blk % nsb, t.blk / nsb);
+  });
 }
 __global__ void __launch_bounds__(256) k_sk_reduce_packed(const KParams* __restrict__ ps,
-                                                          const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const KParams p = ps[t.rep];
-  sk_reduce<float>(p, t.blk);
+                                                          const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
+      sk_reduce<float>(ps[t.rep], t.blk);
+  });
 }
 template <int NP, bool FULL>
 __global__ void __launch_bounds__(NP * kScatterParts) k_kscatter_packed(const KParams* __restrict__ ps,
-                                                                        const Task* __restrict__ tk, int kcmax) {
-  const Task t = tk[blockIdx.x];
-  const KParams p = ps[t.rep];
-  kscatter<float, NP, FULL>(p, t.blk, kcmax);
+                                                                        const Task* __restrict__ tk, int kcmax,
+                                                                        int ntask, WorkQ* wq) {
+  for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
+      kscatter<float, NP, FULL>(ps[t.rep], t.blk, kcmax);
+  });
 }
 
 int sk_threads() { return kSkThreads; }
@@ -536,18 +539,22 @@ int launch_phase_tables(cudaStream_t st, const KParams& p, bool fp64) {
 
 int launch_phase_tables_packed(cudaStream_t st, const KParams* ps, const Packed& phase) {
   if (!phase.n) return 0;
-  k_phase_tables_packed<<<phase.n, kPhaseThreads, 0, st>>>(ps, phase.tasks);
+  k_phase_tables_packed<<<persistent_grid((const void*)k_phase_tables_packed, kPhaseThreads, 0, phase.n),
+                          kPhaseThreads, 0, st>>>(ps, phase.tasks, phase.n, phase.wq);
   return 1;
 }
 
 template <int NP>
 static void scatter_packed(cudaStream_t st, const KParams* ps, const Packed& sc, bool full, int kcmax, size_t smem) {
+  const int th = NP * kScatterParts;
   if (full) {
     cudaFuncSetAttribute(k_kscatter_packed<NP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_kscatter_packed<NP, true><<<sc.n, NP * kScatterParts, smem, st>>>(ps, sc.tasks, kcmax);
+    const int g = persistent_grid((const void*)k_kscatter_packed<NP, true>, th, smem, sc.n);
+    k_kscatter_packed<NP, true><<<g, th, smem, st>>>(ps, sc.tasks, kcmax, sc.n, sc.wq);
   } else {
     cudaFuncSetAttribute(k_kscatter_packed<NP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_kscatter_packed<NP, false><<<sc.n, NP * kScatterParts, smem, st>>>(ps, sc.tasks, kcmax);
+    const int g = persistent_grid((const void*)k_kscatter_packed<NP, false>, th, smem, sc.n);
+    k_kscatter_packed<NP, false><<<g, th, smem, st>>>(ps, sc.tasks, kcmax, sc.n, sc.wq);
   }
 }
 
@@ -557,11 +564,13 @@ int launch_kspace_packed(cudaStream_t st, const KParams* ps, const Packed& sk, c
   if (sk.n) {
     const size_t sm1 = ksf_smem(kcmax, false);
     cudaFuncSetAttribute(k_sk_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-    k_sk_packed<<<sk.n, kSkThreads, sm1, st>>>(ps, sk.tasks);
+    k_sk_packed<<<persistent_grid((const void*)k_sk_packed, kSkThreads, sm1, sk.n), kSkThreads, sm1, st>>>(
+        ps, sk.tasks, sk.n, sk.wq);
     l++;
   }
   if (red.n) {
-    k_sk_reduce_packed<<<red.n, 256, 0, st>>>(ps, red.tasks);
+    k_sk_reduce_packed<<<persistent_grid((const void*)k_sk_reduce_packed, 256, 0, red.n), 256, 0, st>>>(
+        ps, red.tasks, red.n, red.wq);
     l++;
   }
   if (sc.n) {

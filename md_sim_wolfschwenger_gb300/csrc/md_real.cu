@@ -937,12 +937,14 @@ __global__ void __launch_bounds__(((FULL && COAT) ? kRealWarps : kFieldWarps) * 
   real_eval<T, FULL, COAT, (FULL && COAT) ? kRealWarps : kFieldWarps>(p, blockIdx.x);
 }
 
+// persistent: blocks stride over the task table (see md_cells.cu); the
+// list build and the pair loop are warp-private (no block barrier)
 template <bool FILL>
 __global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build_packed(const RealParams* __restrict__ ps,
-                                                                      const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const RealParams p = ps[t.rep];
-  nbr_build<float, FILL>(p, t.blk);
+                                                                      const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<false>(tk, ntask, wq, [&](const Task& t) {
+      nbr_build<float, FILL>(ps[t.rep], t.blk);
+  });
 }
 __global__ void __launch_bounds__(1024) k_nbr_scan_packed(const RealParams* __restrict__ ps) {
   const RealParams p = ps[blockIdx.x];
@@ -950,10 +952,10 @@ __global__ void __launch_bounds__(1024) k_nbr_scan_packed(const RealParams* __re
 }
 template <bool FULL, bool COAT>
 __global__ void __launch_bounds__(kRealWarps * 32, COAT ? 2 : 4) k_real_packed(const RealParams* __restrict__ ps,
-                                                                 const Task* __restrict__ tk) {
-  const Task t = tk[blockIdx.x];
-  const RealParams p = ps[t.rep];
-  real_eval<float, FULL, COAT>(p, t.blk);
+                                                                 const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+  for_tasks<false>(tk, ntask, wq, [&](const Task& t) {
+      real_eval<float, FULL, COAT>(ps[t.rep], t.blk);
+  });
 }
 
 int real_blocks(int n) { return (n + kRealWarps - 1) / kRealWarps; }
@@ -995,19 +997,27 @@ int launch_real(cudaStream_t st, const RealParams& p, bool full, bool fp64) {
 }
 
 int launch_nbr_packed(cudaStream_t st, const RealParams* ps, int R, const Packed& real) {
-  if (real.n) k_nbr_build_packed<false><<<real.n, kRealWarps * 32, 0, st>>>(ps, real.tasks);
+  const int th = kRealWarps * 32;
+  if (real.n)
+    k_nbr_build_packed<false><<<persistent_grid((const void*)k_nbr_build_packed<false>, th, 0, real.n), th, 0, st>>>(
+        ps, real.tasks, real.n, real.wq);
   k_nbr_scan_packed<<<R, 1024, 0, st>>>(ps);
-  if (real.n) k_nbr_build_packed<true><<<real.n, kRealWarps * 32, 0, st>>>(ps, real.tasks);
+  if (real.n)
+    k_nbr_build_packed<true><<<persistent_grid((const void*)k_nbr_build_packed<true>, th, 0, real.n), th, 0, st>>>(
+        ps, real.tasks, real.n, real.wq);
   return 3;
 }
 
 int launch_real_packed(cudaStream_t st, const RealParams* ps, const Packed& real, bool full, bool coat) {
   if (!real.n) return 0;
+  const int th = kRealWarps * 32;
+  auto go = [&](auto kern) {
+    kern<<<persistent_grid((const void*)kern, th, 0, real.n), th, 0, st>>>(ps, real.tasks, real.n, real.wq);
+  };
   if (full)
-    coat ? k_real_packed<true, true><<<real.n, kRealWarps * 32, 0, st>>>(ps, real.tasks)
-         : k_real_packed<true, false><<<real.n, kRealWarps * 32, 0, st>>>(ps, real.tasks);
+    coat ? go(k_real_packed<true, true>) : go(k_real_packed<true, false>);
   else
-    k_real_packed<false, false><<<real.n, kRealWarps * 32, 0, st>>>(ps, real.tasks);
+    go(k_real_packed<false, false>);
   return 1;
 }
 
