@@ -19,19 +19,20 @@
 // from the accumulators in tensor memory.  Complex products run as real
 // ones: [Re a, Im a] against [[Re b, Im b], [-Im b, Re b]] blocks.
 //
-// Precision: each FP32 operand is split into TF32 hi + lo and the products
-// are hi*hi + hi*lo + lo*hi (three kind::tf32 MMAs into one FP32
-// accumulator), ~22 significant bits per product like FP32 arithmetic.  The
-// tensor core's FP32 accumulation loses precision with the number of MMAs
-// added into one accumulator (measured at N = 32768: 5.5e-6 relative error
-// of S with 392 particles per accumulator, 1.8e-6 with 128), so the
-// structure factor uses chunks of <= 512 particles (4 accumulators of <= 128
-// each, added in FP32) and sums the chunks exactly (error-free FP32 pairs,
-// then FP64), like the reference's FP64 sums over particles; the scatter sums
-// over the nx of a row in the MMA
-// (<= 2 kc + 1 terms), over the rows of a tile in FP32 and over tiles with
-// compensated FP32 sums.  All sums have a fixed order: results are
-// deterministic.
+// Precision: each FP32 operand is split into a hi + lo pair (FP16 pairs in
+// the structure factor, kind::f16; TF32 pairs in the scatter, kind::tf32,
+// whose W operand spans more decades than FP16 holds) and the products are
+// hi*hi + hi*lo + lo*hi (three MMAs into one FP32 accumulator), ~21-22
+// significant bits per product like FP32 arithmetic.  The tensor core's FP32
+// accumulation loses precision with the number of MMAs added into one
+// accumulator (measured at N = 32768: 5.5e-6 relative error of S with 392
+// particles per accumulator, 1.8e-6 with 128), so the structure factor uses
+// chunks of <= 512 particles (4 accumulators of <= 128 each, added in FP32)
+// and sums the chunks exactly (error-free FP32 pairs, then FP64), like the
+// reference's FP64 sums over particles; the scatter sums over the nx of a
+// row in the MMA (<= 2 kc + 1 terms), over the rows of a tile in FP32 and
+// over tiles with compensated FP32 sums.  All sums have a fixed order:
+// results are deterministic.
 //
 // Kernels:
 //   k_tc_prep    once per step (positions are frozen across the step's
@@ -55,11 +56,15 @@
 //                (4 per tile quarter) turn each accumulator into per-row terms
 //                of B and F.
 //
-// Pipeline latency, not arithmetic, bounds these kernels on GB300: a stage
-// is released by tcgen05.commit -> mbarrier, and that round trip (~1-2 us,
-// measured with the stage work removed) is long against the ~0.3 us of MMA
-// work per 16 particles; stages of 32 particles halve the hand-offs per
-// block, and the rings hide the rest only partly.
+// What sets the pace (GB300, measured at N = 32768, kc = 16): an mbarrier
+// hand-off between warps takes ~0.1 us, an MMA commit round trip ~0.2 us
+// plus the MMAs (one 32-particle stage of the structure factor: 12 MMAs,
+// ~0.3 us alone), a bulk copy of a stage from L2 ~0.3 us.  A structure-factor
+// block (16 stages) takes ~19 us: ~0.9 us per stage, in which every role
+// (generators, issuers, copies) runs well below its own rate and no single
+// wait dominates (a per-block timeline of each role's stage events), plus
+// ~5 us of setup, pipeline fill, drain and tensor-memory read-out.  The
+// scatter's CUDA-core epilogue is the bound of the scatter.
 #include "md_common.cuh"
 #include "md_kernels.h"
 #include "md_tc.cuh"
@@ -77,7 +82,7 @@ constexpr int kSfIssuers = 4;        // structure factor: MMA-issuing warps (one
 constexpr int kSfThreads = 32 * (kSfGenWarps + 1 + kSfIssuers);  // + copy producer + issuers
 constexpr int kSfMaxSlots = 8;       // deepest operand rings
 constexpr int kSfMaxChunk = 512;     // particles per structure-factor chunk (4 accumulators of <= 128)
-constexpr int kTabPad = kSfSC + 1;   // Y, Z block row stride (bank spread)
+constexpr int kTabPad = kSfSC + 2;   // Y, Z block row stride: even (16-byte pairs), 4 banks apart
 constexpr int kSfPairs = kSfSC / 2;  // particle pairs per stage (4 K elements each)
 static_assert(kSfSC % 16 == 0, "stages of whole 16-particle generator passes");
 constexpr int kTcMaxKc = 25;         // operand bounds: A of the scatter in 256 tensor-memory columns
@@ -350,11 +355,12 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
     const int arow = 8 * (warp & 7) + (lane & 7);
     const int c0 = (lane >> 3) + 4 * (warp >> 3);  // pair c: particles 2c, 2c + 1 -> k = 4c .. 4c + 3
     const int rg = mtile * 64 + arow;
-    const bool rvalid = rg < p.tc_rows;
-    const int2 rr = rvalid ? p.tc_row[rg] : make_int2(0, 0);
+    // rows beyond R (last M tile) take row (0, 0): finite operands whose
+    // accumulator rows the reduction never reads (a row of A reaches only its
+    // own row of the product)
+    const int2 rr = rg < p.tc_rows ? p.tc_row[rg] : make_int2(0, 0);
     const int ny = rr.x, nz = rr.y, ay = ny < 0 ? -ny : ny;
-    // rows beyond R (last M tile) get zero coefficients: their U, V are 0
-    const float nyf = (float)ny, nzf = (float)nz, vsc = rvalid ? 1.f : 0.f;
+    const float nyf = (float)ny, nzf = (float)nz;
     const float ysg = ny < 0 ? -1.f : 1.f;  // conj Y for ny < 0
     // this thread's first particle in the stage's Y, Z rows and moments
     const int yo = ay * kTabPad + 2 * c0, zo = (K1 + nz) * kTabPad + 2 * c0, mo = 2 * c0;
@@ -367,27 +373,45 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
     // last stage of a chunk: its slot beyond jlim holds older data)
     auto gen = [&](auto checked, unsigned char* sa, const float2* tb, const float4* mus, int jlim) {
       constexpr bool CHECKED = decltype(checked)::value;
-#pragma unroll 1
-      for (int u = 0; u < kSfPairs / 8; u++) {
+      constexpr int NP = kSfPairs / 8;  // passes of two particles
+      // every load of the stage first: the operand stores below go to the
+      // same shared memory, so loads after a store could not be moved up
+      float2 Ys[2 * NP], Zs[2 * NP];
+      float4 Ms[2 * NP];
+#pragma unroll
+      for (int u = 0; u < NP; u++) {
+        // the pass's two particles are adjacent: one 16-byte load per table
+        // row (the rows of a generator warp's 8 lanes fall 4 banks apart)
+        const float4 y2 = *(const float4*)(tb + yo + 16 * u), z2 = *(const float4*)(tb + zo + 16 * u);
+        Ys[2 * u] = make_float2(y2.x, y2.y);
+        Ys[2 * u + 1] = make_float2(y2.z, y2.w);
+        Zs[2 * u] = make_float2(z2.x, z2.y);
+        Zs[2 * u + 1] = make_float2(z2.z, z2.w);
+        Ms[2 * u] = mus[mo + 16 * u];
+        Ms[2 * u + 1] = mus[mo + 16 * u + 1];
+      }
+#pragma unroll
+      for (int u = 0; u < NP; u++) {
         float U[4], V[4];
 #pragma unroll
         for (int h = 0; h < 2; h++) {
           const int jj = 16 * u + h;
-          float2 Y = tb[yo + jj];
-          const float2 Z = tb[zo + jj];
-          float4 mu = mus[mo + jj];
-          float pr = Y.x * Z.x - ysg * Y.y * Z.y, pi = Y.x * Z.y + ysg * Y.y * Z.x;
+          const float2 Y = Ys[2 * u + h];
+          const float2 Z = Zs[2 * u + h];
+          float4 mu = Ms[2 * u + h];
+          const float yi = ysg * Y.y;
+          float pr = fmaf(Y.x, Z.x, -yi * Z.y), pi = fmaf(Y.x, Z.y, yi * Z.x);
           if constexpr (CHECKED) {
             const bool in = mo + jj < jlim;
             pr = in ? pr : 0.f;
             pi = in ? pi : 0.f;
             mu = in ? mu : make_float4(0.f, 0.f, 0.f, 0.f);
           }
-          const float cf = (nyf * mu.y + nzf * mu.z) * vsc, mx = mu.x * vsc;
+          const float cf = fmaf(nyf, mu.y, nzf * mu.z);
           U[2 * h] = cf * pr;
           U[2 * h + 1] = cf * pi;
-          V[2 * h] = mx * pr;
-          V[2 * h + 1] = mx * pi;
+          V[2 * h] = mu.x * pr;
+          V[2 * h + 1] = mu.x * pi;
         }
         uint2 hi, lo;
         unsigned char* d = sa + so + kPairStep * u;

@@ -71,7 +71,8 @@ __device__ __forceinline__ void tc_mma_f16(uint32_t d_tmem, uint64_t a, uint64_t
 __device__ __forceinline__ void f16_split2(float a, float b, uint32_t& hi, uint32_t& lo) {
   const __half2 h = __floats2half2_rn(a, b);
   const float2 hf = __half22float2(h);
-  const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+  const float2 r = __fadd2_rn(make_float2(a, b), make_float2(-hf.x, -hf.y));  // remainders (exact in FP16 range)
+  const __half2 l = __floats2half2_rn(r.x, r.y);
   hi = *reinterpret_cast<const uint32_t*>(&h);
   lo = *reinterpret_cast<const uint32_t*>(&l);
 }
