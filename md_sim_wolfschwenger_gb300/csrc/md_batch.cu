@@ -54,8 +54,13 @@ struct md_batch {
   int* d_status = nullptr;
   Task* d_tasks = nullptr;
   size_t task_cap = 0;
-  Packed n256{}, sort{}, real{}, phase{}, sk{}, red{}, sc{};
+  Packed n256{}, sort{}, real{}, pass{}, phase{}, sk{}, red{}, sc{};
   WorkQ* d_wq = nullptr;  // one work queue per task table (persistent packed launches)
+  // systems whose k space runs on the tensor cores (the context's engine):
+  // operand prep, structure factor, reduction and scatter tables, and the
+  // largest dynamic shared memory among them; the others take sk, red, sc
+  Packed tprep{}, tsf{}, tred{}, tsc{};
+  size_t tc_sf_smem = 0, tc_sc_smem = 0;
   int kcmax = 0, np = 64;
   bool coat = false;
   int64_t launches_per_step = 0;
@@ -87,6 +92,14 @@ int upload(P* d, const std::vector<P>& h, cudaStream_t st) {
   return e == cudaSuccess ? MD_OK : set_err(nullptr, MD_ERR_CUDA, "parameter upload: %s", cudaGetErrorString(e));
 }
 
+// Structure-factor chunking of a tensor-core system in a batch: the fewest
+// chunks of <= 512 particles (the other systems of the batch fill the GPU;
+// alone, md_step splits a small system into more, smaller chunks to fill it),
+// a function of the system alone, so its sums do not depend on the mix.
+TcShape batch_tc_shape(const md_ctx* c) {
+  return kspace_tc_shape((int)c->kc, (int)c->n, c->tc_rows, 1, c->tc_ring, 1);
+}
+
 // Parameters of every system in pack order.
 int upload_params(md_batch* b) {
   const size_t R = b->order.size();
@@ -104,6 +117,12 @@ int upload_params(md_batch* b) {
     rfield[r] = real_params(c, c->Br2, nullptr, nullptr);
     kfull[r] = k_params(c, c->Bk, c->Fk);
     kfield[r] = k_params(c, c->Bk2, nullptr);
+    if (c->tc_rows > 0) {
+      // the context's buffers hold its own (more numerous) chunks' partials
+      const TcShape bt = batch_tc_shape(c);
+      kfull[r].tc_chunk = kfield[r].tc_chunk = bt.chunk;
+      kfull[r].tc_nchunk = kfield[r].tc_nchunk = bt.nchunk;
+    }
     i1[r] = int_params(c, s.dt, c->Br, c->Bk);
     i2[r] = int_params(c, s.dt, c->Br2, c->Bk2);
     // packed launches evaluate every pair in FP32 (no strong-pair kernels):
@@ -138,14 +157,26 @@ int pack(md_batch* b) {
   // larger systems first: their blocks start first in every packed grid
   std::stable_sort(b->order.begin(), b->order.end(),
                    [&](int x, int y) { return b->slots[x].ctx->n > b->slots[y].ctx->n; });
+  // a system's k space runs on the tensor cores in the batch when it does
+  // alone (tc_rows > 0: mixed precision, the tensor-core engine, kc within
+  // the kernels' bounds), otherwise on the CUDA-core kernels
+  auto on_tc = [](const md_ctx* c) { return c->tc_rows > 0; };
   b->kcmax = 0;
   b->coat = false;
+  b->tc_sf_smem = b->tc_sc_smem = 0;
+  bool any_simt = false;
   for (const Slot& s : b->slots) {
-    b->kcmax = std::max<int>(b->kcmax, (int)s.ctx->kc);
+    if (on_tc(s.ctx)) {
+      b->tc_sf_smem = std::max(b->tc_sf_smem, kspace_tc_sf_bytes(s.ctx->tcs, (int)s.ctx->kc));
+      b->tc_sc_smem = std::max(b->tc_sc_smem, (size_t)s.ctx->tcs.scat_smem);
+    } else {
+      b->kcmax = std::max<int>(b->kcmax, (int)s.ctx->kc);
+      any_simt = true;
+    }
     b->coat = b->coat || s.ctx->cfg.ENABLE_COATING_POT;
   }
   b->np = scatter_particles(b->kcmax, false);
-  if (!b->np) return set_err(nullptr, MD_ERR_UNSUPPORTED, "kc too large for the packed k-space scatter");
+  if (any_simt && !b->np) return set_err(nullptr, MD_ERR_UNSUPPORTED, "kc too large for the packed k-space scatter");
   // task tables, one segment per kernel shape
   std::vector<Task> tasks;
   auto table = [&](Packed& pk, auto blocks_of) {
@@ -160,11 +191,22 @@ int pack(md_batch* b) {
   table(b->n256, [](md_ctx* c) { return cell_blocks((int)c->n); });
   table(b->sort, [](md_ctx* c) { return cell_sort_blocks(c->grid); });
   table(b->real, [](md_ctx* c) { return real_blocks((int)c->n); });
+  table(b->pass, [](md_ctx* c) { return real_pass_blocks((int)c->n); });
   table(b->phase, [](md_ctx* c) { return phase_blocks((int)c->n); });
-  table(b->sk, [](md_ctx* c) { return sk_blocks(k_params(c, nullptr, nullptr)); });
-  table(b->red, [](md_ctx* c) { return skred_blocks(k_params(c, nullptr, nullptr)); });
+  table(b->sk, [&](md_ctx* c) { return on_tc(c) ? 0 : sk_blocks(k_params(c, nullptr, nullptr)); });
+  table(b->red, [&](md_ctx* c) { return on_tc(c) ? 0 : skred_blocks(k_params(c, nullptr, nullptr)); });
   const int np = b->np;
-  table(b->sc, [np](md_ctx* c) { return scatter_blocks(k_params(c, nullptr, nullptr), np); });
+  table(b->sc, [&](md_ctx* c) { return on_tc(c) ? 0 : scatter_blocks(k_params(c, nullptr, nullptr), np); });
+  // tensor-core systems: the blocks of their grids, the structure factor
+  // with the batch chunking (batch_tc_shape)
+  table(b->tprep, [&](md_ctx* c) { return on_tc(c) ? c->tcs.nsb : 0; });
+  table(b->tsf, [&](md_ctx* c) {
+    if (!on_tc(c)) return 0;
+    const TcShape bt = batch_tc_shape(c);
+    return bt.mt * bt.nchunk;
+  });
+  table(b->tred, [&](md_ctx* c) { return on_tc(c) ? c->tcs.mt * (2 * (int)c->kc + 1) : 0; });
+  table(b->tsc, [&](md_ctx* c) { return on_tc(c) ? (int)((c->n + 127) / 128) : 0; });
   if (tasks.size() > b->task_cap) {
     if (b->d_tasks) cudaFree(b->d_tasks);
     b->d_tasks = nullptr;
@@ -174,18 +216,19 @@ int pack(md_batch* b) {
     if (e != cudaSuccess) return set_err(nullptr, MD_ERR_NOMEM, "task table: %s", cudaGetErrorString(e));
     b->task_cap = cap;
   }
-  for (Packed* pk : {&b->n256, &b->sort, &b->real, &b->phase, &b->sk, &b->red, &b->sc})
+  for (Packed* pk : {&b->n256, &b->sort, &b->real, &b->pass, &b->phase, &b->sk, &b->red, &b->sc, &b->tprep, &b->tsf,
+                     &b->tred, &b->tsc})
     pk->tasks = b->d_tasks + reinterpret_cast<size_t>(pk->tasks);
   if (!b->d_wq) {
-    cudaError_t e = cudaMalloc(&b->d_wq, sizeof(WorkQ) * 7);
-    if (e == cudaSuccess) e = cudaMemset(b->d_wq, 0, sizeof(WorkQ) * 7);
+    cudaError_t e = cudaMalloc(&b->d_wq, sizeof(WorkQ) * 8);
+    if (e == cudaSuccess) e = cudaMemset(b->d_wq, 0, sizeof(WorkQ) * 8);
     if (e != cudaSuccess) return set_err(nullptr, MD_ERR_NOMEM, "work queues: %s", cudaGetErrorString(e));
   }
   {
     // launches over one table run in stream order (never two at once), so a
     // queue per table suffices
     int q = 0;
-    for (Packed* pk : {&b->n256, &b->sort, &b->real, &b->phase, &b->sk, &b->red, &b->sc}) pk->wq = b->d_wq + q++;
+    for (Packed* pk : {&b->n256, &b->sort, &b->real, &b->pass, &b->phase, &b->sk, &b->red, &b->sc}) pk->wq = b->d_wq + q++;
   }
   int st;
   if ((st = upload(b->d_tasks, tasks, b->stream))) return st;
@@ -215,14 +258,17 @@ int pack(md_batch* b) {
   l += launch_cells_packed(s, b->d_cell, R, b->n256, b->sort);
   fork(0);
   l += launch_phase_tables_packed(k, b->d_kfull, b->phase);
+  l += launch_kspace_tc_prep_packed(k, b->d_kfull, b->tprep);
   l += launch_kspace_packed(k, b->d_kfull, b->sk, b->red, b->sc, true, b->kcmax, b->np);
+  l += launch_kspace_tc_packed(k, b->d_kfull, b->tsf, b->tred, b->tsc, true, b->tc_sf_smem, b->tc_sc_smem);
   l += launch_nbr_packed(s, b->d_rfull, R, b->real);
-  l += launch_real_packed(s, b->d_rfull, b->real, true, b->coat);
+  l += launch_real_packed(s, b->d_rfull, b->real, b->pass, true, b->coat);
   join(0);
   l += launch_heun1_packed(s, b->d_i1, b->n256);
   fork(1);
   l += launch_kspace_packed(k, b->d_kfield, b->sk, b->red, b->sc, false, b->kcmax, b->np);
-  l += launch_real_packed(s, b->d_rfield, b->real, false, false);
+  l += launch_kspace_tc_packed(k, b->d_kfield, b->tsf, b->tred, b->tsc, false, b->tc_sf_smem, b->tc_sc_smem);
+  l += launch_real_packed(s, b->d_rfield, b->real, b->pass, false, false);
   join(1);
   l += launch_heun2_packed(s, b->d_i2, b->n256);
   l += launch_obs_packed(s, b->d_obs, R);

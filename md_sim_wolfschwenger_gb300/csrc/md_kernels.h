@@ -27,6 +27,7 @@ int persistent_grid(const void* fn, int threads, size_t smem, int ntask);
 int cell_blocks(int n);                 // cell assign/scatter/fill, integrator
 int cell_sort_blocks(const CellGrid& g);
 int real_blocks(int n);                 // real space and neighbour list
+int real_pass_blocks(int n);            // real-space passes without coating (4-warp blocks)
 int phase_blocks(int n);
 int sk_blocks(const KParams& p);
 // Threads (segments) per structure-factor block, and how many such blocks
@@ -55,7 +56,9 @@ int launch_set_mu(cudaStream_t st, int n, const double* mm, const double* magMom
 
 // Real space: full (field + force + pressure + overlap) or field only.
 int launch_real(cudaStream_t st, const RealParams& p, bool full, bool fp64);
-int launch_real_packed(cudaStream_t st, const RealParams* ps, const Packed& real, bool full, bool coat);
+// pass: the 4-warp-block table (real_pass_blocks), used unless full && coat
+int launch_real_packed(cudaStream_t st, const RealParams* ps, const Packed& real, const Packed& pass, bool full,
+                       bool coat);
 
 // k space: structure factor partials, reduction, scatter (full or field only).
 // ev (optional): two events recorded after the structure factor and after
@@ -94,6 +97,14 @@ size_t kspace_tc_tblk_entries(int kc, int nsb);  // per-step Y, Z blocks (float2
 // Per-step operand images (after the phase tables), then per evaluation.
 int launch_kspace_tc_prep(cudaStream_t st, const KParams& p);
 int launch_kspace_tc(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* ev = nullptr);
+// Packed systems on the tensor cores: per-step operand prep (after the phase
+// tables), and structure factor + reduction + scatter of one evaluation;
+// task tables with one block per task, dynamic shared memory the largest of
+// the packed systems' (kspace_tc_sf_bytes, TcShape::scat_smem).
+size_t kspace_tc_sf_bytes(const TcShape& t, int kc);
+int launch_kspace_tc_prep_packed(cudaStream_t st, const KParams* ps, const Packed& prep);
+int launch_kspace_tc_packed(cudaStream_t st, const KParams* ps, const Packed& sf, const Packed& red,
+                            const Packed& sc, bool full, size_t sf_smem, size_t sc_smem);
 // One warp waits on an mbarrier that gets an arrival only when `arrive` is
 // set; a wait that gives up after `limit` cycles sets kErrTcWait in *err.
 int launch_tc_wait_probe(cudaStream_t st, int* err, int arrive, long long limit);

@@ -182,8 +182,7 @@ static size_t scat_smem(int kc, int nst, int /*rows*/, bool yz = false) {
 // 2q + 1 = (Im X, Re X) per particle (q = nx + kc; zero beyond 2 kc and
 // beyond n) as FP16 hi, lo tiles [ns][2 kSfSC]; Y(|ny|), Z(nz) of the stage's
 // particles.
-__global__ void __launch_bounds__(256) k_tc_prep(KParams p) {
-  const int sb = blockIdx.x;
+__device__ __forceinline__ void tc_prep_body(const KParams& p, int sb) {
   const int NS = p.tc_ns, kc = p.kc, K1 = kc + 1, n = p.n;
   const int j0 = sb * kSfSC;
   const float2* gtab = (const float2*)p.tab;
@@ -221,6 +220,13 @@ __global__ void __launch_bounds__(256) k_tc_prep(KParams p) {
   }
 }
 
+__global__ void __launch_bounds__(256) k_tc_prep(KParams p) { tc_prep_body(p, blockIdx.x); }
+// Packed systems: one block per task (system, stage block).
+__global__ void __launch_bounds__(256) k_tc_prep_packed(const KParams* __restrict__ ps, const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  tc_prep_body(ps[t.rep], t.blk);
+}
+
 // ------------------------------------------------------ structure factor
 
 // Roles (warps): 0-15 generate the U, V operand of a stage into a
@@ -229,7 +235,7 @@ __global__ void __launch_bounds__(256) k_tc_prep(KParams p) {
 // taking the stages s = i (mod kSfIssuers) into its own accumulator (several
 // issuing threads keep the tensor cores busy with these N <= 112 MMAs); the
 // accumulators are added in a fixed order at the end.
-__global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
+__device__ __forceinline__ void sf_tc_body(const KParams& p, int mtile, int chunk) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t full_bt[kSfMaxSlots];   // X tiles, tables, moments landed
   __shared__ __align__(8) uint64_t bt_empty[kSfMaxSlots];  // MMAs that read the copied slot are complete
@@ -239,7 +245,6 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
   __shared__ double red[3][kSfGenWarps];
-  const int mtile = blockIdx.x, chunk = blockIdx.y;
   const int NS = p.tc_ns, kc = p.kc, K1 = kc + 1, n = p.n;
   const SfLayout L(NS, K1, p.tc_sfa, p.tc_sfb);
   const int kSfA = L.na, kSfB = L.nb;
@@ -521,6 +526,16 @@ __global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) {
   if (warp == 0) tmem_free(tmem, ncols);
 }
 
+__global__ void __launch_bounds__(kSfThreads) k_sf_tc(KParams p) { sf_tc_body(p, blockIdx.x, blockIdx.y); }
+// Packed systems: one block per task (system, M tile + tc_mt x chunk).
+__global__ void __launch_bounds__(kSfThreads) k_sf_tc_packed(const KParams* __restrict__ ps,
+                                                            const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  const KParams& p = ps[t.rep];
+  const int mt = p.tc_mt;
+  sf_tc_body(p, t.blk % mt, t.blk / mt);
+}
+
 // One element of the scatter operand image: hi at [t][0], lo at [t][1].
 __device__ __forceinline__ void w_put(float* img, int kp, int row, int k, float x) {
   float h, l;
@@ -546,13 +561,13 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float v) {
 }
 
 template <bool FULL>
-__global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
+__device__ __forceinline__ void sf_reduce_body(const KParams& p, int bx) {
   using L = ScatLayout<FULL>;
   __shared__ double red[8][4][64];  // [group][4 values][row]
   const int Q = 2 * p.kc + 1;
-  const int mtile = blockIdx.x / Q, q = blockIdx.x - mtile * Q;
+  const int mtile = bx / Q, q = bx - mtile * Q;
   const int rl = threadIdx.x & 63, grp = threadIdx.x >> 6;
-  if (blockIdx.x == 0 && threadIdx.x < 3) {
+  if (bx == 0 && threadIdx.x < 3) {
     double s = 0;
     for (int c = 0; c < p.tc_nchunk; c++) s += p.musum_part[3 * c + threadIdx.x];
     p.musum[threadIdx.x] = s;
@@ -605,6 +620,18 @@ __global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
   }
 }
 
+template <bool FULL>
+__global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
+  sf_reduce_body<FULL>(p, blockIdx.x);
+}
+// Packed systems: one block per task (system, M tile x column).
+template <bool FULL>
+__global__ void __launch_bounds__(512) k_sf_tc_reduce_packed(const KParams* __restrict__ ps,
+                                                             const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  sf_reduce_body<FULL>(ps[t.rep], t.blk);
+}
+
 // ---------------------------------------------------------------- scatter
 
 // Roles (warps): 0-15 epilogue (warp w owns the tensor-memory lanes
@@ -616,7 +643,7 @@ __global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
 // (columns [0, 2 kp)), the accumulators at columns 256 and 384.  An
 // epilogue warp releases an accumulator as soon as it has loaded it.
 template <bool FULL>
-__global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
+__device__ __forceinline__ void kscat_body(const KParams& p, int bx) {
   using L = ScatLayout<FULL>;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t full_bar[kScMaxStages];  // W tile landed in a stage
@@ -637,7 +664,7 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
   const bool epi = warp < kScEpiWarps;
   const int quarter = warp & 3, cq = (warp >> 2) & 3;  // lane quarter, column quarter
   const int pl = 32 * quarter + lane;  // particle of this epilogue thread = tensor-memory lane
-  const int i = blockIdx.x * kScParticles + pl;
+  const int i = bx * kScParticles + pl;
   const bool act = epi && i < n;
   const int ii = i < n ? i : n - 1;
   const float2* gtab = (const float2*)p.tab;
@@ -879,6 +906,18 @@ __global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
   if (warp == 0) tmem_free(tmem, 512);
 }
 
+template <bool FULL>
+__global__ void __launch_bounds__(kScThreads) k_kscat_tc(KParams p) {
+  kscat_body<FULL>(p, blockIdx.x);
+}
+// Packed systems: one block per task (system, block of 128 particles).
+template <bool FULL>
+__global__ void __launch_bounds__(kScThreads) k_kscat_tc_packed(const KParams* __restrict__ ps,
+                                                                 const Task* __restrict__ tk) {
+  const Task t = tk[blockIdx.x];
+  kscat_body<FULL>(ps[t.rep], t.blk);
+}
+
 // ------------------------------------------------------------ host side
 
 static int rows_bound(int kc) { return (kc + 1) * (2 * kc + 1); }
@@ -954,6 +993,31 @@ size_t kspace_tc_tblk_entries(int kc, int nsb) { return (size_t)nsb * 2 * (kc + 
 int launch_kspace_tc_prep(cudaStream_t st, const KParams& p) {
   k_tc_prep<<<(p.n + kSfSC - 1) / kSfSC, 256, 0, st>>>(p);
   return 1;
+}
+
+size_t kspace_tc_sf_bytes(const TcShape& t, int kc) { return (size_t)SfLayout(t.ns, kc + 1, t.sfa, t.sfb).bytes; }
+
+int launch_kspace_tc_prep_packed(cudaStream_t st, const KParams* ps, const Packed& prep) {
+  if (!prep.n) return 0;
+  k_tc_prep_packed<<<prep.n, 256, 0, st>>>(ps, prep.tasks);
+  return 1;
+}
+
+int launch_kspace_tc_packed(cudaStream_t st, const KParams* ps, const Packed& sf, const Packed& red,
+                            const Packed& sc, bool full, size_t sf_smem, size_t sc_smem) {
+  if (!sf.n) return 0;
+  cudaFuncSetAttribute(k_sf_tc_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sf_smem);
+  k_sf_tc_packed<<<sf.n, kSfThreads, sf_smem, st>>>(ps, sf.tasks);
+  if (full) {
+    k_sf_tc_reduce_packed<true><<<red.n, 512, 0, st>>>(ps, red.tasks);
+    cudaFuncSetAttribute(k_kscat_tc_packed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem);
+    k_kscat_tc_packed<true><<<sc.n, kScThreads, sc_smem, st>>>(ps, sc.tasks);
+  } else {
+    k_sf_tc_reduce_packed<false><<<red.n, 512, 0, st>>>(ps, red.tasks);
+    cudaFuncSetAttribute(k_kscat_tc_packed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem);
+    k_kscat_tc_packed<false><<<sc.n, kScThreads, sc_smem, st>>>(ps, sc.tasks);
+  }
+  return 3;
 }
 
 int launch_kspace_tc(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* ev) {

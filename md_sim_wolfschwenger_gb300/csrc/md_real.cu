@@ -950,15 +950,19 @@ __global__ void __launch_bounds__(1024) k_nbr_scan_packed(const RealParams* __re
   const RealParams p = ps[blockIdx.x];
   nbr_scan(p);
 }
+// the block shape and occupancy of the single-system passes (k_real): 8
+// warps with coating in the field + force pass, otherwise 4 warps at 7
+// (field + force) or 9 (field) blocks per SM
 template <bool FULL, bool COAT>
-__global__ void __launch_bounds__(kRealWarps * 32, COAT ? 2 : 4) k_real_packed(const RealParams* __restrict__ ps,
-                                                                 const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+__global__ void __launch_bounds__(((FULL && COAT) ? kRealWarps : kFieldWarps) * 32, COAT ? 2 : (FULL ? 7 : 9))
+    k_real_packed(const RealParams* __restrict__ ps, const Task* __restrict__ tk, int ntask, WorkQ* wq) {
   for_tasks<false>(tk, ntask, wq, [&](const Task& t) {
-      real_eval<float, FULL, COAT>(ps[t.rep], t.blk);
+      real_eval<float, FULL, COAT, (FULL && COAT) ? kRealWarps : kFieldWarps>(ps[t.rep], t.blk);
   });
 }
 
 int real_blocks(int n) { return (n + kRealWarps - 1) / kRealWarps; }
+int real_pass_blocks(int n) { return (n + kFieldWarps - 1) / kFieldWarps; }
 
 int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64) {
   const int nsm = num_sms();
@@ -1008,16 +1012,18 @@ int launch_nbr_packed(cudaStream_t st, const RealParams* ps, int R, const Packed
   return 3;
 }
 
-int launch_real_packed(cudaStream_t st, const RealParams* ps, const Packed& real, bool full, bool coat) {
-  if (!real.n) return 0;
-  const int th = kRealWarps * 32;
-  auto go = [&](auto kern) {
-    kern<<<persistent_grid((const void*)kern, th, 0, real.n), th, 0, st>>>(ps, real.tasks, real.n, real.wq);
+int launch_real_packed(cudaStream_t st, const RealParams* ps, const Packed& real, const Packed& pass, bool full,
+                       bool coat) {
+  auto go = [&](auto kern, const Packed& tb, int th) {
+    kern<<<persistent_grid((const void*)kern, th, 0, tb.n), th, 0, st>>>(ps, tb.tasks, tb.n, tb.wq);
   };
-  if (full)
-    coat ? go(k_real_packed<true, true>) : go(k_real_packed<true, false>);
-  else
-    go(k_real_packed<false, false>);
+  if (full && coat) {
+    if (!real.n) return 0;
+    go(k_real_packed<true, true>, real, kRealWarps * 32);
+  } else {
+    if (!pass.n) return 0;
+    full ? go(k_real_packed<true, false>, pass, kFieldWarps * 32) : go(k_real_packed<false, false>, pass, kFieldWarps * 32);
+  }
   return 1;
 }
 

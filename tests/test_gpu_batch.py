@@ -107,7 +107,9 @@ def test_batch_info_and_launch_count():
     assert b.run(5) == 5
     nsys, npart, lps, ms = b.info()
     assert nsys == 3 and npart == sum(s[0] for s in SPECS[:3])
-    assert 10 <= lps <= 20   # one launch per kernel for all systems
+    # one launch per kernel for all systems: at most 28 with both k-space
+    # engines in the batch (CUDA-core and tensor-core systems)
+    assert 10 <= lps <= 28
     assert ms > 0
 
 
