@@ -52,8 +52,10 @@ struct md_batch {
   IntParams *d_i1 = nullptr, *d_i2 = nullptr;
   ObsParams* d_obs = nullptr;
   int* d_status = nullptr;
-  Task* d_tasks = nullptr;
+  Task* d_tasks = nullptr;  // task tables (expanded on the device from d_toff)
   size_t task_cap = 0;
+  int* d_toff = nullptr;    // per-system first-task offsets of every table
+  size_t toff_cap = 0;
   Packed n256{}, sort{}, real{}, pass{}, phase{}, sk{}, red{}, sc{};
   WorkQ* d_wq = nullptr;  // one work queue per task table (persistent packed launches)
   // systems whose k space runs on the tensor cores (the context's engine):
@@ -148,6 +150,23 @@ int upload_params(md_batch* b) {
   return MD_OK;
 }
 
+// Task tables on the device from the per-system offsets (off[r] .. off[r+1]
+// are system r's tasks): block (system, table) writes its system's entries.
+// The host uploads R + 1 offsets per table instead of one entry per block.
+constexpr int kMaxTables = 16;
+struct ExpandArgs {
+  int off_start[kMaxTables];  // first offset of each table in toff
+  int task_base[kMaxTables];  // first entry of each table in tasks
+};
+__global__ void __launch_bounds__(256) k_expand_tasks(const int* __restrict__ toff, Task* __restrict__ tasks,
+                                                      ExpandArgs a) {
+  const int t = blockIdx.y, r = blockIdx.x;
+  const int* off = toff + a.off_start[t];
+  const int q0 = off[r], q1 = off[r + 1];
+  Task* out = tasks + a.task_base[t];
+  for (int q = q0 + (int)threadIdx.x; q < q1; q += blockDim.x) out[q] = Task{r, q - q0};
+}
+
 // Task tables, parameters and the captured step for the current systems.
 int pack(md_batch* b) {
   drop_graph(b);
@@ -177,16 +196,29 @@ int pack(md_batch* b) {
   }
   b->np = scatter_particles(b->kcmax, false);
   if (any_simt && !b->np) return set_err(nullptr, MD_ERR_UNSUPPORTED, "kc too large for the packed k-space scatter");
-  // task tables, one segment per kernel shape
-  std::vector<Task> tasks;
+  // task tables, one per kernel shape: R + 1 offsets each on the host
+  std::vector<int> toff;
+  ExpandArgs ex{};
+  int ntab = 0;
+  size_t ntask = 0;
   auto table = [&](Packed& pk, auto blocks_of) {
-    const size_t start = tasks.size();
-    for (int r = 0; r < R; r++) {
-      const int nb = blocks_of(b->slots[b->order[r]].ctx);
-      for (int q = 0; q < nb; q++) tasks.push_back(Task{r, q});
+    if (ntab == kMaxTables) {  // a table beyond ExpandArgs' bounds: a build error, caught by every test
+      pk.n = 0;
+      pk.tasks = nullptr;
+      return;
     }
-    pk.n = (int)(tasks.size() - start);
-    pk.tasks = reinterpret_cast<const Task*>(start);  // offset until the upload
+    ex.off_start[ntab] = (int)toff.size();
+    ex.task_base[ntab] = (int)ntask;
+    ntab++;
+    int cnt = 0;
+    for (int r = 0; r < R; r++) {
+      toff.push_back(cnt);
+      cnt += blocks_of(b->slots[b->order[r]].ctx);
+    }
+    toff.push_back(cnt);
+    pk.n = cnt;
+    pk.tasks = reinterpret_cast<const Task*>(ntask);  // offset until the allocation
+    ntask += (size_t)cnt;
   };
   table(b->n256, [](md_ctx* c) { return cell_blocks((int)c->n); });
   table(b->sort, [](md_ctx* c) { return cell_sort_blocks(c->grid); });
@@ -207,11 +239,20 @@ int pack(md_batch* b) {
   });
   table(b->tred, [&](md_ctx* c) { return on_tc(c) ? c->tcs.mt * (2 * (int)c->kc + 1) : 0; });
   table(b->tsc, [&](md_ctx* c) { return on_tc(c) ? (int)((c->n + 127) / 128) : 0; });
-  if (tasks.size() > b->task_cap) {
+  if (toff.size() > b->toff_cap) {
+    if (b->d_toff) cudaFree(b->d_toff);
+    b->d_toff = nullptr;
+    b->toff_cap = 0;
+    const size_t cap = toff.size() + toff.size() / 4 + 256;
+    cudaError_t e = cudaMalloc(&b->d_toff, sizeof(int) * cap);
+    if (e != cudaSuccess) return set_err(nullptr, MD_ERR_NOMEM, "task offsets: %s", cudaGetErrorString(e));
+    b->toff_cap = cap;
+  }
+  if (ntask > b->task_cap) {
     if (b->d_tasks) cudaFree(b->d_tasks);
     b->d_tasks = nullptr;
     b->task_cap = 0;
-    const size_t cap = tasks.size() + tasks.size() / 4 + 1024;
+    const size_t cap = ntask + ntask / 4 + 1024;
     cudaError_t e = cudaMalloc(&b->d_tasks, sizeof(Task) * cap);
     if (e != cudaSuccess) return set_err(nullptr, MD_ERR_NOMEM, "task table: %s", cudaGetErrorString(e));
     b->task_cap = cap;
@@ -231,7 +272,12 @@ int pack(md_batch* b) {
     for (Packed* pk : {&b->n256, &b->sort, &b->real, &b->pass, &b->phase, &b->sk, &b->red, &b->sc}) pk->wq = b->d_wq + q++;
   }
   int st;
-  if ((st = upload(b->d_tasks, tasks, b->stream))) return st;
+  if ((st = upload(b->d_toff, toff, b->stream))) return st;
+  if (R > 0) {
+    k_expand_tasks<<<dim3(R, ntab), 256, 0, b->stream>>>(b->d_toff, b->d_tasks, ex);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "task tables: %s", cudaGetErrorString(e));
+  }
   if ((st = upload_params(b))) return st;
   if (R == 0) {
     b->packed = true;
@@ -380,7 +426,7 @@ int md_batch_destroy(md_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
   void* arrays[] = {b->d_cell, b->d_rfull, b->d_rfield, b->d_kfull, b->d_kfield, b->d_i1, b->d_i2, b->d_obs,
-                    b->d_status, b->d_tasks, b->d_wq};
+                    b->d_status, b->d_tasks, b->d_toff, b->d_wq};
   for (void* p : arrays)
     if (p) cudaFree(p);
   if (b->ev0) cudaEventDestroy(b->ev0);
