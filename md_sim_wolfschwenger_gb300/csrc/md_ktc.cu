@@ -545,8 +545,11 @@ __device__ __forceinline__ void w_put(float* img, int kp, int row, int k, float 
   img[kScCols * kp + o] = l;
 }
 
-// Block per (M tile, column q): 64 rows x 8 groups of chunks, the groups
-// combined in a fixed order.  The chunk partials (FP32 tensor-memory sums of
+// Block per (M tile, column q): 64 rows x G groups of chunks, the groups
+// combined in a fixed order.  A single system (its chunks fill the GPU, 64 at
+// N = 32768) takes 8 groups; packed batches take 2 (blocks of 128 threads, 16
+// resident per SM: a small system has few chunks, which would leave most
+// threads of a wider block idle, and a batch runs thousands of these blocks).  The chunk partials (FP32 tensor-memory sums of
 // <= 512 particles) are added exactly: within a group with error-free FP32
 // transformations (TwoSum: the running sum and its exact rounding errors;
 // GB300's FP64 rate is a small fraction of FP32, so a conversion and an FP64
@@ -560,10 +563,12 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float v) {
   s = t;
 }
 
-template <bool FULL>
+constexpr int kRedGroups = 8, kRedGroupsPacked = 2;
+
+template <bool FULL, int G>
 __device__ __forceinline__ void sf_reduce_body(const KParams& p, int bx) {
   using L = ScatLayout<FULL>;
-  __shared__ double red[8][4][64];  // [group][4 values][row]
+  __shared__ double red[G][4][64];  // [group][4 values][row]
   const int Q = 2 * p.kc + 1;
   const int mtile = bx / Q, q = bx - mtile * Q;
   const int rl = threadIdx.x & 63, grp = threadIdx.x >> 6;
@@ -577,7 +582,7 @@ __device__ __forceinline__ void sf_reduce_body(const KParams& p, int bx) {
   const float* b = p.tc_part + (size_t)mtile * NS * 128;
   float su[4] = {0.f, 0.f, 0.f, 0.f}, cu[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 4
-  for (int c = grp; c < p.tc_nchunk; c += 8) {
+  for (int c = grp; c < p.tc_nchunk; c += G) {
     const float* bc = b + (size_t)c * cstride;
     two_sum_acc(su[0], cu[0], bc[(2 * q) * 128 + rl]);
     two_sum_acc(su[1], cu[1], bc[(2 * q + 1) * 128 + rl]);
@@ -590,9 +595,9 @@ __device__ __forceinline__ void sf_reduce_body(const KParams& p, int bx) {
   if (grp != 0) return;
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-  for (int g8 = 0; g8 < 8; g8++)
+  for (int g = 0; g < G; g++)
 #pragma unroll
-    for (int v = 0; v < 4; v++) acc[v] += red[g8][v][rl];
+    for (int v = 0; v < 4; v++) acc[v] += red[g][v][rl];
   const int r = mtile * 64 + rl;
   if (r >= p.tc_rows) return;
   const int kk = p.tc_kmap[r * Q + q];
@@ -621,15 +626,15 @@ __device__ __forceinline__ void sf_reduce_body(const KParams& p, int bx) {
 }
 
 template <bool FULL>
-__global__ void __launch_bounds__(512) k_sf_tc_reduce(KParams p) {
-  sf_reduce_body<FULL>(p, blockIdx.x);
+__global__ void __launch_bounds__(64 * kRedGroups) k_sf_tc_reduce(KParams p) {
+  sf_reduce_body<FULL, kRedGroups>(p, blockIdx.x);
 }
 // Packed systems: one block per task (system, M tile x column).
 template <bool FULL>
-__global__ void __launch_bounds__(512) k_sf_tc_reduce_packed(const KParams* __restrict__ ps,
-                                                             const Task* __restrict__ tk) {
+__global__ void __launch_bounds__(64 * kRedGroupsPacked) k_sf_tc_reduce_packed(const KParams* __restrict__ ps,
+                                                                             const Task* __restrict__ tk) {
   const Task t = tk[blockIdx.x];
-  sf_reduce_body<FULL>(ps[t.rep], t.blk);
+  sf_reduce_body<FULL, kRedGroupsPacked>(ps[t.rep], t.blk);
 }
 
 // ---------------------------------------------------------------- scatter
@@ -1009,11 +1014,11 @@ int launch_kspace_tc_packed(cudaStream_t st, const KParams* ps, const Packed& sf
   cudaFuncSetAttribute(k_sf_tc_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sf_smem);
   k_sf_tc_packed<<<sf.n, kSfThreads, sf_smem, st>>>(ps, sf.tasks);
   if (full) {
-    k_sf_tc_reduce_packed<true><<<red.n, 512, 0, st>>>(ps, red.tasks);
+    k_sf_tc_reduce_packed<true><<<red.n, 64 * kRedGroupsPacked, 0, st>>>(ps, red.tasks);
     cudaFuncSetAttribute(k_kscat_tc_packed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem);
     k_kscat_tc_packed<true><<<sc.n, kScThreads, sc_smem, st>>>(ps, sc.tasks);
   } else {
-    k_sf_tc_reduce_packed<false><<<red.n, 512, 0, st>>>(ps, red.tasks);
+    k_sf_tc_reduce_packed<false><<<red.n, 64 * kRedGroupsPacked, 0, st>>>(ps, red.tasks);
     cudaFuncSetAttribute(k_kscat_tc_packed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem);
     k_kscat_tc_packed<false><<<sc.n, kScThreads, sc_smem, st>>>(ps, sc.tasks);
   }
@@ -1027,9 +1032,9 @@ int launch_kspace_tc(cudaStream_t st, const KParams& p, bool full, cudaEvent_t* 
   if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
   const int nred = p.tc_mt * (2 * p.kc + 1);
   if (full)
-    k_sf_tc_reduce<true><<<nred, 512, 0, st>>>(p);
+    k_sf_tc_reduce<true><<<nred, 64 * kRedGroups, 0, st>>>(p);
   else
-    k_sf_tc_reduce<false><<<nred, 512, 0, st>>>(p);
+    k_sf_tc_reduce<false><<<nred, 64 * kRedGroups, 0, st>>>(p);
   if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
   const size_t sm2 = (size_t)p.tc_scat_smem;
   const int nb = (p.n + kScParticles - 1) / kScParticles;
