@@ -56,12 +56,34 @@ int set_err(md_ctx* c, int status, const char* fmt, ...) {
 }
 
 
+// Device memory of a context comes from the device's default memory pool,
+// ordered on the context's stream: freeing (cudaFreeAsync) does not wait for
+// the whole GPU as cudaFree does, so contexts that finish while a batch runs
+// cost the request loop little, and their memory serves the next contexts.
+// The pool keeps freed memory for reuse (release threshold raised once per
+// device) instead of returning it to the driver at every synchronisation.
+void pool_keep(int device) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lk(mu);
+  if (std::find(done.begin(), done.end(), device) != done.end()) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done.push_back(device);
+}
+
 int dalloc_raw(md_ctx* c, void** p, size_t bytes) {
   void* q = nullptr;
   if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMalloc(&q, bytes);
+  cudaError_t e = cudaMallocAsync(&q, bytes, c->stream);
+  // the allocation is complete before any stream, or a synchronous copy,
+  // touches it
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess)
-    return set_err(c, MD_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    return set_err(c, MD_ERR_NOMEM, "device allocation (%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
   c->allocs.push_back(q);
   c->alloc_bytes.push_back(bytes);
   c->bytes += (int64_t)bytes;
@@ -78,7 +100,7 @@ void dfree(md_ctx* c, void* p) {
     c->alloc_bytes.erase(c->alloc_bytes.begin() + (ptrdiff_t)k);
     c->allocs.erase(it);
   }
-  cudaFree(p);
+  cudaFreeAsync(p, c->stream);  // after the context's queued work (its side stream joins it)
 }
 
 bool fp64(const md_ctx* c) { return c->prec == MD_PREC_FP64; }
@@ -714,6 +736,7 @@ int md_ctx_create(const md_config* cfg, int64_t n, int precision, md_ctx** out) 
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess)
     return fail(set_err(nullptr, MD_ERR_CUDA, "cudaStreamCreate failed"));
+  pool_keep(c->device);
   for (int q = 0; q < 2; q++)
     if (cudaEventCreateWithFlags(&c->fork_ev[q], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->join_ev[q], cudaEventDisableTiming) != cudaSuccess)
@@ -768,7 +791,8 @@ int md_ctx_destroy(md_ctx* c) {
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   if (c->side) cudaStreamSynchronize(c->side);
-  for (void* p : c->allocs) cudaFree(p);
+  for (void* p : c->allocs) cudaFreeAsync(p, c->stream);
+  if (c->stream) cudaStreamSynchronize(c->stream);
   c->allocs.clear();
   c->alloc_bytes.clear();
   for (int q = 0; q < 2; q++) {
