@@ -58,6 +58,7 @@ struct md_batch {
   size_t toff_cap = 0;
   Packed n256{}, sort{}, real{}, pass{}, phase{}, sk{}, red{}, sc{};
   WorkQ* d_wq = nullptr;  // one work queue per task table (persistent packed launches)
+  unsigned* d_anyrb = nullptr;  // some system rebuilds its lists this step (zeroed)
   // systems whose k space runs on the tensor cores (the context's engine):
   // operand prep, structure factor, reduction and scatter tables, and the
   // largest dynamic shared memory among them; the others take sk, red, sc
@@ -263,6 +264,8 @@ int pack(md_batch* b) {
   if (!b->d_wq) {
     cudaError_t e = cudaMalloc(&b->d_wq, sizeof(WorkQ) * 8);
     if (e == cudaSuccess) e = cudaMemset(b->d_wq, 0, sizeof(WorkQ) * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_anyrb, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(b->d_anyrb, 0, sizeof(unsigned));
     if (e != cudaSuccess) return set_err(nullptr, MD_ERR_NOMEM, "work queues: %s", cudaGetErrorString(e));
   }
   {
@@ -300,14 +303,14 @@ int pack(md_batch* b) {
     cudaEventRecord(b->join_ev[q], k);
     cudaStreamWaitEvent(s, b->join_ev[q], 0);
   };
-  l += launch_step_begin_packed(s, b->d_cell, R);
-  l += launch_cells_packed(s, b->d_cell, R, b->n256, b->sort);
+  l += launch_step_begin_packed(s, b->d_cell, R, b->d_anyrb);
+  l += launch_cells_packed(s, b->d_cell, R, b->n256, b->sort, b->d_anyrb);
   fork(0);
   l += launch_phase_tables_packed(k, b->d_kfull, b->phase);
   l += launch_kspace_tc_prep_packed(k, b->d_kfull, b->tprep);
   l += launch_kspace_packed(k, b->d_kfull, b->sk, b->red, b->sc, true, b->kcmax, b->np);
   l += launch_kspace_tc_packed(k, b->d_kfull, b->tsf, b->tred, b->tsc, true, b->tc_sf_smem, b->tc_sc_smem);
-  l += launch_nbr_packed(s, b->d_rfull, R, b->real);
+  l += launch_nbr_packed(s, b->d_rfull, R, b->real, b->d_anyrb);
   l += launch_real_packed(s, b->d_rfull, b->real, b->pass, true, b->coat);
   join(0);
   l += launch_heun1_packed(s, b->d_i1, b->n256);
@@ -317,7 +320,7 @@ int pack(md_batch* b) {
   l += launch_real_packed(s, b->d_rfield, b->real, b->pass, false, false);
   join(1);
   l += launch_heun2_packed(s, b->d_i2, b->n256);
-  l += launch_obs_packed(s, b->d_obs, R);
+  l += launch_obs_packed(s, b->d_obs, R, b->d_anyrb);
   e = cudaStreamEndCapture(s, &b->graph);
   if (e != cudaSuccess) return set_err(nullptr, MD_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
   e = cudaGraphInstantiate(&b->gexec, b->graph, 0);
@@ -426,7 +429,7 @@ int md_batch_destroy(md_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
   void* arrays[] = {b->d_cell, b->d_rfull, b->d_rfield, b->d_kfull, b->d_kfield, b->d_i1, b->d_i2, b->d_obs,
-                    b->d_status, b->d_tasks, b->d_toff, b->d_wq};
+                    b->d_status, b->d_tasks, b->d_toff, b->d_wq, b->d_anyrb};
   for (void* p : arrays)
     if (p) cudaFree(p);
   if (b->ev0) cudaEventDestroy(b->ev0);

@@ -208,15 +208,24 @@ __global__ void __launch_bounds__(kCellThreads) k_sorted_fill(CellParams p) {
 
 // ---------------------------------------------------------------- packed
 
-__global__ void k_step_begin_packed(const CellParams* __restrict__ ps, int R) {
+// anyrb: raised when some system of the batch rebuilds its cell and
+// neighbour lists this step; the packed list kernels return at once while it
+// is clear (most steps), instead of claiming every task to find its system
+// skips the work.  The step's last kernel clears it (k_obs_packed).
+__global__ void k_step_begin_packed(const CellParams* __restrict__ ps, int R, unsigned* anyrb) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < R) step_begin(ps[r].flags, ps[r].half_skin);
+  if (r < R) {
+    step_begin(ps[r].flags, ps[r].half_skin);
+    if (ps[r].flags->rebuild) atomicOr(anyrb, 1u);
+  }
 }
 // Packed kernels are persistent: their blocks stride over the task table,
 // finishing one task before the next (the barrier keeps a task's shared
 // memory until every thread of the block is done with it).
 __global__ void __launch_bounds__(kCellThreads) k_cell_assign_packed(const CellParams* __restrict__ ps,
-                                                                     const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+                                                                     const Task* __restrict__ tk, int ntask, WorkQ* wq,
+                                                                     const unsigned* anyrb) {
+  if (!__ldcg(anyrb)) return;  // the whole grid: no system rebuilds this step
   for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
       cell_assign(ps[t.rep], t.blk);
   });
@@ -226,13 +235,17 @@ __global__ void __launch_bounds__(1024) k_cell_scan_packed(const CellParams* __r
   cell_scan(p);
 }
 __global__ void __launch_bounds__(kCellThreads) k_cell_scatter_packed(const CellParams* __restrict__ ps,
-                                                                      const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+                                                                      const Task* __restrict__ tk, int ntask, WorkQ* wq,
+    const unsigned* anyrb) {
+  if (!__ldcg(anyrb)) return;
   for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
       cell_scatter(ps[t.rep], t.blk);
   });
 }
 __global__ void __launch_bounds__(kCellThreads) k_cell_sort_packed(const CellParams* __restrict__ ps,
-                                                                   const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+                                                                   const Task* __restrict__ tk, int ntask, WorkQ* wq,
+    const unsigned* anyrb) {
+  if (!__ldcg(anyrb)) return;
   for_tasks<true>(tk, ntask, wq, [&](const Task& t) {
       cell_sort(ps[t.rep], t.blk);
   });
@@ -339,25 +352,26 @@ int launch_cells(cudaStream_t st, const CellParams& p, bool fp64) {
   return launches + 1;
 }
 
-int launch_step_begin_packed(cudaStream_t st, const CellParams* ps, int R) {
-  k_step_begin_packed<<<(R + 127) / 128, 128, 0, st>>>(ps, R);
+int launch_step_begin_packed(cudaStream_t st, const CellParams* ps, int R, unsigned* anyrb) {
+  k_step_begin_packed<<<(R + 127) / 128, 128, 0, st>>>(ps, R, anyrb);
   return 1;
 }
 
-int launch_cells_packed(cudaStream_t st, const CellParams* ps, int R, const Packed& n256, const Packed& sort) {
+int launch_cells_packed(cudaStream_t st, const CellParams* ps, int R, const Packed& n256, const Packed& sort,
+                        const unsigned* anyrb) {
   int l = 0;
   if (n256.n) {
-    k_cell_assign_packed<<<persistent_grid((const void*)k_cell_assign_packed, kCellThreads, 0, n256.n), kCellThreads, 0, st>>>(ps, n256.tasks, n256.n, n256.wq);
+    k_cell_assign_packed<<<persistent_grid((const void*)k_cell_assign_packed, kCellThreads, 0, n256.n), kCellThreads, 0, st>>>(ps, n256.tasks, n256.n, n256.wq, anyrb);
     l++;
   }
   k_cell_scan_packed<<<R, 1024, 0, st>>>(ps);
   l++;
   if (n256.n) {
-    k_cell_scatter_packed<<<persistent_grid((const void*)k_cell_scatter_packed, kCellThreads, 0, n256.n), kCellThreads, 0, st>>>(ps, n256.tasks, n256.n, n256.wq);
+    k_cell_scatter_packed<<<persistent_grid((const void*)k_cell_scatter_packed, kCellThreads, 0, n256.n), kCellThreads, 0, st>>>(ps, n256.tasks, n256.n, n256.wq, anyrb);
     l++;
   }
   if (sort.n) {
-    k_cell_sort_packed<<<persistent_grid((const void*)k_cell_sort_packed, kCellThreads, 0, sort.n), kCellThreads, 0, st>>>(ps, sort.tasks, sort.n, sort.wq);
+    k_cell_sort_packed<<<persistent_grid((const void*)k_cell_sort_packed, kCellThreads, 0, sort.n), kCellThreads, 0, st>>>(ps, sort.tasks, sort.n, sort.wq, anyrb);
     l++;
   }
   if (n256.n) {

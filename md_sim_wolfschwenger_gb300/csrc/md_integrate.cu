@@ -410,9 +410,12 @@ __global__ void __launch_bounds__(kIntThreads, 4) k_heun2_packed(const IntParams
       heun2<float>(ps[t.rep], t.blk);
   });
 }
-__global__ void __launch_bounds__(256) k_obs_packed(const ObsParams* __restrict__ ps) {
+// The step's last packed kernel: it also clears the batch's rebuild word
+// (raised by k_step_begin_packed; every reader of it ran earlier in the step).
+__global__ void __launch_bounds__(256) k_obs_packed(const ObsParams* __restrict__ ps, unsigned* anyrb) {
   const ObsParams p = ps[blockIdx.x];
   obs(p);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *anyrb = 0u;
 }
 
 // B and F in SI, particle order; optional overlap push of the positions
@@ -658,9 +661,9 @@ int launch_heun2_packed(cudaStream_t st, const IntParams* ps, const Packed& n256
   return 1;
 }
 
-int launch_obs_packed(cudaStream_t st, const ObsParams* ps, int R) {
+int launch_obs_packed(cudaStream_t st, const ObsParams* ps, int R, unsigned* anyrb) {
   if (!R) return 0;
-  k_obs_packed<<<R, 256, 0, st>>>(ps);
+  k_obs_packed<<<R, 256, 0, st>>>(ps, anyrb);
   return 1;
 }
 

@@ -42,15 +42,18 @@ int int_blocks_one(int n);        // single-system Heun launches (128-thread blo
 // Step start: decides whether this step rebuilds the cell order and the
 // neighbour list (host request, or a particle moved more than half_skin).
 int launch_step_begin(cudaStream_t st, StepFlags* flags, double half_skin);
-int launch_step_begin_packed(cudaStream_t st, const CellParams* ps, int R);
+// anyrb: the batch's word "some system rebuilds its lists this step" (set here,
+// read by the packed list kernels, cleared by launch_obs_packed's kernel)
+int launch_step_begin_packed(cudaStream_t st, const CellParams* ps, int R, unsigned* anyrb);
 // Raises the displacement since the last build after new positions arrived.
 int launch_disp_check(cudaStream_t st, int n, const double* pos, const double* xbuild, double L, StepFlags* flags);
 // Cell order (skipped unless the step rebuilds) and the sorted views.
 int launch_cells(cudaStream_t st, const CellParams& p, bool fp64);
-int launch_cells_packed(cudaStream_t st, const CellParams* ps, int R, const Packed& n256, const Packed& sort);
+int launch_cells_packed(cudaStream_t st, const CellParams* ps, int R, const Packed& n256, const Packed& sort,
+                        const unsigned* anyrb);
 // Neighbour list within rc + skin (count, scan, fill; skipped unless rebuilding).
 int launch_nbr(cudaStream_t st, const RealParams& p, StepFlags* flags, bool fp64);
-int launch_nbr_packed(cudaStream_t st, const RealParams* ps, int R, const Packed& real);
+int launch_nbr_packed(cudaStream_t st, const RealParams* ps, int R, const Packed& real, const unsigned* anyrb);
 int launch_set_mu(cudaStream_t st, int n, const double* mm, const double* magMom_u, const double* rMag_u,
                   const SortedView& s, bool fp64);
 
@@ -125,7 +128,7 @@ int launch_obs(cudaStream_t st, const ObsParams& p);
 int launch_heun2_obs(cudaStream_t st, const IntParams& p, const ObsParams& o, unsigned* done, bool fp64);
 int launch_heun1_packed(cudaStream_t st, const IntParams* ps, const Packed& n256);
 int launch_heun2_packed(cudaStream_t st, const IntParams* ps, const Packed& n256);
-int launch_obs_packed(cudaStream_t st, const ObsParams* ps, int R);
+int launch_obs_packed(cudaStream_t st, const ObsParams* ps, int R, unsigned* anyrb);
 // B, F in SI (orig order, double) from the stage outputs; optional overlap push.
 // Real-space field and force alone of the last full evaluation (test hook).
 int launch_real_part(cudaStream_t st, const IntParams& p, double* Bout, double* Fout, bool fp64);

@@ -941,7 +941,9 @@ __global__ void __launch_bounds__(((FULL && COAT) ? kRealWarps : kFieldWarps) * 
 // list build and the pair loop are warp-private (no block barrier)
 template <bool FILL>
 __global__ void __launch_bounds__(kRealWarps * 32) k_nbr_build_packed(const RealParams* __restrict__ ps,
-                                                                      const Task* __restrict__ tk, int ntask, WorkQ* wq) {
+                                                                      const Task* __restrict__ tk, int ntask, WorkQ* wq,
+                                                                      const unsigned* anyrb) {
+  if (!__ldcg(anyrb)) return;  // the whole grid: no system rebuilds this step
   for_tasks<false>(tk, ntask, wq, [&](const Task& t) {
       nbr_build<float, FILL>(ps[t.rep], t.blk);
   });
@@ -1000,15 +1002,15 @@ int launch_real(cudaStream_t st, const RealParams& p, bool full, bool fp64) {
   return 1;
 }
 
-int launch_nbr_packed(cudaStream_t st, const RealParams* ps, int R, const Packed& real) {
+int launch_nbr_packed(cudaStream_t st, const RealParams* ps, int R, const Packed& real, const unsigned* anyrb) {
   const int th = kRealWarps * 32;
   if (real.n)
     k_nbr_build_packed<false><<<persistent_grid((const void*)k_nbr_build_packed<false>, th, 0, real.n), th, 0, st>>>(
-        ps, real.tasks, real.n, real.wq);
+        ps, real.tasks, real.n, real.wq, anyrb);
   k_nbr_scan_packed<<<R, 1024, 0, st>>>(ps);
   if (real.n)
     k_nbr_build_packed<true><<<persistent_grid((const void*)k_nbr_build_packed<true>, th, 0, real.n), th, 0, st>>>(
-        ps, real.tasks, real.n, real.wq);
+        ps, real.tasks, real.n, real.wq, anyrb);
   return 3;
 }
 
