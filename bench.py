@@ -359,7 +359,54 @@ def fp64_plain(n, sysd, ewald, seed, steps=4, warm=1):
             "mixed_error_vs_fp64": err}
 
 
-def stress_sample(steps, warm=3, fp64_steps=2, seed=1):
+def segment_rooflines(seg_mean, n, kc, pairs, nk_real, tensor_cores, peak_fp32, hbm_peak):
+    """Per-segment achieved rates of a profiled pass (ms per kernel segment):
+    algorithmic FLOPs or bytes per unit (the constants above) over the
+    segment's time, against the FP32 FMA-chain peak, the HBM copy peak or the
+    measured tensor rate; returns the segments and their work table."""
+    work = {"real_full": ("fp32", pairs * FLOPS_PAIR_FULL), "real_field": ("fp32", pairs * FLOPS_PAIR_FIELD),
+            "ksf_full": ("fp32", nk_real * n * FLOPS_KSF), "ksf_field": ("fp32", nk_real * n * FLOPS_KSF),
+            "kscat_full": ("fp32", nk_real * n * FLOPS_KSCAT_FULL),
+            "kscat_field": ("fp32", nk_real * n * FLOPS_KSCAT_FIELD),
+            "cells": ("hbm", n * BYTES_CELLS), "heun1": ("hbm", n * BYTES_HEUN1), "heun2": ("hbm", n * BYTES_HEUN2)}
+    peak_tf32 = peak_f16 = None
+    if tensor_cores:
+        # the tensor-core k space: the structure factor's executed 3-pass FP16
+        # MMA work against the measured bf16 rate (the same rate), the
+        # scatter's 3-pass TF32 work against half of it (nominal 1:2)
+        sf_fl, scf_fl, scd_fl = tc_mma_flops(n, kc)
+        work.update(ksf_full=("tensor16", sf_fl), ksf_field=("tensor16", sf_fl), kscat_full=("tensor", scf_fl),
+                    kscat_field=("tensor", scd_fl))
+        try:
+            peak_f16 = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]
+        except Exception:
+            peak_f16 = 1900.0
+        peak_tf32 = peak_f16 / 2
+    segs = {}
+    for k, ms in seg_mean.items():
+        ent = {"ms": ms}
+        if k in work and ms > 0:
+            kind, amount = work[k]
+            if kind == "fp32":
+                ach = amount / (ms * 1e-3) / 1e12
+                ent.update(bound="fp32", achieved=ach, unit="TFLOP/s", peak=peak_fp32, frac=ach / peak_fp32)
+            elif kind == "tensor":
+                ach = amount / (ms * 1e-3) / 1e12
+                ent.update(bound="tensor", achieved=ach, unit="TFLOP/s", peak=peak_tf32, frac=ach / peak_tf32,
+                           note="3-pass TF32 MMAs executed (padding included); peak = measured bf16 / 2")
+            elif kind == "tensor16":
+                ach = amount / (ms * 1e-3) / 1e12
+                ent.update(bound="tensor", achieved=ach, unit="TFLOP/s", peak=peak_f16, frac=ach / peak_f16,
+                           note="3-pass FP16 MMAs executed (padding included); peak = measured bf16 (same rate)")
+            else:
+                ach = amount / (ms * 1e-3) / 1e9
+                ent.update(bound="hbm", achieved=ach, unit="GB/s", peak=hbm_peak,
+                           frac=(ach / hbm_peak) if hbm_peak else None)
+        segs[k] = ent
+    return segs, work
+
+
+def stress_sample(steps, peak_fp32, hbm_peak, warm=3, fp64_steps=2, seed=1):
     """The stress instance (N = 131072, log-normal sigma 0.25, volume fraction
     0.20, 30 mT): mixed particle-steps/s from CUDA events around `steps`
     graph replays, the plain FP64 path on the same system and Ewald
@@ -393,8 +440,29 @@ def stress_sample(steps, warm=3, fp64_steps=2, seed=1):
         if prec == MD_PREC_MIXED:
             extra = {"pairs": sim.pairs(), "strong_pair_entries_fp64": sim.strong_pairs(),
                      "kspace_tensor_cores": sim.kspace_tensor_cores()}
+            # per-kernel segments: a profiled pass (kernels one after another)
+            sim.profile(True)
+            sim.step(1, 1e-12)
+            acc = None
+            for _ in range(3):
+                sim.step(1, 1e-12)
+                sg = sim.profile_read()
+                acc = sg if acc is None else {a: acc[a] + b for a, b in sg.items()}
+            sim.profile(False)
+            seg_mean = {a: b / 3 for a, b in acc.items()}
+            segs, _ = segment_rooflines(seg_mean, n, kc, extra["pairs"], len(sim.debug_structure_factor()),
+                                        sim.kspace_tensor_cores(), peak_fp32, hbm_peak)
+            kspace = [q for q in seg_mean if q.startswith("k")]
+            extra_segs = {"segments": segs,
+                          "kspace_share_of_serialised_step": sum(seg_mean[q] for q in kspace) / sum(seg_mean.values()),
+                          "fp64_accumulation_ms": seg_mean.get("kred_full", 0.0) + seg_mean.get("kred_field", 0.0),
+                          "fp64_accumulation_note": "the structure factor's exact chunk sums (TwoSum FP32 pairs, "
+                                                    "then FP64), S and e S in FP64 and the scatter operand image: "
+                                                    "the reduction segments, ms per step"}
         sim.close()
         out[prec] = (ms, k, extra)
+        if prec == MD_PREC_MIXED:
+            out["segs"] = extra_segs
     err, _ = workloads.mixed_vs_fp64(cfg, rMag, rHydr, pos, mm, ea, (alpha, rc, kc))
     ms, k, extra = out[MD_PREC_MIXED]
     ms64, k64, _ = out[MD_PREC_FP64]
@@ -406,6 +474,7 @@ def stress_sample(steps, warm=3, fp64_steps=2, seed=1):
                            "steps": k64},
             "mixed_over_fp64_plain": ms64 / ms,
             "mixed_error_vs_fp64": err,
+            **out["segs"],
             "note": "graph replays back to back (no L2 flush; the working set exceeds the 129 MB L2); torque "
                     "error is the FP32 k-space floor for a moment ratio of ~700 (below the parameters' own "
                     "Ewald truncation error pred_torque_err_rel_contact)"}
@@ -646,44 +715,7 @@ def run_ours(args):
         hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
     except Exception:
         pass
-    work = {"real_full": ("fp32", pairs * FLOPS_PAIR_FULL), "real_field": ("fp32", pairs * FLOPS_PAIR_FIELD),
-            "ksf_full": ("fp32", nk_real * n * FLOPS_KSF), "ksf_field": ("fp32", nk_real * n * FLOPS_KSF),
-            "kscat_full": ("fp32", nk_real * n * FLOPS_KSCAT_FULL),
-            "kscat_field": ("fp32", nk_real * n * FLOPS_KSCAT_FIELD),
-            "cells": ("hbm", n * BYTES_CELLS), "heun1": ("hbm", n * BYTES_HEUN1), "heun2": ("hbm", n * BYTES_HEUN2)}
-    peak_tf32 = peak_f16 = None
-    if sim.kspace_tensor_cores():
-        # the tensor-core k space: executed 3-pass TF32 MMA work against the
-        # TF32 dense rate, half the measured bf16 rate (nominal 1:2)
-        sf_fl, scf_fl, scd_fl = tc_mma_flops(n, kc)
-        work.update(ksf_full=("tensor16", sf_fl), ksf_field=("tensor16", sf_fl), kscat_full=("tensor", scf_fl),
-                    kscat_field=("tensor", scd_fl))
-        try:
-            peak_f16 = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]
-        except Exception:
-            peak_f16 = 1900.0
-        peak_tf32 = peak_f16 / 2
-    segs = {}
-    for k, ms in seg_mean.items():
-        ent = {"ms": ms}
-        if k in work and ms > 0:
-            kind, amount = work[k]
-            if kind == "fp32":
-                ach = amount / (ms * 1e-3) / 1e12
-                ent.update(bound="fp32", achieved=ach, unit="TFLOP/s", peak=peak_fp32, frac=ach / peak_fp32)
-            elif kind == "tensor":
-                ach = amount / (ms * 1e-3) / 1e12
-                ent.update(bound="tensor", achieved=ach, unit="TFLOP/s", peak=peak_tf32, frac=ach / peak_tf32,
-                           note="3-pass TF32 MMAs executed (padding included); peak = measured bf16 / 2")
-            elif kind == "tensor16":
-                ach = amount / (ms * 1e-3) / 1e12
-                ent.update(bound="tensor", achieved=ach, unit="TFLOP/s", peak=peak_f16, frac=ach / peak_f16,
-                           note="3-pass FP16 MMAs executed (padding included); peak = measured bf16 (same rate)")
-            else:
-                ach = amount / (ms * 1e-3) / 1e9
-                ent.update(bound="hbm", achieved=ach, unit="GB/s", peak=hbm_peak,
-                           frac=(ach / hbm_peak) if hbm_peak else None)
-        segs[k] = ent
+    segs, work = segment_rooflines(seg_mean, n, kc, pairs, nk_real, sim.kspace_tensor_cores(), peak_fp32, hbm_peak)
     dom = max((k for k in segs if k in work), key=lambda k: segs[k]["ms"])
     traffic = None  # from the ncu capture of this workload, when there is one
     try:
@@ -712,7 +744,7 @@ def run_ours(args):
         if not args.no_fp64:
             fp64 = fp64_plain(n, sysd, (alpha, rc, kc), seed)
         if args.stress_steps > 0 and args.workload == "large":
-            stress = stress_sample(args.stress_steps)
+            stress = stress_sample(args.stress_steps, peak_fp32, hbm_peak)
         if args.sweep_replicas > 0:
             sweep = sweep_sample(args.sweep_replicas, args.sweep_steps)
         if args.serve_requests > 0:
