@@ -451,7 +451,8 @@ typedef struct md_serve_stats {
   double wall;            /* s from start to the last completion              */
   double particle_steps;  /* sum over requests of n * steps                   */
   double gpu_ms;          /* GPU time of all packed rounds (CUDA events)      */
-  double admit_ms;        /* host time spent admitting (init, upload, setup)  */
+  double admit_ms;        /* host time creating contexts (upload, setup), on
+                             the admitting thread, overlapping the rounds      */
   int64_t rounds, repacks, peak_systems;
   double peak_bytes;
 } md_serve_stats;
@@ -460,9 +461,9 @@ typedef struct md_serve_stats {
  * arrival order as device memory (hbm_budget) and batch slots free up; each
  * admitted request becomes a system (md_init_system with base's keys and the
  * request's n, volFrac, field and seed; Ewald parameters for
- * base.errTolEwald) that joins the packed batch at the next round, while the
- * current round runs on the GPU.  Finished systems leave the batch and free
- * their memory.  results[i] belongs to reqs[i]. */
+ * base.errTolEwald) that joins the packed batch at the next round; a second
+ * host thread admits while this one keeps the rounds going.  Finished systems
+ * leave the batch and free their memory.  results[i] belongs to reqs[i]. */
 int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, const md_serve_opts* opts,
                  md_request_result* results, md_serve_stats* stats);
 

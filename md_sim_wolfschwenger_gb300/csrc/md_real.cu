@@ -907,12 +907,13 @@ __device__ __forceinline__ void real_eval(const RealParams& p, int bx) {
 }
 
 static int num_sms() {
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
+  // initialised once (thread-safe: contexts may be created on several threads)
+  static const int nsm = [] {
+    int dev = 0, k = 0;
     cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
-  }
+    if (cudaDeviceGetAttribute(&k, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || k <= 0) k = 148;
+    return k;
+  }();
   return nsm;
 }
 

@@ -4,23 +4,27 @@
 // systems).  Host code only; every device operation goes through the
 // library's own C ABI (md_ctx_*, md_batch_*).
 //
-// Loop (md_serve_run):
-//   1. while the current packed round runs on the GPU, admit arrived
-//      requests in arrival order: build the system on the host, create its
-//      context, upload the state, choose the Ewald parameters -- as long as
-//      the admitted systems stay inside the memory budget and batch slots.
-//      The host-side systems of the next arrived requests (sizes, placement,
-//      Ewald parameters) are prepared ahead on worker threads;
-//   2. wait for the round; systems that have run all their steps are read
-//      back (final m_z, state checksum), leave the batch and free memory;
-//   3. the newly admitted systems join the batch (it re-packs its launches)
-//      and the next round starts.
+// Loop (md_serve_run), two threads:
+//   admitting thread: in arrival order, as batch slots and the memory budget
+//      allow, build each request's system on the host (prepared ahead on
+//      worker threads: sizes, placement, Ewald parameters), create its
+//      context, upload the state, set the Ewald parameters, and hand the
+//      context over;
+//   this thread: wait for the round in flight; systems that have run all
+//      their steps are read back (final m_z, state checksum), leave the batch
+//      and free their memory; the contexts handed over join the batch (it
+//      re-packs its launches) and the next round starts.
 // A round runs at most round_steps steps and ends early when a system
-// finishes, so no system runs past its own step count.
+// finishes, so no system runs past its own step count.  Creating a context
+// costs milliseconds (and waits on the busy GPU in places): on the loop's own
+// thread it delayed the next round whenever several requests arrived at once.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <deque>
 #include <future>
+#include <mutex>
 #include <map>
 #include <string>
 #include <thread>
@@ -191,61 +195,60 @@ int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, co
 
   const Clock::time_point t0 = Clock::now();
   auto now = [&] { return std::chrono::duration<double>(Clock::now() - t0).count(); };
-  std::vector<Live> live, staged;
-  HostSys pend;  // the next request's host system, kept while it waits for memory
-  // host systems prepared ahead on worker threads, by request index
-  using Prep = std::pair<int, HostSys>;
-  std::map<int64_t, std::future<Prep>> ahead;
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const size_t nahead = std::min<size_t>(16, std::max<size_t>(1, hw / 2));
-  auto prepare_async = [&](int64_t qi) {
-    ahead.emplace(qi, std::async(std::launch::async, [base, reqs, qi]() {
-      Prep r;
-      r.first = prepare_host(*base, reqs[qi], qi, &r.second);
-      return r;
-    }));
-  };
-  size_t next = 0;
-  int64_t completed = 0;
+
+  // State shared by the admitting thread and this one (under mu): the
+  // contexts created and not yet finished hold `used` bytes and `held` batch
+  // slots; `ready` hands created contexts over in arrival order.
+  std::mutex mu;
+  std::condition_variable cv_admit, cv_loop;
+  std::deque<Live> ready;
   double used = 0;
-  bool in_flight = false;
-  int fatal = MD_OK;
+  int64_t held = 0, completed = 0;
+  bool stop = false;
+  double admit_s = 0;
 
-  auto finish_request = [&](Live& s, int status) {
-    md_request_result* r = &results[s.req];
-    if (status == MD_OK)
-      harvest(s, reqs[s.req], r);  // sets the status of the read-back
-    else
-      r->status = status;
-    r->finished = now();
-    r->latency = r->finished - reqs[s.req].arrival;
-    r->device_bytes = s.bytes;
-    md_ctx_destroy(s.ctx);
-    used -= (double)s.bytes;
-    completed++;
-  };
-
-  while (completed < nreq && !fatal) {
-    // 1. admission (overlaps the round in flight)
-    nvtxRangePushA("admission");
-    const double ta = now();
-    for (size_t k = next; k < order.size() && k < next + nahead; k++) {
-      const int64_t qi = order[k];
-      if (opts->realtime && reqs[qi].arrival > now()) break;
-      if ((int64_t)qi != pend.req && !ahead.count(qi)) prepare_async(qi);
-    }
-    while (next < order.size() && (int64_t)(live.size() + staged.size()) < opts->max_systems) {
+  // Admission on its own thread: host systems (prepared ahead on worker
+  // threads), contexts, state upload and Ewald parameters, in arrival order,
+  // while this thread keeps the packed rounds going (creating a context costs
+  // milliseconds and waits on the busy GPU in places; on the loop's thread it
+  // delayed the next round whenever several requests arrived together).
+  std::thread admitter([&] {
+    using Prep = std::pair<int, HostSys>;
+    std::map<int64_t, std::future<Prep>> ahead;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nahead = std::min<size_t>(16, std::max<size_t>(1, hw / 2));
+    HostSys pend;  // the next request's host system, kept while it waits for memory
+    auto reject = [&](int64_t qi, int as) {  // this request cannot run: report it
+      std::lock_guard<std::mutex> lk(mu);
+      results[qi].status = as;
+      results[qi].finished = now();
+      results[qi].latency = results[qi].finished - reqs[qi].arrival;
+      completed++;
+      cv_loop.notify_all();
+    };
+    for (size_t next = 0; next < order.size();) {
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        if (stop) break;
+      }
       const int64_t qi = order[next];
       const md_request& q = reqs[qi];
-      if (opts->realtime && q.arrival > now()) break;
-      auto reject = [&](int as) {  // this request cannot run: report it
-        results[qi].status = as;
-        results[qi].finished = now();
-        results[qi].latency = results[qi].finished - q.arrival;
-        completed++;
-        next++;
-        pend = HostSys();
-      };
+      if (opts->realtime && q.arrival > now()) {  // wait for the arrival (or the end)
+        std::unique_lock<std::mutex> lk(mu);
+        cv_admit.wait_for(lk, std::chrono::duration<double>(std::min(q.arrival - now(), 0.05)), [&] { return stop; });
+        if (stop) break;
+        continue;
+      }
+      for (size_t k = next; k < order.size() && k < next + nahead; k++) {
+        const int64_t qk = order[k];
+        if (opts->realtime && reqs[qk].arrival > now()) break;
+        if (qk != pend.req && !ahead.count(qk))
+          ahead.emplace(qk, std::async(std::launch::async, [base, reqs, qk]() {
+            Prep r;
+            r.first = prepare_host(*base, reqs[qk], qk, &r.second);
+            return r;
+          }));
+      }
       if (pend.req != qi) {
         pend = HostSys();
         int hs;
@@ -259,35 +262,96 @@ int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, co
           hs = prepare_host(*base, q, qi, &pend);
         }
         if (hs) {
-          reject(hs);
+          reject(qi, hs);
+          pend = HostSys();
+          next++;
           continue;
         }
       }
-      const bool alone = live.empty() && staged.empty();
-      if (used + pend.est > opts->hbm_budget && !alone) break;  // wait until memory frees up
-      Live s{qi, nullptr, 0, 0, 0};
-      const int as = create_device(pend, q, opts->autotune, &s);
+      bool alone;
+      {  // a batch slot and room in the budget (a request that would run alone always tries)
+        std::unique_lock<std::mutex> lk(mu);
+        cv_admit.wait(lk, [&] {
+          return stop || (held < opts->max_systems && (used + pend.est <= opts->hbm_budget || held == 0));
+        });
+        if (stop) break;
+        alone = held == 0;
+      }
+      Live sys{qi, nullptr, 0, 0, 0};
+      const double ta = now();
+      const int as = create_device(pend, q, opts->autotune, &sys);
+      admit_s += now() - ta;
       if (as) {
-        reject(as);
+        reject(qi, as);
+        pend = HostSys();
+        next++;
         continue;
       }
-      if (used + (double)s.bytes > opts->hbm_budget) {  // the estimate was low: the actual bytes decide
-        md_ctx_destroy(s.ctx);
-        if (alone) {
-          reject(set_err(nullptr, MD_ERR_NOMEM, "request %lld needs more than the memory budget", (long long)qi));
+      bool wait_memory = false;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        if (used + (double)sys.bytes > opts->hbm_budget && !(alone && held == 0)) {
+          wait_memory = true;  // the estimate was low: the actual bytes decide
+        } else if (used + (double)sys.bytes > opts->hbm_budget) {
+          wait_memory = false;
+        } else {
+          results[qi].admitted = now();
+          used += (double)sys.bytes;
+          held++;
+          S.peak_bytes = std::max(S.peak_bytes, used);
+          ready.push_back(sys);
+          cv_loop.notify_all();
+          pend = HostSys();
+          next++;
           continue;
         }
-        break;
       }
-      pend = HostSys();
-      results[qi].admitted = now();
-      used += (double)s.bytes;
-      S.peak_bytes = std::max(S.peak_bytes, used);
-      staged.push_back(s);
-      next++;
+      md_ctx_destroy(sys.ctx);
+      if (!wait_memory) {  // alone and still over the budget
+        reject(qi, set_err(nullptr, MD_ERR_NOMEM, "request %lld needs more than the memory budget", (long long)qi));
+        pend = HostSys();
+        next++;
+        continue;
+      }
+      {  // wait until a finished system frees memory, then create it again
+        std::unique_lock<std::mutex> lk(mu);
+        const double u0 = used;
+        const int64_t h0 = held;
+        cv_admit.wait(lk, [&] { return stop || used < u0 || held < h0; });
+        if (stop) break;
+      }
     }
-    S.admit_ms += 1e3 * (now() - ta);
-    nvtxRangePop();
+  });
+
+  std::vector<Live> live, staged;
+  bool in_flight = false;
+  int fatal = MD_OK;
+  auto finish_request = [&](Live& s, int status) {
+    md_request_result* r = &results[s.req];
+    if (status == MD_OK)
+      harvest(s, reqs[s.req], r);  // sets the status of the read-back
+    else
+      r->status = status;
+    r->finished = now();
+    r->latency = r->finished - reqs[s.req].arrival;
+    r->device_bytes = s.bytes;
+    md_ctx_destroy(s.ctx);
+    std::lock_guard<std::mutex> lk(mu);
+    used -= (double)s.bytes;
+    held--;
+    completed++;
+    cv_admit.notify_all();
+  };
+
+  for (;;) {
+    {  // 1. contexts the admitting thread has created join at the next round
+      std::lock_guard<std::mutex> lk(mu);
+      if (completed >= nreq && !in_flight) break;
+      while (!ready.empty()) {
+        staged.push_back(ready.front());
+        ready.pop_front();
+      }
+    }
     // 2. the round in flight
     if (in_flight) {
       const int ws = md_batch_wait(b);
@@ -309,7 +373,10 @@ int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, co
           k++;
         }
       }
-      if (ws != MD_OK && ws != MD_ERR_NONFINITE) fatal = ws;
+      if (ws != MD_OK && ws != MD_ERR_NONFINITE) {
+        fatal = ws;
+        break;
+      }
     }
     // 3. newly admitted systems join
     if (!staged.empty()) S.repacks++;
@@ -323,8 +390,8 @@ int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, co
     }
     staged.clear();
     S.peak_systems = std::max<int64_t>(S.peak_systems, (int64_t)live.size());
-    // 4. next round, or wait for the next arrival
-    if (!live.empty() && !fatal) {
+    // 4. the next round, or wait for the next admission
+    if (!live.empty()) {
       int64_t k = 0;
       const int ls = md_batch_launch(b, opts->round_steps, &k);
       if (ls) {
@@ -332,16 +399,24 @@ int md_serve_run(const md_config* base, const md_request* reqs, int64_t nreq, co
         break;
       }
       in_flight = k > 0;
-    } else if (next < order.size() && opts->realtime) {
-      const double wait = reqs[order[next]].arrival - now();
-      if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.05)));
+    } else {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_loop.wait_for(lk, std::chrono::milliseconds(50), [&] { return !ready.empty() || completed >= nreq; });
     }
   }
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    stop = true;
+    cv_admit.notify_all();
+  }
+  admitter.join();
   if (in_flight) md_batch_wait(b);
   for (Live& s : live) finish_request(s, fatal ? fatal : MD_ERR_INVALID);
   for (Live& s : staged) finish_request(s, fatal ? fatal : MD_ERR_INVALID);
+  for (Live& s : ready) finish_request(s, fatal ? fatal : MD_ERR_INVALID);
   md_batch_destroy(b);
   S.wall = now();
+  S.admit_ms = 1e3 * admit_s;
   for (int64_t i = 0; i < nreq; i++)
     if (results[i].status == MD_OK) S.particle_steps += (double)reqs[i].n * (double)reqs[i].steps;
   if (stats) *stats = S;

@@ -174,13 +174,15 @@ def test_serve_respects_memory_budget():
     for q in reqs:
         q["arrival"] = 0.0
     res, st = m.serve(cfg, reqs, hbm_budget=40e9, max_systems=16, round_steps=8, realtime=False)
+    assert all(r["status"] == 0 for r in res)
     held = [r["device_bytes"] for r in res]
-    assert st["peak_systems"] == len(reqs)
+    assert st["peak_bytes"] <= 40e9
+    # a budget below what all six hold together: admission must hold some back
     budget = max(1.05 * max(held), 0.5 * sum(held))
+    assert budget < sum(held)
     res2, st2 = m.serve(cfg, reqs, hbm_budget=budget, max_systems=16, round_steps=8, realtime=False)
     assert all(r["status"] == 0 for r in res2)
     assert st2["peak_bytes"] <= budget
-    assert st2["peak_systems"] < len(reqs)   # the budget held some back
     assert [r["checksum"] for r in res2] == [r["checksum"] for r in res]
 
 
