@@ -371,6 +371,23 @@ int md_calibrate_fp32(double* tflops);
 int md_init_system(const md_config* cfg, int64_t n, uint64_t seed, double* rMag, double* rHydr, double* pos,
                    double* mm, double* ea, double* lBox);
 
+/* Initial positions on the GPU (the calling thread's device) by random
+ * sequential addition, the placement of InitCoordsFromSketch
+ * (src/simulation.cpp:241-264) with its box-interior draw and overlap rule
+ * (plain distance below the sum of the hydrodynamic radii): in placement order
+ * (largest_first = 0: index order, as the reference; 1: decreasing radius,
+ * for dense polydisperse systems) each particle takes the first attempt that
+ * overlaps no particle placed before it.  Attempt t of particle i is drawn
+ * from Philox4x32-10 with counters {i, t} (the reference draws all attempts
+ * from one generator), so the parallel placement equals the sequential rule
+ * exactly.  pos: 3 x n column-major, box centred at 0.  MD_ERR_INVALID when
+ * a particle finds no place in 1e5 attempts or all particles together need
+ * more than 100 n + 1e6 (volume fraction too high for random addition);
+ * MD_ERR_UNSUPPORTED when more than 64 particles fall into one cell of its
+ * search grid (cells span the largest contact distance, 2N cells at most: an
+ * extremely wide size distribution). */
+int md_place_rsa(int64_t n, double lBox, const double* rHydr, uint64_t seed, int largest_first, double* pos);
+
 /* Ewald cutoff tuned per (N, volume fraction) bucket: the first system of a
  * bucket runs md_autotune_ewald (timed field evaluations over candidate
  * cutoffs, each with alpha and kc from the error model); later systems of the

@@ -143,6 +143,7 @@ def lib():
         "md_profile_read": (C.c_int, [V, P]),
         "md_calibrate_fp32": (C.c_int, [P]),
         "md_init_system": (C.c_int, [C.POINTER(MdConfig), I64, C.c_uint64, P, P, P, P, P, P]),
+        "md_place_rsa": (C.c_int, [I64, C.c_double, P, C.c_uint64, C.c_int, P]),
         "md_autotune_ewald_cached": (C.c_int, [V, C.c_double, P, P, PI64, C.POINTER(C.c_int)]),
         "md_tune_cache_save": (C.c_int, [C.c_char_p]),
         "md_tune_cache_load": (C.c_int, [C.c_char_p]),

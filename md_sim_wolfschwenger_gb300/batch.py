@@ -31,6 +31,16 @@ def init_system(config: Configuration, n: int, seed: int):
     return rMag, rHydr, pos, mm, ea, L.value
 
 
+def place_rsa(rHydr, lBox: float, seed: int, largest_first: bool = False):
+    """(3, N) positions by random sequential addition on the GPU
+    (md_place_rsa): index order as the reference (or largest radius first),
+    a Philox stream per particle."""
+    rH = np.ascontiguousarray(rHydr, dtype=np.float64)
+    pos = np.empty((3, len(rH)))
+    check(lib().md_place_rsa(len(rH), float(lBox), _P(rH), int(seed), int(bool(largest_first)), _P(pos)))
+    return pos
+
+
 def autotune_ewald_cached(sim: Simulation, volFrac: float):
     """Ewald parameters from the per-(N, volume fraction) tuning cache:
     (alpha, rc, kc, hit)."""

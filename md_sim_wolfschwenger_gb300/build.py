@@ -21,7 +21,8 @@ LIB = os.path.join(OUT, "libmd_gb300.so")
 EXE = os.path.join(OUT, "md_run")
 
 CUDA_SOURCES = ["md_cells.cu", "md_real.cu", "md_kspace.cu", "md_integrate.cu", "md_ctx.cu", "md_batch.cu",
-                "md_noalloc.cu", "md_post.cu", "md_ktc.cu"]
+                "md_noalloc.cu", "md_post.cu", "md_ktc.cu",
+                "md_place.cu"]
 HOST_SOURCES = ["md_host.cpp", "md_serve.cpp", "md_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC,

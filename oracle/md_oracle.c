@@ -1093,6 +1093,59 @@ static uint64_t sm64(uint64_t* x) {
 }
 static double sm64_unit(uint64_t* x) { return (double)(sm64(x) >> 11) * (1.0 / 9007199254740992.0); }
 
+/* Placement by random sequential addition with a stream per particle (the
+ * restatement the GPU placement md_place_rsa is checked against bit for bit):
+ * the particles in `order` (NULL: index order, as the reference) each take
+ * the first attempt t = 0, 1, ... whose position overlaps no particle placed
+ * before it -- distance below the sum of the hydrodynamic radii, plain
+ * distance inside the box as in the reference's InitCoordsFromSketch
+ * (src/simulation.cpp:241-264).  Attempt t of particle i: Philox4x32-10 with
+ * key {seed_lo, seed_hi} and counters {i, t_lo, t_hi, 0xA5A5A5A5},
+ * {i, t_lo, t_hi, 0x5A5A5A5A}; uniforms u = ((w_a << 21) ^ (w_b >> 11)) 2^-53
+ * from the word pairs (0,1), (2,3) of the first and (0,1) of the second;
+ * coordinate (2u - 1)(L/2 - r_i), the reference's box-interior draw.  The
+ * build turns floating-point contraction off, so the distance test rounds
+ * like the GPU's.  tries (optional) gets each particle's accepted attempt. */
+static void rsa_cand(uint64_t seed, int64_t i, int64_t t, double ext, double x[3]) {
+  uint32_t a[4] = {(uint32_t)i, (uint32_t)t, (uint32_t)((uint64_t)t >> 32), 0xA5A5A5A5u};
+  uint32_t b[4] = {(uint32_t)i, (uint32_t)t, (uint32_t)((uint64_t)t >> 32), 0x5A5A5A5Au};
+  philox4x32_10(a, (uint32_t)seed, (uint32_t)(seed >> 32));
+  philox4x32_10(b, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const uint32_t w[6] = {a[0], a[1], a[2], a[3], b[0], b[1]};
+  for (int c = 0; c < 3; c++) {
+    const uint64_t m = ((uint64_t)w[2 * c] << 21) ^ (uint64_t)(w[2 * c + 1] >> 11);
+    const double u = (double)m * 1.1102230246251565e-16; /* 2^-53 */
+    x[c] = (2.0 * u - 1.0) * ext;
+  }
+}
+
+int orc_rsa_philox(int64_t n, double lBox, const double* rHydr, uint64_t seed, const int64_t* order,
+                   int64_t max_tries, double* pos, int64_t* tries) {
+  for (int64_t q = 0; q < n; q++) {
+    const int64_t i = order ? order[q] : q;
+    const double ri = rHydr[i], ext = 0.5 * lBox - ri;
+    int placed = 0;
+    for (int64_t t = 0; t < max_tries && !placed; t++) {
+      double x[3];
+      rsa_cand(seed, i, t, ext, x);
+      placed = 1;
+      for (int64_t p = 0; p < q && placed; p++) {
+        const int64_t j = order ? order[p] : p;
+        const double dx = AX(pos, j, 0, n) - x[0], dy = AX(pos, j, 1, n) - x[1], dz = AX(pos, j, 2, n) - x[2];
+        const double s = ri + rHydr[j];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < s * s) placed = 0;
+      }
+      if (placed) {
+        for (int c = 0; c < 3; c++) AX(pos, i, c, n) = x[c];
+        if (tries) tries[i] = t;
+      }
+    }
+    if (!placed) return 1;
+  }
+  return 0;
+}
+
 int orc_rsa(int64_t n, double lBox, const double* rHydr, uint64_t seed, int64_t max_tries, double* pos) {
   uint64_t st = seed;
   double L = lBox;

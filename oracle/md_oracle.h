@@ -108,6 +108,10 @@ int orc_set_threads(orc_ctx* c, int t);
 /* Random sequential addition in index order (InitCoordsFromSketch,
  * simulation.cpp:241-264) with a seeded splitmix64 generator. */
 int orc_rsa(int64_t n, double lBox, const double* rHydr, uint64_t seed, int64_t max_tries, double* pos);
+/* Random sequential addition with a Philox stream per particle (the GPU
+ * placement's restatement; order NULL: index order). */
+int orc_rsa_philox(int64_t n, double lBox, const double* rHydr, uint64_t seed, const int64_t* order,
+                   int64_t max_tries, double* pos, int64_t* tries);
 double orc_last_seconds(const orc_ctx* c);
 
 #ifdef __cplusplus

@@ -32,7 +32,8 @@ def build(force=False) -> str:
                 os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "md_oracle.h"))):
             os.makedirs(BUILD, exist_ok=True)
             tmp = LIB + f".{os.getpid()}.tmp"
-            subprocess.check_call(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-pthread", "-o", tmp, src, "-lm"])
+            subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-std=c11", "-fPIC", "-shared", "-pthread", "-o", tmp, src,
+                                   "-lm"])
             os.replace(tmp, LIB)
     return LIB
 
@@ -87,6 +88,8 @@ def lib():
         L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.orc_rsa.restype = C.c_int
         L.orc_rsa.argtypes = [C.c_int64, C.c_double, P, C.c_uint64, C.c_int64, P]
+        L.orc_rsa_philox.restype = C.c_int
+        L.orc_rsa_philox.argtypes = [C.c_int64, C.c_double, P, C.c_uint64, C.c_void_p, C.c_int64, P, C.c_void_p]
         _lib = L
     return _lib
 
@@ -371,6 +374,22 @@ def rsa_fast(n, lBox, rHydr, seed, max_tries=100000):
     if lib().orc_rsa(n, lBox, _p(rH), int(seed), int(max_tries), _p(pos)) != 0:
         raise RuntimeError("random sequential addition failed: volume fraction too high")
     return pos
+
+
+def rsa_philox(n, lBox, rHydr, seed, order=None, max_tries=2000000):
+    """(3, N) positions and each particle's accepted attempt: random
+    sequential addition with a Philox stream per particle (orc_rsa_philox, the
+    restatement of the GPU placement md_place_rsa); order: placement order
+    (None: index order, as the reference)."""
+    rH = np.ascontiguousarray(rHydr, dtype=np.float64)
+    pos = np.zeros((3, n))
+    tries = np.zeros(n, dtype=np.int64)
+    o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    st = lib().orc_rsa_philox(n, lBox, _p(rH), int(seed), None if o is None else o.ctypes.data_as(C.c_void_p),
+                              int(max_tries), _p(pos), tries.ctypes.data_as(C.c_void_p))
+    if st != 0:
+        raise RuntimeError("random sequential addition failed: volume fraction too high")
+    return pos, tries
 
 
 def cost_model_rc(d, rMag, rHydr, lBox, kc_tc=25):

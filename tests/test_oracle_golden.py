@@ -108,3 +108,23 @@ def test_oracle_matches_reference_adaptive(name):
         np.testing.assert_allclose(obs[:2], g["ref_obs"][s][:2], rtol=1e-11, atol=1e-15)
     # the cases exercise rejections
     assert np.any(g["ref_dtUsed"] != g["ref_dt0"])
+
+
+def test_rsa_philox_restatement_properties():
+    """The placement restatement (orc_rsa_philox): inside the box, no
+    overlaps, deterministic, and the largest-first order places the same
+    particles differently but validly."""
+    rng = np.random.default_rng(3)
+    n = 400
+    rH = 15e-9 * np.exp(0.25 * rng.standard_normal(n))
+    L = float((np.sum(4.0 / 3.0 * np.pi * rH ** 3) / 0.2) ** (1.0 / 3.0))
+    for order in (None, np.argsort(-rH, kind="stable")):
+        pos, tries = O.rsa_philox(n, L, rH, 9, order=order)
+        pos2, _ = O.rsa_philox(n, L, rH, 9, order=order)
+        assert np.array_equal(pos, pos2)
+        assert np.all(np.abs(pos) <= L / 2 - rH[None, :])
+        d = np.linalg.norm(pos[:, :, None] - pos[:, None, :], axis=0)
+        s = rH[:, None] + rH[None, :]
+        np.fill_diagonal(d, np.inf)
+        assert np.all(d >= s)
+        assert tries.min() >= 0
