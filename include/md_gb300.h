@@ -248,7 +248,11 @@ int md_step(md_ctx* ctx, int64_t nsteps, double dt, const double* xi);
  * dt) with the context's drawn noise (Philox or off; MD_NOISE_UPLOADED is
  * MD_ERR_INVALID), md_state_download(pos_out, mm_out, ea_out).  For a caller
  * that keeps the state on the host between steps, as the reference's own
- * loop does (src/simulation.cpp:469-518); pinned host buffers copy fastest. */
+ * loop does (src/simulation.cpp:469-518).  Page-locked host buffers
+ * (cudaHostAlloc, cudaHostRegister, a pinned framework tensor) are read and
+ * written by kernels through their device mapping (on GB300 over
+ * NVLink-C2C), which saves the copies' overhead; other host memory goes
+ * through cudaMemcpyAsync.  md_state_upload does the same for its input. */
 int md_step_io(md_ctx* ctx, const double* pos, const double* mm, const double* ea, int64_t nsteps, double dt,
                double* pos_out, double* mm_out, double* ea_out);
 /* RunSimulation's loop with the adaptive solvers of IntegrationRot

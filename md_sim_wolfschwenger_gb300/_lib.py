@@ -122,7 +122,8 @@ def lib():
         "md_compute_field": (C.c_int, [V, P, P]),
         "md_set_noise": (C.c_int, [V, C.c_int, C.c_uint64]),
         "md_step": (C.c_int, [V, I64, C.c_double, P]),
-        "md_step_io": (C.c_int, [V, P, P, P, I64, C.c_double, P, P, P]),
+        # the state arrays as plain addresses (the per-step call is kept lean)
+        "md_step_io": (C.c_int, [V, V, V, V, I64, C.c_double, V, V, V]),
         "md_step_adaptive": (C.c_int, [V, I64, C.c_double, P, P, PI64]),
         "md_records": (C.c_int, [V, I64, I64, P]),
         "md_num_records": (C.c_int, [V, PI64]),

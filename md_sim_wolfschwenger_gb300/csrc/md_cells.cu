@@ -320,7 +320,62 @@ __global__ void k_disp_check(int n, const double* __restrict__ pos, const double
   if ((threadIdx.x & 31) == 0 && d > 0.f) atomicMax(&f->maxdisp, __float_as_uint(d));
 }
 
+// md_step_io with host buffers that the device addresses directly
+// (page-locked and mapped; on GB300 over NVLink-C2C): the state comes in
+// through one kernel that also does k_disp_check's test (xbuild null: no
+// list to test against), and goes out through one kernel, instead of three
+// copies each way and a separate check.
+__global__ void k_state_in(int n, const double* __restrict__ hpos, const double* __restrict__ hmm,
+                           const double* __restrict__ hea, double* __restrict__ pos, double* __restrict__ mm,
+                           double* __restrict__ ea, const double* __restrict__ xbuild, double L, StepFlags* f) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double d2 = 0;
+  if (i < n)
+    for (int a = 0; a < 3; a++) {
+      const size_t q = (size_t)a * n + i;
+      const double x = hpos[q];
+      pos[q] = x;
+      mm[q] = hmm[q];
+      ea[q] = hea[q];
+      if (xbuild) {
+        double d = x - xbuild[q];
+        d -= L * round(d / L);
+        d2 += d * d;
+      }
+    }
+  if (!xbuild) return;  // uniform over the grid
+  float d = (float)(sqrt(d2) / L);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_xor_sync(kFull, d, o));
+  if ((threadIdx.x & 31) == 0 && d > 0.f) atomicMax(&f->maxdisp, __float_as_uint(d));
+}
+
+__global__ void k_state_out(int n, const double* __restrict__ pos, const double* __restrict__ mm,
+                            const double* __restrict__ ea, double* __restrict__ hpos, double* __restrict__ hmm,
+                            double* __restrict__ hea) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int a = 0; a < 3; a++) {
+    const size_t q = (size_t)a * n + i;
+    hpos[q] = pos[q];
+    hmm[q] = mm[q];
+    hea[q] = ea[q];
+  }
+}
+
 // ------------------------------------------------------------- launchers
+
+int launch_state_in(cudaStream_t st, int n, const double* hpos, const double* hmm, const double* hea, double* pos,
+                    double* mm, double* ea, const double* xbuild, double L, StepFlags* flags) {
+  k_state_in<<<(n + 255) / 256, 256, 0, st>>>(n, hpos, hmm, hea, pos, mm, ea, xbuild, L, flags);
+  return 1;
+}
+
+int launch_state_out(cudaStream_t st, int n, const double* pos, const double* mm, const double* ea, double* hpos,
+                     double* hmm, double* hea) {
+  k_state_out<<<(n + 255) / 256, 256, 0, st>>>(n, pos, mm, ea, hpos, hmm, hea);
+  return 1;
+}
 
 int cell_blocks(int n) { return (n + kCellThreads - 1) / kCellThreads; }
 int cell_sort_blocks(const CellGrid& g) { return g.ncx == 1 ? 0 : (g.ncell * 32 + kCellThreads - 1) / kCellThreads; }

@@ -865,19 +865,40 @@ int md_set_box(md_ctx* c, double lBox) {
   return MD_OK;
 }
 
-// The copies and checks of md_state_upload, queued on the stream.
+// Device-side address of a host buffer that kernels may read and write
+// directly (page-locked memory mapped into the device's address space),
+// else null (pageable memory: copied by the copy engines).
+static double* mapped_addr(const double* h) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();  // not a CUDA allocation: no sticky error
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? (double*)a.devicePointer : nullptr;
+}
+
+// The copies and checks of md_state_upload, queued on the stream.  Mapped
+// host buffers come in through one kernel that also does the displacement
+// check; others through three copies and the check's own launch.
 static int enqueue_upload(md_ctx* c, const double* pos, const double* mm, const double* ea, int reset) {
   const size_t B = 24 * (size_t)c->n;
-  CK(c, cudaMemcpyAsync(c->pos, pos, B, cudaMemcpyHostToDevice, c->stream));
-  CK(c, cudaMemcpyAsync(c->mm, mm, B, cudaMemcpyHostToDevice, c->stream));
-  CK(c, cudaMemcpyAsync(c->ea, ea, B, cudaMemcpyHostToDevice, c->stream));
+  const double *dp = mapped_addr(pos), *dm = mapped_addr(mm), *de = mapped_addr(ea);
+  const bool direct = dp && dm && de;
+  if (direct) {
+    launch_state_in(c->stream, (int)c->n, dp, dm, de, c->pos, c->mm, c->ea, c->list_valid ? c->xbuild : nullptr, c->L,
+                    &c->sc->flags);
+  } else {
+    CK(c, cudaMemcpyAsync(c->pos, pos, B, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->mm, mm, B, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->ea, ea, B, cudaMemcpyHostToDevice, c->stream));
+  }
   if (reset || !c->have_state) {
     CK(c, cudaMemcpyAsync(c->truePos, c->pos, B, cudaMemcpyDeviceToDevice, c->stream));
     CK(c, cudaMemcpyAsync(c->posRef, c->pos, B, cudaMemcpyDeviceToDevice, c->stream));
   }
   if (c->list_valid) {
     // same particles: rebuild on the next step only if they moved beyond the skin
-    launch_disp_check(c->stream, (int)c->n, c->pos, c->xbuild, c->L, &c->sc->flags);
+    if (!direct) launch_disp_check(c->stream, (int)c->n, c->pos, c->xbuild, c->L, &c->sc->flags);
   } else if (int st = force_rebuild(c)) {
     return st;
   }
@@ -1317,9 +1338,15 @@ int md_step_io(md_ctx* c, const double* pos, const double* mm, const double* ea,
     return st;
   }
   const size_t B = 24 * (size_t)c->n;
-  CK(c, cudaMemcpyAsync(pos_out, c->pos, B, cudaMemcpyDeviceToHost, c->stream));
-  CK(c, cudaMemcpyAsync(mm_out, c->mm, B, cudaMemcpyDeviceToHost, c->stream));
-  CK(c, cudaMemcpyAsync(ea_out, c->ea, B, cudaMemcpyDeviceToHost, c->stream));
+  double *op = mapped_addr(pos_out), *om = mapped_addr(mm_out), *oe = mapped_addr(ea_out);
+  if (op && om && oe) {
+    // mapped host buffers: written by one kernel
+    launch_state_out(c->stream, (int)c->n, c->pos, c->mm, c->ea, op, om, oe);
+  } else {
+    CK(c, cudaMemcpyAsync(pos_out, c->pos, B, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(mm_out, c->mm, B, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(ea_out, c->ea, B, cudaMemcpyDeviceToHost, c->stream));
+  }
   return read_err_word(c);
 }
 

@@ -47,6 +47,13 @@ int launch_step_begin(cudaStream_t st, StepFlags* flags, double half_skin);
 int launch_step_begin_packed(cudaStream_t st, const CellParams* ps, int R, unsigned* anyrb);
 // Raises the displacement since the last build after new positions arrived.
 int launch_disp_check(cudaStream_t st, int n, const double* pos, const double* xbuild, double L, StepFlags* flags);
+// State in from / out to host buffers the device addresses directly
+// (device-side addresses of page-locked mapped memory); state_in also
+// raises maxdisp against xbuild when it is not null.
+int launch_state_in(cudaStream_t st, int n, const double* hpos, const double* hmm, const double* hea, double* pos,
+                    double* mm, double* ea, const double* xbuild, double L, StepFlags* flags);
+int launch_state_out(cudaStream_t st, int n, const double* pos, const double* mm, const double* ea, double* hpos,
+                     double* hmm, double* hea);
 // Cell order (skipped unless the step rebuilds) and the sorted views.
 int launch_cells(cudaStream_t st, const CellParams& p, bool fp64);
 int launch_cells_packed(cudaStream_t st, const CellParams* ps, int R, const Packed& n256, const Packed& sort,

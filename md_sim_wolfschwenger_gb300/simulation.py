@@ -22,6 +22,12 @@ from ._lib import (MD_NOISE_OFF, MD_NOISE_PHILOX, MD_NOISE_UPLOADED, MD_PREC_FP6
 _P = lambda a: None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def _plain(x, size):
+    """A C-contiguous float64 ndarray of `size` values (its address can be
+    handed to the library as it is)."""
+    return type(x) is np.ndarray and x.dtype == np.float64 and x.flags.c_contiguous and x.size == size
+
+
 def _getter_map():
     # getter name -> field (src/configuration.h:98-175)
     m = {"getNumbPart": "numbPart", "getInitConfigRot": "INIT_CONFIG_ROT",
@@ -248,9 +254,16 @@ class Simulation:
         and one synchronisation (md_step_io); `out` may be three (3, N)
         float64 arrays to fill.  Pinned host arrays copy fastest."""
         dt = float(self.config.c.deltaTinit if dt is None else dt)
-        a = [np.ascontiguousarray(x, dtype=np.float64).reshape(3, self.n) for x in state]
-        o = out if out is not None else [np.empty((3, self.n)) for _ in range(3)]
-        self._ck(self.L.md_step_io(self.h, *(_P(x) for x in a), int(nsteps), dt, *(_P(x) for x in o)))
+        n3 = 3 * self.n
+        a = [x if _plain(x, n3) else np.ascontiguousarray(x, dtype=np.float64).reshape(3, self.n) for x in state]
+        if out is None:
+            o = [np.empty((3, self.n)) for _ in range(3)]
+        else:
+            o = out
+            if not all(_plain(x, n3) for x in o):
+                raise ValueError("out must be three C-contiguous float64 arrays of 3N values")
+        self._ck(self.L.md_step_io(self.h, a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data, int(nsteps), dt,
+                                   o[0].ctypes.data, o[1].ctypes.data, o[2].ctypes.data))
         return tuple(o)
 
     def step_adaptive(self, max_steps, dt, t_end=float("inf"), xi=None):
