@@ -383,8 +383,10 @@ __global__ void __launch_bounds__(256) k_obs(ObsParams p) { obs(p); }
 // Stage 2 and the step records in one launch: the block that finishes last
 // (counted in *done) sums the blocks' partials in block order, so the
 // records do not depend on which block that is, and clears the counter.
+// Launched in blocks of kIntOne threads (bounded so: 72 registers and no
+// spills, where the bound of kIntThreads gave 64 and spilled).
 template <typename T>
-__global__ void __launch_bounds__(kIntThreads) k_heun2_obs(IntParams p, ObsParams o, unsigned* done) {
+__global__ void __launch_bounds__(kIntOne) k_heun2_obs(IntParams p, ObsParams o, unsigned* done) {
   heun2<T>(p, blockIdx.x);
   __shared__ int last;
   __threadfence();
