@@ -212,9 +212,14 @@ int md_set_kspace_tiling(md_ctx* ctx, int ring, int waves);
 int md_get_kspace_tiling(const md_ctx* ctx, int* ring, int* waves, int* chunk);
 /* Times candidate cut-offs on the device and sets the fastest that meets
  * the error model; the GPU counterpart of the timing sweep of
- * CompEwaldParams (src/interaction.cpp:185-296).  At the chosen cut-off it
- * also times the k-space engines and the tensor-core tilings
- * (md_set_kspace_tiling) on the mixed path and keeps the fastest. */
+ * CompEwaldParams (src/interaction.cpp:185-296).  Candidates: the cost
+ * model's cut-off (md_ewald_params) and ncand cut-offs from 0.75 to 1.35
+ * times it; each is timed as the median of 5 field + force and field-only
+ * evaluations, each after an L2 flush (a temporary device buffer of twice
+ * the L2), and replaces the cost model's choice only when faster by more
+ * than 3 %.  At the chosen cut-off it times the k-space engines and the
+ * tensor-core tilings (md_set_kspace_tiling) on the mixed path the same way,
+ * the default tiling first. */
 int md_autotune_ewald(md_ctx* ctx, int ncand, double* alpha, double* rc, int64_t* kc,
                       double* best_ms);
 

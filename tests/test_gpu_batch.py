@@ -208,3 +208,12 @@ def test_autotune_cache_hit_for_same_bucket(tmp_path):
     m.tune_cache_clear()
     m.tune_cache_load(p)
     assert m.autotune_ewald_cached(_system(1050, 23), 0.05)[3]
+
+
+def test_autotune_single_candidate_is_the_cost_model_choice():
+    """With one candidate the autotuner times only the cost model's split
+    and keeps it: the same (alpha, rc, kc) as md_ewald_params."""
+    a = _system(2048, 31, phi=0.08, lognormal=True)
+    al, rc, kc, _, _ = a.ewald_params()
+    ta, trc, tkc, ms = a.autotune_ewald(1)
+    assert (ta, trc, tkc) == (al, rc, kc) and ms > 0
