@@ -865,16 +865,25 @@ int md_set_box(md_ctx* c, double lBox) {
   return MD_OK;
 }
 
-// Device-side address of a host buffer that kernels may read and write
-// directly (page-locked memory mapped into the device's address space),
-// else null (pageable memory: copied by the copy engines).
-static double* mapped_addr(const double* h) {
-  cudaPointerAttributes a{};
-  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
-    cudaGetLastError();  // not a CUDA allocation: no sticky error
-    return nullptr;
-  }
-  return a.type == cudaMemoryTypeHost ? (double*)a.devicePointer : nullptr;
+// Device-side address of a host buffer of `bytes` bytes that kernels may
+// read and write directly (page-locked memory mapped into the device's
+// address space, its first and last element in one contiguous mapping),
+// else null (pageable or partly registered memory: copied by the copy
+// engines).
+static double* mapped_addr(const double* h, size_t bytes) {
+  auto dev = [](const void* q) -> char* {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+      cudaGetLastError();  // not a CUDA allocation: no sticky error
+      return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? (char*)a.devicePointer : nullptr;
+  };
+  if (bytes < sizeof(double)) return nullptr;
+  const char* last = (const char*)h + bytes - sizeof(double);
+  char* d0 = dev(h);
+  char* d1 = d0 ? dev(last) : nullptr;
+  return (d1 && d1 - d0 == last - (const char*)h) ? (double*)d0 : nullptr;
 }
 
 // The copies and checks of md_state_upload, queued on the stream.  Mapped
@@ -882,7 +891,7 @@ static double* mapped_addr(const double* h) {
 // check; others through three copies and the check's own launch.
 static int enqueue_upload(md_ctx* c, const double* pos, const double* mm, const double* ea, int reset) {
   const size_t B = 24 * (size_t)c->n;
-  const double *dp = mapped_addr(pos), *dm = mapped_addr(mm), *de = mapped_addr(ea);
+  const double *dp = mapped_addr(pos, B), *dm = mapped_addr(mm, B), *de = mapped_addr(ea, B);
   const bool direct = dp && dm && de;
   if (direct) {
     launch_state_in(c->stream, (int)c->n, dp, dm, de, c->pos, c->mm, c->ea, c->list_valid ? c->xbuild : nullptr, c->L,
@@ -1338,7 +1347,7 @@ int md_step_io(md_ctx* c, const double* pos, const double* mm, const double* ea,
     return st;
   }
   const size_t B = 24 * (size_t)c->n;
-  double *op = mapped_addr(pos_out), *om = mapped_addr(mm_out), *oe = mapped_addr(ea_out);
+  double *op = mapped_addr(pos_out, B), *om = mapped_addr(mm_out, B), *oe = mapped_addr(ea_out, B);
   if (op && om && oe) {
     // mapped host buffers: written by one kernel
     launch_state_out(c->stream, (int)c->n, c->pos, c->mm, c->ea, op, om, oe);

@@ -96,3 +96,33 @@ def test_step_io_with_mapped_host_buffers(prec):
         for x, y in zip(sin, sout):
             x[...] = y
     np.testing.assert_array_equal(a.records(), b.records())
+
+
+def test_step_io_partly_registered_buffer_is_refused():
+    """A host array page-locked over its first part only is not handed to
+    the transfer kernels (both ends must lie in one mapping); the copy
+    engines refuse a range that straddles a registration, so the call
+    reports MD_ERR_CUDA, and the context goes on with proper arrays."""
+    torch = pytest.importorskip("torch")
+    rt = torch.cuda.cudart()
+    ini, g = random_system(700, seed=41, rc_frac=0.3, noise=True)
+    a = gpu_system(ini, g, 1, noise=2, seed=5)
+    b = gpu_system(ini, g, 1, noise=2, seed=5)
+    n = g["n"]
+    raw = np.empty(3 * n + 1024)
+    off = ((-raw.ctypes.data) % 4096) // 8
+    pos = raw[off:off + 3 * n].reshape(3, n)
+    pos[...] = g["pos"]
+    part = (3 * n * 8 // 2) // 4096 * 4096
+    assert part > 0
+    torch.cuda.check_error(rt.cudaHostRegister(pos.ctypes.data, part, 2))  # cudaHostRegisterMapped
+    try:
+        with pytest.raises(MdError):
+            a.step_io((pos, g["mm"], g["ea"]), 2, 1e-12)
+    finally:
+        torch.cuda.check_error(rt.cudaHostUnregister(pos.ctypes.data))
+    out = a.step_io((pos, g["mm"], g["ea"]), 2, 1e-12)
+    b.set_state(g["pos"], g["mm"], g["ea"], reset=False)
+    b.step(2, 1e-12)
+    for x, y in zip(out, b.get_state()):
+        np.testing.assert_array_equal(x, y)
