@@ -221,3 +221,18 @@ def test_tune_cache_file_round_trip(tmp_path):
     rows = [ln.split() for ln in out.read_text().splitlines() if not ln.startswith("#")]
     got = {(int(r[0]), int(r[1])): (float(r[2]), int(r[3]), int(r[4]), int(r[5])) for r in rows}
     assert got == {(30, 5): (0.245, 1, 3, 2), (28, 10): (0.3, 0, -1, 1)}  # rc > 0.5 L is refused
+
+
+def test_step_io_hands_over_only_plain_arrays():
+    """md_step_io receives the state arrays' addresses as they are: only
+    C-contiguous float64 arrays of 3N values qualify (others are copied,
+    or refused as outputs, by Simulation.step_io)."""
+    from md_sim_wolfschwenger_gb300.simulation import _plain
+    n3 = 3 * 10
+    assert _plain(np.zeros((3, 10)), n3)
+    assert _plain(np.zeros(n3), n3)
+    assert not _plain(np.zeros((3, 10), dtype=np.float32), n3)
+    assert not _plain(np.asfortranarray(np.zeros((3, 10))), n3)
+    assert not _plain(np.zeros((3, 20))[:, ::2], n3)
+    assert not _plain(np.zeros((3, 11)), n3)
+    assert not _plain([0.0] * n3, n3)
