@@ -953,11 +953,13 @@ __global__ void __launch_bounds__(1024) k_nbr_scan_packed(const RealParams* __re
   const RealParams p = ps[blockIdx.x];
   nbr_scan(p);
 }
-// the block shape and occupancy of the single-system passes (k_real): 8
-// warps with coating in the field + force pass, otherwise 4 warps at 7
-// (field + force) or 9 (field) blocks per SM
+// the block shape of the single-system passes (k_real): 8 warps with
+// coating in the field + force pass, otherwise 4; 6 (field + force) or 7
+// (field) blocks per SM, one fewer than k_real's 7 / 9: the task loop
+// around the pair loop needs the registers (at 7 / 9 both spilled, and the
+// field sweep ran 1.1 % slower)
 template <bool FULL, bool COAT>
-__global__ void __launch_bounds__(((FULL && COAT) ? kRealWarps : kFieldWarps) * 32, COAT ? 2 : (FULL ? 7 : 9))
+__global__ void __launch_bounds__(((FULL && COAT) ? kRealWarps : kFieldWarps) * 32, COAT ? 2 : (FULL ? 6 : 7))
     k_real_packed(const RealParams* __restrict__ ps, const Task* __restrict__ tk, int ntask, WorkQ* wq) {
   for_tasks<false>(tk, ntask, wq, [&](const Task& t) {
       real_eval<float, FULL, COAT, (FULL && COAT) ? kRealWarps : kFieldWarps>(ps[t.rep], t.blk);
